@@ -1,0 +1,546 @@
+// Device-side geometry for the fused sequential trace.
+//
+// Every function here evaluates one piece of the reference's per-ray
+// arithmetic (src/*.cpp of jmeyers314/batoid) for a descriptor staged in
+// shared memory.  The reference dispatches through C++ virtual calls per ray
+// and per surface; here a surface is a tagged POD record and the dispatch is a
+// warp-uniform switch (all lanes of a warp work on the same stage).
+//
+// Numerical contract: same decision rules as the reference (root choice,
+// failure tests, strict/non-strict comparisons), FP64 throughout.  Where an
+// expression is rearranged (e.g. the Newton step uses the un-normalised normal
+// (-dz/dx, -dz/dy, 1), which leaves dt = ((rP-r).n)/(v.n) unchanged) the
+// results agree with the reference to rounding.
+#pragma once
+#include <stdint.h>
+#include <math.h>
+#include "bt_desc.h"
+
+struct Prog {
+    const bt_stage* stages;
+    const bt_surf* surfs;
+    const bt_medium* media;
+    const bt_obsc* obsc;
+    const double* pool;
+    int nstages;
+    int nmedia;
+};
+
+__device__ __forceinline__ Prog prog_from_blob(const unsigned char* b) {
+    const bt_prog_header* h = reinterpret_cast<const bt_prog_header*>(b);
+    Prog p;
+    p.stages = reinterpret_cast<const bt_stage*>(b + h->off_stages);
+    p.surfs = reinterpret_cast<const bt_surf*>(b + h->off_surfs);
+    p.media = reinterpret_cast<const bt_medium*>(b + h->off_media);
+    p.obsc = reinterpret_cast<const bt_obsc*>(b + h->off_obsc);
+    p.pool = reinterpret_cast<const double*>(b + h->off_pool);
+    p.nstages = h->nstages;
+    p.nmedia = h->nmedia;
+    return p;
+}
+
+// ---------------------------------------------------------------------------
+// Polynomials
+// ---------------------------------------------------------------------------
+
+// 1-D Horner over coefs[0..n), highest power last (src/polynomialSurface.cpp:50-57).
+__device__ __forceinline__ double bt_horner(double x, const double* c, int n) {
+    double r = 0.0;
+    for (int i = n - 1; i >= 0; i--) r = r * x + c[i];
+    return r;
+}
+
+// 2-D Horner: coefs laid out [iy][ix] (row i is the polynomial in y for x^i
+// in the reference's indexing; src/polynomialSurface.cpp:59-66).
+__device__ __forceinline__ double bt_horner2d(double x, double y, const double* c, int nx, int ny) {
+    double r = 0.0;
+    for (int i = ny - 1; i >= 0; i--) r = r * x + bt_horner(y, c + i * nx, nx);
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// Bicubic table (src/table.cpp:42-158)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ double bt_spline1(double x, double v0, double v1, double d0, double d1) {
+    double a = 2 * (v0 - v1) + d0 + d1;
+    double b = 3 * (v1 - v0) - 2 * d0 - d1;
+    return v0 + x * (d0 + x * (b + x * a));
+}
+
+__device__ __forceinline__ double bt_spline1_grad(double x, double v0, double v1, double d0, double d1) {
+    double a = 2 * (v0 - v1) + d0 + d1;
+    double b = 3 * (v1 - v0) - 2 * d0 - d1;
+    return d0 + x * (2 * b + x * 3 * a);
+}
+
+// Evaluates the Hermite bicubic patch value and gradient.  Returns false
+// outside the grid (caller substitutes NaN or 0 per use_nan).
+__device__ __forceinline__ bool bt_table_eval(const bt_surf& s, double x, double y,
+                                              double* val, double* gx, double* gy,
+                                              bool want_val, bool want_grad) {
+    const double x0 = s.p[0], y0 = s.p[1], dx = s.p[2], dy = s.p[3];
+    const int nx = s.n, ny = s.m;
+    const double fx = floor((x - x0) / dx);
+    const double fy = floor((y - y0) / dy);
+    // NaN or out-of-range cell index: outside the grid (src/table.cpp:61-62)
+    if (!(fx >= 0.0) || !(fy >= 0.0) || fx >= (double)(nx - 1) || fy >= (double)(ny - 1)) return false;
+    const int ix = (int)fx, iy = (int)fy;
+    const double xfrac = (x - (x0 + ix * dx)) / dx;
+    const double yfrac = (y - (y0 + iy * dy)) / dy;
+    const size_t plane = (size_t)nx * (size_t)ny;
+    const double* Z = s.tab;
+    const double* ZX = s.tab + plane;
+    const double* ZY = s.tab + 2 * plane;
+    const double* ZXY = s.tab + 3 * plane;
+    const size_t i00 = (size_t)nx * iy + ix, i01 = i00 + 1;
+    const size_t i10 = i00 + nx, i11 = i10 + 1;
+    const double z00 = __ldg(Z + i00), z01 = __ldg(Z + i01), z10 = __ldg(Z + i10), z11 = __ldg(Z + i11);
+    const double zx00 = __ldg(ZX + i00), zx01 = __ldg(ZX + i01), zx10 = __ldg(ZX + i10), zx11 = __ldg(ZX + i11);
+    const double zy00 = __ldg(ZY + i00), zy01 = __ldg(ZY + i01), zy10 = __ldg(ZY + i10), zy11 = __ldg(ZY + i11);
+    const double c00 = __ldg(ZXY + i00), c01 = __ldg(ZXY + i01), c10 = __ldg(ZXY + i10), c11 = __ldg(ZXY + i11);
+    if (want_val) {
+        double v0 = bt_spline1(xfrac, z00, z01, zx00 * dx, zx01 * dx);
+        double v1 = bt_spline1(xfrac, z10, z11, zx10 * dx, zx11 * dx);
+        double d0 = bt_spline1(xfrac, zy00, zy01, c00 * dx, c01 * dx);
+        double d1 = bt_spline1(xfrac, zy10, zy11, c10 * dx, c11 * dx);
+        *val = bt_spline1(yfrac, v0, v1, d0 * dy, d1 * dy);
+    }
+    if (want_grad) {
+        double v0 = bt_spline1_grad(xfrac, z00, z01, zx00 * dx, zx01 * dx);
+        double v1 = bt_spline1_grad(xfrac, z10, z11, zx10 * dx, zx11 * dx);
+        double d0 = bt_spline1_grad(xfrac, zy00, zy01, c00 * dx, c01 * dx);
+        double d1 = bt_spline1_grad(xfrac, zy10, zy11, c10 * dx, c11 * dx);
+        *gx = bt_spline1(yfrac, v0, v1, d0 * dy, d1 * dy) / dx;
+        v0 = bt_spline1_grad(yfrac, z00, z10, zy00 * dy, zy10 * dy);
+        v1 = bt_spline1_grad(yfrac, z01, z11, zy01 * dy, zy11 * dy);
+        d0 = bt_spline1_grad(yfrac, zx00, zx10, c00 * dy, c10 * dy);
+        d1 = bt_spline1_grad(yfrac, zx01, zx11, c01 * dy, c11 * dy);
+        *gy = bt_spline1(xfrac, v0, v1, d0 * dx, d1 * dx) / dy;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Sag and slope of one non-Sum surface.
+//
+// "slope" returns (ux, uy) = (nx/nz, ny/nz) of the reference's unit normal,
+// i.e. the un-normalised normal is (ux, uy, 1).  For every kind except Tilted
+// this is (-dz/dx, -dz/dy); Tilted reproduces the reference's own normal
+// (-tanx, -tany, sqrt(1-tanx^2-tany^2)) (src/tilted.cpp:20-27).
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void bt_leaf_eval(const bt_surf& s, const double* pool,
+                                             double x, double y,
+                                             bool want_sag, bool want_slope,
+                                             double* sag, double* ux, double* uy) {
+    switch (s.kind) {
+    case BT_S_PLANE:
+        if (want_sag) *sag = 0.0;
+        if (want_slope) { *ux = 0.0; *uy = 0.0; }
+        break;
+    case BT_S_TILTED:
+        if (want_sag) *sag = x * s.p[0] + y * s.p[1];
+        if (want_slope) { *ux = -s.p[0] / s.p[2]; *uy = -s.p[1] / s.p[2]; }
+        break;
+    case BT_S_SPHERE: {
+        // src/sphere.cpp:15-48
+        const double R = s.p[0];
+        if (R == 0.0) {
+            if (want_sag) *sag = 0.0;
+            if (want_slope) { *ux = 0.0; *uy = 0.0; }
+            break;
+        }
+        const double r2 = x * x + y * y;
+        if (want_sag) *sag = R * (1 - sqrt(1 - r2 * s.p[3]));
+        if (want_slope) {
+            // (dz/dr)/r = (1/R) / sqrt(1 - (r/R)^2)
+            const double k = s.p[2] / sqrt(1 - r2 * s.p[3]);
+            *ux = -x * k;
+            *uy = -y * k;
+        }
+        break;
+    }
+    case BT_S_PARABOLOID: {
+        // src/paraboloid.cpp:15-37
+        if (s.p[0] == 0.0) {
+            if (want_sag) *sag = 0.0;
+            if (want_slope) { *ux = 0.0; *uy = 0.0; }
+            break;
+        }
+        if (want_sag) *sag = (x * x + y * y) * s.p[2];
+        if (want_slope) { *ux = -x * s.p[1]; *uy = -y * s.p[1]; }
+        break;
+    }
+    case BT_S_QUADRIC:
+    case BT_S_ASPHERE: {
+        // src/quadric.cpp:18-38, src/asphere.cpp:37-74
+        const double R = s.p[0];
+        const double r2 = x * x + y * y;
+        double z = 0.0, k = 0.0;
+        if (R != 0.0) {
+            const double q = sqrt(1. - r2 * s.p[8]);
+            if (want_sag) z = r2 / (R * (1. + q));
+            if (want_slope) k = 1.0 / (R * q);   // (dz/dr)/r of the conic
+        }
+        if (s.kind == BT_S_ASPHERE) {
+            const double* c = pool + s.off;
+            const double* dc = c + s.n;
+            // sum_i c_i r^(2i+2) and sum_i dc_i r^(2i) by Horner in r^2
+            double a = 0.0, da = 0.0;
+            for (int i = s.n - 1; i >= 0; i--) {
+                a = a * r2 + c[i];
+                da = da * r2 + dc[i];
+            }
+            z += a * r2;
+            k += da;
+        }
+        if (want_sag) *sag = z;
+        if (want_slope) { *ux = -x * k; *uy = -y * k; }
+        break;
+    }
+    case BT_S_POLY: {
+        // src/polynomialSurface.cpp:35-48
+        const double xx = x - s.p[0], yy = y - s.p[1];
+        const double* c = pool + s.off;
+        const int nx = s.n, ny = s.m;
+        if (want_sag) *sag = bt_horner2d(xx, yy, c, nx, ny);
+        if (want_slope) {
+            const int gsz = (nx - 1) * (ny - 1);
+            const double* gxc = c + nx * ny;
+            const double* gyc = gxc + gsz;
+            *ux = -bt_horner2d(xx, yy, gxc, nx - 1, ny - 1);
+            *uy = -bt_horner2d(xx, yy, gyc, nx - 1, ny - 1);
+        }
+        break;
+    }
+    case BT_S_BICUBIC: {
+        // src/bicubic.cpp:19-40
+        double v = 0.0, gx = 0.0, gy = 0.0;
+        bool inside = bt_table_eval(s, x, y, &v, &gx, &gy, want_sag, want_slope);
+        if (!inside) {
+            const double fill = (s.p[4] != 0.0) ? (double)NAN : 0.0;
+            v = fill; gx = fill; gy = fill;
+        }
+        if (want_sag) *sag = v;
+        if (want_slope) { *ux = -gx; *uy = -gy; }
+        break;
+    }
+    default:
+        if (want_sag) *sag = NAN;
+        if (want_slope) { *ux = NAN; *uy = NAN; }
+        break;
+    }
+}
+
+// Sag and slope of any surface (Sum adds its children: src/sum.cpp:23-45).
+__device__ __forceinline__ void bt_surf_eval(const Prog& P, int si, double x, double y,
+                                             bool want_sag, bool want_slope,
+                                             double* sag, double* ux, double* uy) {
+    const bt_surf& s = P.surfs[si];
+    if (s.kind != BT_S_SUM) {
+        bt_leaf_eval(s, P.pool, x, y, want_sag, want_slope, sag, ux, uy);
+        return;
+    }
+    double z = 0.0, gx = 0.0, gy = 0.0;
+    for (int c = 0; c < s.n; c++) {
+        double cz = 0.0, cx = 0.0, cy = 0.0;
+        bt_leaf_eval(P.surfs[s.m + c], P.pool, x, y, want_sag, want_slope, &cz, &cx, &cy);
+        z += cz; gx += cx; gy += cy;
+    }
+    if (want_sag) *sag = z;
+    if (want_slope) { *ux = gx; *uy = gy; }
+}
+
+// ---------------------------------------------------------------------------
+// Intersections
+// ---------------------------------------------------------------------------
+
+// Newton / tangent-plane iteration of the reference (src/surface.cpp:22-49).
+// Stops early once an iterate reproduces the previous one exactly: the
+// iteration map is a pure function of dt, so every further iteration would
+// return the same state and the converged result is identical to running all
+// `niter` iterations.  On exit (ux, uy) hold the slope at the final point.
+__device__ __forceinline__ bool bt_newton(const Prog& P, int si,
+                                          double x, double y, double z,
+                                          double vx, double vy, double vz,
+                                          double& dt, int niter,
+                                          double* ux, double* uy) {
+    double rPx = x + vx * dt;
+    double rPy = y + vy * dt;
+    double rPz = z + vz * dt;
+    double sz, gx, gy;
+    bt_surf_eval(P, si, rPx, rPy, true, true, &sz, &gx, &gy);
+    for (int it = 0; it < niter; it++) {
+        // dt = ((rP - r).n) / (v.n) with n ~ (gx, gy, 1)
+        double num = (rPx - x) * gx + (rPy - y) * gy + (sz - z);
+        double den = gx * vx + gy * vy + vz;
+        double dtn = num / den;
+        if (dtn == dt) break;
+        dt = dtn;
+        rPx = x + vx * dt;
+        rPy = y + vy * dt;
+        rPz = z + vz * dt;
+        bt_surf_eval(P, si, rPx, rPy, true, true, &sz, &gx, &gy);
+    }
+    *ux = gx;
+    *uy = gy;
+    return fabs(sz - rPz) < 1e-12;
+}
+
+// Stable quadratic root pair of the reference (src/sphere.cpp:51-58 and
+// siblings).  Returns false for a negative discriminant.
+__device__ __forceinline__ bool bt_quad_roots(double a, double b, double c, double* dt1, double* dt2) {
+    double disc = b * b - 4 * a * c;
+    if (disc < 0) return false;
+    double r1;
+    if (b > 0) r1 = (-b - sqrt(disc)) / (2 * a);
+    else r1 = 2 * c / (-b + sqrt(disc));
+    *dt1 = r1;
+    *dt2 = c / (a * r1);
+    return true;
+}
+
+// Analytic or iterative time-to-intersect of a non-Sum surface.  `slope_ok`
+// is set when (ux, uy) already hold the slope at the intersection.
+__device__ __forceinline__ bool bt_leaf_tti(const Prog& P, int si,
+                                            double x, double y, double z,
+                                            double vx, double vy, double vz,
+                                            double& dt, int niter,
+                                            double* ux, double* uy, bool* slope_ok) {
+    const bt_surf& s = P.surfs[si];
+    *slope_ok = false;
+    switch (s.kind) {
+    case BT_S_PLANE:
+        // src/plane.cpp:23-30
+        if (vz == 0) return false;
+        dt = -z / vz;
+        return true;
+    case BT_S_TILTED: {
+        // src/tilted.cpp:29-37
+        double num = z - x * s.p[0] - y * s.p[1];
+        double den = vx * s.p[0] + vy * s.p[1] - vz;
+        if (den == 0) return false;
+        dt = num / den;
+        return true;
+    }
+    case BT_S_SPHERE: {
+        // src/sphere.cpp:36-67
+        const double R = s.p[0];
+        double vr2 = vx * vx + vy * vy;
+        double vz2 = vz * vz;
+        double vrr0 = vx * x + vy * y;
+        double r02 = x * x + y * y;
+        double z0 = z - R;
+        double a = vz2 + vr2;
+        double b = 2 * vz * z0 + 2 * vrr0;
+        double c = z0 * z0 - s.p[1] + r02;
+        double t1, t2;
+        if (!bt_quad_roots(a, b, c, &t1, &t2)) return false;
+        dt = (vz * R < 0) ? fmax(t1, t2) : fmin(t1, t2);
+        return true;
+    }
+    case BT_S_PARABOLOID: {
+        // src/paraboloid.cpp:38-71
+        double a = (vx * vx + vy * vy) * s.p[2];
+        double b = (x * vx + y * vy) * s.p[1] - vz;
+        double c = (x * x + y * y) * s.p[2] - z;
+        if (a == 0) { dt = -c / b; return true; }
+        double t1, t2;
+        if (!bt_quad_roots(a, b, c, &t1, &t2)) return false;
+        dt = (vz * s.p[0] < 0) ? fmax(t1, t2) : fmin(t1, t2);
+        return true;
+    }
+    case BT_S_QUADRIC:
+    case BT_S_ASPHERE: {
+        // src/quadric.cpp:41-71; Asphere starts Newton from it (src/asphere.cpp:76-85)
+        double z0 = z - s.p[6];
+        double vrr0 = vx * x + vy * y;
+        double a = vz * vz + (vx * vx + vy * vy) * s.p[5];
+        double b = 2 * (vz * z0 + vrr0 * s.p[5]);
+        double c = z0 * z0 - s.p[7] + (x * x + y * y) * s.p[5];
+        double t1, t2;
+        if (!bt_quad_roots(a, b, c, &t1, &t2)) return false;
+        double z1 = z + vz * t1;
+        double z2 = z + vz * t2;
+        dt = (fabs(z1) < fabs(z2)) ? t1 : t2;
+        if (s.kind == BT_S_QUADRIC) return true;
+        *slope_ok = true;
+        return bt_newton(P, si, x, y, z, vx, vy, vz, dt, niter, ux, uy);
+    }
+    default:
+        // PolynomialSurface, Bicubic: generic Newton from the given dt
+        *slope_ok = true;
+        return bt_newton(P, si, x, y, z, vx, vy, vz, dt, niter, ux, uy);
+    }
+}
+
+__device__ __forceinline__ bool bt_surf_tti(const Prog& P, int si,
+                                            double x, double y, double z,
+                                            double vx, double vy, double vz,
+                                            double& dt, int niter,
+                                            double* ux, double* uy, bool* slope_ok) {
+    const bt_surf& s = P.surfs[si];
+    if (s.kind != BT_S_SUM)
+        return bt_leaf_tti(P, si, x, y, z, vx, vy, vz, dt, niter, ux, uy, slope_ok);
+    // Sum: first child's own solve as the starting point, then Newton on the
+    // sum (src/sum.cpp:47-56).
+    bool dummy;
+    if (!bt_leaf_tti(P, s.m, x, y, z, vx, vy, vz, dt, niter, ux, uy, &dummy)) return false;
+    *slope_ok = true;
+    return bt_newton(P, si, x, y, z, vx, vy, vz, dt, niter, ux, uy);
+}
+
+// Unit normal at (x, y) from the slope form.
+__device__ __forceinline__ void bt_normal_from_slope(double ux, double uy, double* nx, double* ny, double* nz) {
+    double k = 1.0 / sqrt(ux * ux + uy * uy + 1.0);
+    *nx = ux * k;
+    *ny = uy * k;
+    *nz = k;
+}
+
+// The reference's exact normal for surfaces where the slope form and the
+// reference's expression agree only in exact arithmetic, evaluated fresh.
+__device__ __forceinline__ void bt_surf_normal(const Prog& P, int si, double x, double y,
+                                               double* nx, double* ny, double* nz) {
+    const bt_surf& s = P.surfs[si];
+    if (s.kind == BT_S_TILTED) {
+        *nx = -s.p[0]; *ny = -s.p[1]; *nz = s.p[2];
+        return;
+    }
+    if (s.kind == BT_S_PLANE) { *nx = 0.0; *ny = 0.0; *nz = 1.0; return; }
+    double ux, uy, dummy;
+    bt_surf_eval(P, si, x, y, false, true, &dummy, &ux, &uy);
+    bt_normal_from_slope(ux, uy, nx, ny, nz);
+}
+
+// ---------------------------------------------------------------------------
+// Media (src/medium.cpp)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ double bt_getN(const Prog& P, int mi, double w) {
+    const bt_medium& m = P.media[mi];
+    switch (m.kind) {
+    case BT_M_CONST:
+        return m.p[0];
+    case BT_M_TABLE: {
+        // linear search + interpolation, NaN outside (src/medium.cpp:89-105)
+        const double* args = P.pool + m.off;
+        const double* vals = args + m.n;
+        if (w < args[0]) return NAN;
+        if (w > args[m.n - 1]) return NAN;
+        int u;
+        for (u = 1; u < m.n; u++)
+            if (w < args[u]) break;
+        if (u >= m.n) u = m.n - 1;  // w == last arg
+        double out = (w - args[u - 1]);
+        out *= (vals[u] - vals[u - 1]);
+        out /= (args[u] - args[u - 1]);
+        out += vals[u - 1];
+        return out;
+    }
+    case BT_M_SELLMEIER: {
+        // src/medium.cpp:145-149, wavelength in microns squared
+        double x = w * w * 1e12;
+        return sqrt(1.0 + m.p[0] * x / (x - m.p[3]) + m.p[1] * x / (x - m.p[4]) + m.p[2] * x / (x - m.p[5]));
+    }
+    case BT_M_SUMITA: {
+        // src/medium.cpp:186-191
+        double x = w * w * 1e12;
+        double y = 1. / x;
+        return sqrt(m.p[0] + m.p[1] * x + y * (m.p[2] + y * (m.p[3] + y * (m.p[4] + y * m.p[5]))));
+    }
+    case BT_M_AIR: {
+        // Edlen / Filippenko (src/medium.cpp:237-245)
+        const double P_ = m.p[0], T = m.p[1], W = m.p[2];
+        double s2 = 1e-12 / (w * w);
+        double nm1 = (64.328 + (29498.1 / (146.0 - s2)) + (255.4 / (41.0 - s2))) * 1.e-6;
+        nm1 *= P_ * (1.0 + (1.049 - 0.0157 * T) * 1.e-6 * P_) / (720.883 * (1.0 + 0.003661 * T));
+        nm1 -= (0.0624 - 0.000680 * s2) / (1.0 + 0.003661 * T) * W * 1.e-6;
+        return 1 + nm1;
+    }
+    default:
+        return NAN;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Obscurations (src/obscuration.cpp), evaluated as a postfix program.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ bool bt_polygon_contains(const double* xp, const double* yp, int n, double x, double y) {
+    // even-odd crossing test (src/obscuration.cpp:201-225)
+    double x1 = xp[0], y1 = yp[0];
+    double xinters = 0.0;
+    bool inside = false;
+    for (int i = 1; i <= n; i++) {
+        int k = (i == n) ? 0 : i;
+        double x2 = xp[k], y2 = yp[k];
+        if (y > fmin(y1, y2)) {
+            if (y <= fmax(y1, y2)) {
+                if (x <= fmax(x1, x2)) {
+                    if (y1 != y2) xinters = (y - y1) * (x2 - x1) / (y2 - y1) + x1;
+                    if (x1 == x2 || x <= xinters) inside = !inside;
+                }
+            }
+        }
+        x1 = x2;
+        y1 = y2;
+    }
+    return inside;
+}
+
+__device__ __forceinline__ bool bt_obsc_run(const Prog& P, int begin, int end, double x, double y) {
+    uint32_t stack = 0;  // bit k = entry k
+    int sp = 0;
+    for (int k = begin; k < end; k++) {
+        const bt_obsc& o = P.obsc[k];
+        bool v = false;
+        switch (o.op) {
+        case BT_O_CIRCLE:
+            v = hypot(x - o.p[1], y - o.p[2]) < o.p[0];
+            break;
+        case BT_O_ANNULUS: {
+            double h = hypot(x - o.p[2], y - o.p[3]);
+            v = (o.p[0] <= h) && (h < o.p[1]);
+            break;
+        }
+        case BT_O_RECT: {
+            double xp = (x - o.p[2]) * o.p[5] + (y - o.p[3]) * o.p[4];
+            double yp = -(x - o.p[2]) * o.p[4] + (y - o.p[3]) * o.p[5];
+            v = (xp > -o.p[0] / 2 && xp < o.p[0] / 2 && yp > -o.p[1] / 2 && yp < o.p[1] / 2);
+            break;
+        }
+        case BT_O_RAY: {
+            double xp = (x - o.p[1]) * o.p[4] + (y - o.p[2]) * o.p[3];
+            double yp = -(x - o.p[1]) * o.p[3] + (y - o.p[2]) * o.p[4];
+            v = (xp > 0.0 && yp > -o.p[0] / 2 && yp < o.p[0] / 2);
+            break;
+        }
+        case BT_O_POLYGON:
+            v = bt_polygon_contains(P.pool + o.off, P.pool + o.off + o.n, o.n, x, y);
+            break;
+        case BT_O_NEGATION:
+            sp--;
+            v = !((stack >> sp) & 1u);
+            break;
+        case BT_O_UNION: {
+            bool acc = false;
+            for (int j = 0; j < o.n; j++) { sp--; acc |= (bool)((stack >> sp) & 1u); }
+            v = acc;
+            break;
+        }
+        case BT_O_INTERSECTION: {
+            bool acc = true;
+            for (int j = 0; j < o.n; j++) { sp--; acc &= (bool)((stack >> sp) & 1u); }
+            v = acc;
+            break;
+        }
+        default:
+            break;
+        }
+        stack = (stack & ~(1u << sp)) | ((uint32_t)v << sp);
+        sp++;
+    }
+    return sp > 0 ? (bool)((stack >> (sp - 1)) & 1u) : false;
+}

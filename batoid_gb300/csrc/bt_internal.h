@@ -1,0 +1,72 @@
+// Internal declarations shared by the C-ABI translation unit and the kernel
+// translation units.  Not part of the public interface.
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime.h>
+#include "bt_desc.h"
+
+#define BT_MAX_STAGES 64
+
+// Device view of a ray bundle (same fields as bt_rayvector).
+struct RV {
+    double* x;
+    double* y;
+    double* z;
+    double* vx;
+    double* vy;
+    double* vz;
+    double* t;
+    double* w;
+    double* f;
+    uint8_t* vig;
+    uint8_t* fail;
+    long long n;
+};
+
+struct SnapSet {
+    RV s[BT_MAX_STAGES];
+};
+
+// Status word written by kernels whose bounded waits expire (0 = fine).
+// Read and cleared by bt_check_device_status().
+cudaError_t bt_read_device_status(int* status, cudaStream_t stream);
+
+// trace.cu
+cudaError_t bt_launch_trace(const unsigned char* d_blob, int blob_bytes, const RV& in, const RV& out,
+                            const SnapSet* snaps, int nsnaps, int niter, cudaStream_t stream);
+cudaError_t bt_launch_surface_eval(const unsigned char* d_blob, int blob_bytes, const double* x,
+                                   const double* y, double* sag, double* normal, long long n,
+                                   cudaStream_t stream);
+cudaError_t bt_launch_getN(const unsigned char* d_blob, int blob_bytes, const double* w, double* out,
+                           long long n, cudaStream_t stream);
+cudaError_t bt_launch_obsc(const unsigned char* d_blob, int blob_bytes, const double* x, const double* y,
+                           uint8_t* out, const RV* rv, long long n, cudaStream_t stream);
+
+// rayvec.cu
+cudaError_t bt_launch_transform_rv(const double dr[3], const double drot[9], const RV& rv, bool forward,
+                                   cudaStream_t stream);
+cudaError_t bt_launch_transform_arrays(const double dr[3], const double drot[9], double* x, double* y,
+                                       double* z, long long n, bool forward, cudaStream_t stream);
+cudaError_t bt_launch_finish_parallel(const double dr[3], const double drot[9], const double vv[3],
+                                      double* x, double* y, double* z, long long n, cudaStream_t stream);
+cudaError_t bt_launch_position_at_time(const RV& rv, double t, double* xo, double* yo, double* zo,
+                                       cudaStream_t stream);
+cudaError_t bt_launch_propagate(const RV& rv, double t, cudaStream_t stream);
+cudaError_t bt_launch_phase(const RV& rv, double x, double y, double z, double t, double* out,
+                            bool amplitude, cudaStream_t stream);
+cudaError_t bt_launch_sum_amplitude(const RV& rv, double x, double y, double z, double t, bool ignore_vig,
+                                    double* d_out2, cudaStream_t stream);
+cudaError_t bt_launch_rv_equal(const RV& a, const RV& b, int* d_flag, cudaStream_t stream);
+
+// huygens.cu
+cudaError_t bt_launch_huygens(const RV& rv, double px, double py, double pz, const double lat[4], int na,
+                              int nb, double t0, bool ignore_vig, double* out_re, double* out_im,
+                              cudaStream_t stream);
+
+// fit.cu
+cudaError_t bt_launch_zk_normal(const double* x, const double* y, const double* v, const long long* offsets,
+                                int nfits, const double* basis, int jmax, int side, double* G, double* b,
+                                cudaStream_t stream);
+
+int bt_sm_count();

@@ -1,0 +1,1085 @@
+// C-ABI entry points (include/batoid_gb300.h): host-side objects for
+// surfaces, media, obscurations and coatings, the packer that flattens them
+// into a program blob (bt_desc.h), and the launch wrappers.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+#include <string>
+#include <vector>
+#include <mutex>
+#include "../../include/batoid_gb300.h"
+#include "bt_internal.h"
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+static int cuda_fail(cudaError_t e, const char* where) {
+    return fail(BT_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CUDA_TRY(expr, where)                     \
+    do {                                          \
+        cudaError_t _e = (expr);                  \
+        if (_e != cudaSuccess) return cuda_fail(_e, where); \
+    } while (0)
+
+extern "C" const char* bt_last_error(void) { return g_err.c_str(); }
+extern "C" int bt_version(void) { return 1; }
+
+extern "C" int bt_device_sm_count(int* out) {
+    if (!out) return fail(BT_ERR_ARG, "null out");
+    *out = bt_sm_count();
+    return BT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// host objects
+// ---------------------------------------------------------------------------
+
+// A bicubic table keeps its host copy and is uploaded to device memory on
+// first use by a kernel (so surfaces can be built without touching the GPU).
+struct bt_table {
+    double x0, y0, dx, dy;
+    size_t nx, ny;
+    int use_nan;
+    std::vector<double> host;  // 4*nx*ny doubles: z, dzdx, dzdy, d2zdxdy
+    double* d_tab = nullptr;
+    std::mutex mu;
+};
+
+// A surface is a small list of descriptors: recs[0] is the root; a Sum's
+// children follow it (root.m is the index of the first child, relative).
+// pool offsets are relative to `pool`.  tables[i] is the bicubic table of
+// recs[i] (nullptr otherwise); tables are shared, not owned.
+struct bt_surface {
+    std::vector<bt_surf> recs;
+    std::vector<double> pool;
+    std::vector<bt_table*> tables;
+};
+
+static cudaError_t table_device(bt_table* t, const double** out) {
+    std::lock_guard<std::mutex> lock(t->mu);
+    if (!t->d_tab) {
+        cudaError_t e = cudaMalloc((void**)&t->d_tab, t->host.size() * sizeof(double));
+        if (e != cudaSuccess) { t->d_tab = nullptr; return e; }
+        e = cudaMemcpy(t->d_tab, t->host.data(), t->host.size() * sizeof(double), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { cudaFree(t->d_tab); t->d_tab = nullptr; return e; }
+    }
+    *out = t->d_tab;
+    return cudaSuccess;
+}
+
+struct bt_medium_h {
+    bt_medium rec;
+    std::vector<double> pool;
+};
+
+// Postfix obscuration program.
+struct bt_obscuration {
+    std::vector<bt_obsc> ops;
+    std::vector<double> pool;
+};
+
+struct bt_coating {
+    double R, T;
+};
+
+static bt_surf blank_surf(int kind) {
+    bt_surf s;
+    memset(&s, 0, sizeof(s));
+    s.kind = kind;
+    return s;
+}
+
+static void push_rec(bt_surface* s, const bt_surf& r, bt_table* t = nullptr) {
+    s->recs.push_back(r);
+    s->tables.push_back(t);
+}
+
+template <class T>
+static int make_out(T** out, T* obj) {
+    if (!out) {
+        delete obj;
+        return fail(BT_ERR_ARG, "null output handle");
+    }
+    *out = obj;
+    return BT_OK;
+}
+
+extern "C" int bt_plane_create(bt_surface** out) {
+    bt_surface* s = new bt_surface;
+    push_rec(s, blank_surf(BT_S_PLANE));
+    return make_out(out, s);
+}
+
+extern "C" int bt_tilted_create(double tanx, double tany, bt_surface** out) {
+    bt_surface* s = new bt_surface;
+    bt_surf r = blank_surf(BT_S_TILTED);
+    r.p[0] = tanx;
+    r.p[1] = tany;
+    r.p[2] = sqrt(1 - tanx * tanx - tany * tany);
+    push_rec(s, r);
+    return make_out(out, s);
+}
+
+extern "C" int bt_sphere_create(double R, bt_surface** out) {
+    bt_surface* s = new bt_surface;
+    bt_surf r = blank_surf(BT_S_SPHERE);
+    // src/sphere.cpp:10-13
+    r.p[0] = R;
+    r.p[1] = R * R;
+    r.p[2] = 1. / R;
+    r.p[3] = 1. / R / R;
+    push_rec(s, r);
+    return make_out(out, s);
+}
+
+extern "C" int bt_paraboloid_create(double R, bt_surface** out) {
+    bt_surface* s = new bt_surface;
+    bt_surf r = blank_surf(BT_S_PARABOLOID);
+    // src/paraboloid.cpp:10-12
+    r.p[0] = R;
+    r.p[1] = 1. / R;
+    r.p[2] = 1. / 2 / R;
+    push_rec(s, r);
+    return make_out(out, s);
+}
+
+static void fill_quadric(bt_surf& r, double R, double conic) {
+    // src/quadric.cpp:9-14
+    const double cp1 = conic + 1;
+    r.p[0] = R;
+    r.p[1] = conic;
+    r.p[2] = R * R;
+    r.p[3] = 1. / R / R;
+    r.p[4] = cp1;
+    r.p[5] = 1. / cp1;
+    r.p[6] = R / cp1;
+    r.p[7] = R * R / cp1 / cp1;
+    r.p[8] = cp1 / R / R;
+}
+
+extern "C" int bt_quadric_create(double R, double conic, bt_surface** out) {
+    bt_surface* s = new bt_surface;
+    bt_surf r = blank_surf(BT_S_QUADRIC);
+    fill_quadric(r, R, conic);
+    push_rec(s, r);
+    return make_out(out, s);
+}
+
+extern "C" int bt_asphere_create(double R, double conic, const double* coefs, size_t n, bt_surface** out) {
+    if (n > 0 && !coefs) return fail(BT_ERR_ARG, "asphere: null coefs");
+    bt_surface* s = new bt_surface;
+    bt_surf r = blank_surf(BT_S_ASPHERE);
+    fill_quadric(r, R, conic);
+    r.n = (int32_t)n;
+    r.off = 0;
+    s->pool.assign(coefs, coefs + n);
+    // dz/dr coefficients: entry j multiplies r^(2j+1) with factor 2(j+1)
+    // (src/asphere.cpp:10-16)
+    for (size_t j = 0; j < n; j++) s->pool.push_back(coefs[j] * (double)(2 * (j + 1)));
+    push_rec(s, r);
+    return make_out(out, s);
+}
+
+extern "C" int bt_polynomial_create(const double* coefs, const double* gradx, const double* grady,
+                                    double xorigin, double yorigin, size_t xsize, size_t ysize,
+                                    bt_surface** out) {
+    if (xsize < 1 || ysize < 1 || !coefs) return fail(BT_ERR_ARG, "polynomial: bad coefficient array");
+    const size_t gsz = (xsize - 1) * (ysize - 1);
+    if (gsz > 0 && (!gradx || !grady)) return fail(BT_ERR_ARG, "polynomial: null gradient arrays");
+    bt_surface* s = new bt_surface;
+    bt_surf r = blank_surf(BT_S_POLY);
+    r.p[0] = xorigin;
+    r.p[1] = yorigin;
+    r.n = (int32_t)xsize;
+    r.m = (int32_t)ysize;
+    r.off = 0;
+    s->pool.assign(coefs, coefs + xsize * ysize);
+    if (gsz > 0) {
+        s->pool.insert(s->pool.end(), gradx, gradx + gsz);
+        s->pool.insert(s->pool.end(), grady, grady + gsz);
+    }
+    push_rec(s, r);
+    return make_out(out, s);
+}
+
+extern "C" int bt_table_create(double x0, double y0, double dx, double dy, const double* z, const double* dzdx,
+                               const double* dzdy, const double* d2zdxdy, size_t nx, size_t ny, int use_nan,
+                               bt_table** out) {
+    if (!z || !dzdx || !dzdy || !d2zdxdy || nx < 2 || ny < 2) return fail(BT_ERR_ARG, "table: bad arrays");
+    bt_table* t = new bt_table;
+    t->x0 = x0; t->y0 = y0; t->dx = dx; t->dy = dy;
+    t->nx = nx; t->ny = ny; t->use_nan = use_nan ? 1 : 0;
+    const size_t plane = nx * ny;
+    const double* src[4] = {z, dzdx, dzdy, d2zdxdy};
+    t->host.reserve(4 * plane);
+    for (int k = 0; k < 4; k++) t->host.insert(t->host.end(), src[k], src[k] + plane);
+    return make_out(out, t);
+}
+
+extern "C" void bt_table_destroy(bt_table* t) {
+    if (!t) return;
+    if (t->d_tab) cudaFree(t->d_tab);
+    delete t;
+}
+
+extern "C" int bt_bicubic_create(const bt_table* t, bt_surface** out) {
+    if (!t) return fail(BT_ERR_ARG, "bicubic: null table");
+    bt_surface* s = new bt_surface;
+    bt_surf r = blank_surf(BT_S_BICUBIC);
+    r.p[0] = t->x0; r.p[1] = t->y0; r.p[2] = t->dx; r.p[3] = t->dy;
+    r.p[4] = t->use_nan ? 1.0 : 0.0;
+    r.n = (int32_t)t->nx;
+    r.m = (int32_t)t->ny;
+    r.tab = nullptr;  // resolved to the device copy when packed into a program
+    push_rec(s, r, const_cast<bt_table*>(t));
+    return make_out(out, s);
+}
+
+extern "C" int bt_sum_create(const bt_surface* const* surfaces, size_t n, bt_surface** out) {
+    if (!surfaces || n < 1) return fail(BT_ERR_ARG, "sum: no surfaces");
+    if (n > BT_MAX_SUM_CHILDREN) return fail(BT_ERR_UNSUPPORTED, "sum: too many surfaces");
+    for (size_t i = 0; i < n; i++) {
+        if (!surfaces[i]) return fail(BT_ERR_ARG, "sum: null surface");
+        if (surfaces[i]->recs[0].kind == BT_S_SUM)
+            return fail(BT_ERR_UNSUPPORTED, "sum: nested Sum surfaces are not supported");
+    }
+    bt_surface* s = new bt_surface;
+    bt_surf root = blank_surf(BT_S_SUM);
+    root.n = (int32_t)n;
+    root.m = 1;
+    push_rec(s, root);
+    for (size_t i = 0; i < n; i++) {
+        bt_surf c = surfaces[i]->recs[0];
+        c.off += (int32_t)s->pool.size();
+        s->pool.insert(s->pool.end(), surfaces[i]->pool.begin(), surfaces[i]->pool.end());
+        push_rec(s, c, surfaces[i]->tables[0]);
+    }
+    return make_out(out, s);
+}
+
+extern "C" void bt_surface_destroy(bt_surface* s) { delete s; }
+
+// media ---------------------------------------------------------------------
+
+static bt_medium_h* new_medium(int kind) {
+    bt_medium_h* m = new bt_medium_h;
+    memset(&m->rec, 0, sizeof(m->rec));
+    m->rec.kind = kind;
+    return m;
+}
+
+extern "C" int bt_const_medium_create(double n, bt_medium_h** out) {
+    bt_medium_h* m = new_medium(BT_M_CONST);
+    m->rec.p[0] = n;
+    return make_out(out, m);
+}
+
+extern "C" int bt_table_medium_create(const double* w, const double* ns, size_t n, bt_medium_h** out) {
+    if (!w || !ns || n < 1) return fail(BT_ERR_ARG, "table medium: bad arrays");
+    bt_medium_h* m = new_medium(BT_M_TABLE);
+    m->rec.n = (int32_t)n;
+    m->pool.assign(w, w + n);
+    m->pool.insert(m->pool.end(), ns, ns + n);
+    return make_out(out, m);
+}
+
+extern "C" int bt_sellmeier_medium_create(double B1, double B2, double B3, double C1, double C2, double C3,
+                                          bt_medium_h** out) {
+    bt_medium_h* m = new_medium(BT_M_SELLMEIER);
+    double p[6] = {B1, B2, B3, C1, C2, C3};
+    memcpy(m->rec.p, p, sizeof(p));
+    return make_out(out, m);
+}
+
+extern "C" int bt_sumita_medium_create(double A0, double A1, double A2, double A3, double A4, double A5,
+                                       bt_medium_h** out) {
+    bt_medium_h* m = new_medium(BT_M_SUMITA);
+    double p[6] = {A0, A1, A2, A3, A4, A5};
+    memcpy(m->rec.p, p, sizeof(p));
+    return make_out(out, m);
+}
+
+extern "C" int bt_air_create(double pressure, double temperature, double h2o_pressure, bt_medium_h** out) {
+    bt_medium_h* m = new_medium(BT_M_AIR);
+    // SI inputs converted as src/medium.cpp:230-233
+    m->rec.p[0] = pressure * 7.50061683;
+    m->rec.p[1] = temperature - 273.15;
+    m->rec.p[2] = h2o_pressure * 7.50061683;
+    return make_out(out, m);
+}
+
+extern "C" void bt_medium_destroy(bt_medium_h* m) { delete m; }
+
+// obscurations --------------------------------------------------------------
+
+static bt_obsc blank_op(int op) {
+    bt_obsc o;
+    memset(&o, 0, sizeof(o));
+    o.op = op;
+    return o;
+}
+
+static bt_obscuration* leaf_obsc(const bt_obsc& o) {
+    bt_obscuration* r = new bt_obscuration;
+    r->ops.push_back(o);
+    return r;
+}
+
+extern "C" int bt_obsc_circle_create(double radius, double x0, double y0, bt_obscuration** out) {
+    bt_obsc o = blank_op(BT_O_CIRCLE);
+    o.p[0] = radius; o.p[1] = x0; o.p[2] = y0;
+    return make_out(out, leaf_obsc(o));
+}
+
+extern "C" int bt_obsc_annulus_create(double inner, double outer, double x0, double y0, bt_obscuration** out) {
+    bt_obsc o = blank_op(BT_O_ANNULUS);
+    o.p[0] = inner; o.p[1] = outer; o.p[2] = x0; o.p[3] = y0;
+    return make_out(out, leaf_obsc(o));
+}
+
+extern "C" int bt_obsc_rectangle_create(double width, double height, double x0, double y0, double theta,
+                                        bt_obscuration** out) {
+    bt_obsc o = blank_op(BT_O_RECT);
+    o.p[0] = width; o.p[1] = height; o.p[2] = x0; o.p[3] = y0;
+    o.p[4] = sin(theta); o.p[5] = cos(theta);  // src/obscuration.cpp:110-113
+    return make_out(out, leaf_obsc(o));
+}
+
+extern "C" int bt_obsc_ray_create(double width, double theta, double x0, double y0, bt_obscuration** out) {
+    bt_obsc o = blank_op(BT_O_RAY);
+    o.p[0] = width; o.p[1] = x0; o.p[2] = y0;
+    o.p[3] = sin(theta); o.p[4] = cos(theta);  // src/obscuration.cpp:148-151
+    return make_out(out, leaf_obsc(o));
+}
+
+extern "C" int bt_obsc_polygon_create(const double* xs, const double* ys, size_t n, bt_obscuration** out) {
+    if (!xs || !ys || n < 1) return fail(BT_ERR_ARG, "polygon: bad vertex arrays");
+    bt_obsc o = blank_op(BT_O_POLYGON);
+    o.n = (int32_t)n;
+    o.off = 0;
+    bt_obscuration* r = leaf_obsc(o);
+    r->pool.assign(xs, xs + n);
+    r->pool.insert(r->pool.end(), ys, ys + n);
+    return make_out(out, r);
+}
+
+static void append_obsc(bt_obscuration* dst, const bt_obscuration* src) {
+    const int32_t base = (int32_t)dst->pool.size();
+    for (bt_obsc o : src->ops) {
+        if (o.op == BT_O_POLYGON) o.off += base;
+        dst->ops.push_back(o);
+    }
+    dst->pool.insert(dst->pool.end(), src->pool.begin(), src->pool.end());
+}
+
+// Maximum operand-stack depth of a postfix program.
+static int obsc_depth(const bt_obscuration* o) {
+    int sp = 0, mx = 0;
+    for (const bt_obsc& op : o->ops) {
+        if (op.op == BT_O_NEGATION) sp -= 1;
+        else if (op.op == BT_O_UNION || op.op == BT_O_INTERSECTION) sp -= op.n;
+        sp += 1;
+        if (sp > mx) mx = sp;
+    }
+    return mx;
+}
+
+extern "C" int bt_obsc_negation_create(const bt_obscuration* original, bt_obscuration** out) {
+    if (!original) return fail(BT_ERR_ARG, "negation: null original");
+    bt_obscuration* r = new bt_obscuration;
+    append_obsc(r, original);
+    r->ops.push_back(blank_op(BT_O_NEGATION));
+    return make_out(out, r);
+}
+
+static int compound_obsc(int op, const bt_obscuration* const* items, size_t n, bt_obscuration** out) {
+    if (!items || n < 1) return fail(BT_ERR_ARG, "compound obscuration: no items");
+    bt_obscuration* r = new bt_obscuration;
+    for (size_t i = 0; i < n; i++) {
+        if (!items[i]) { delete r; return fail(BT_ERR_ARG, "compound obscuration: null item"); }
+        append_obsc(r, items[i]);
+    }
+    bt_obsc o = blank_op(op);
+    o.n = (int32_t)n;
+    r->ops.push_back(o);
+    if (obsc_depth(r) > BT_MAX_OBSC_STACK) {
+        delete r;
+        return fail(BT_ERR_UNSUPPORTED, "obscuration expression too deep");
+    }
+    return make_out(out, r);
+}
+
+extern "C" int bt_obsc_union_create(const bt_obscuration* const* items, size_t n, bt_obscuration** out) {
+    return compound_obsc(BT_O_UNION, items, n, out);
+}
+
+extern "C" int bt_obsc_intersection_create(const bt_obscuration* const* items, size_t n, bt_obscuration** out) {
+    return compound_obsc(BT_O_INTERSECTION, items, n, out);
+}
+
+extern "C" void bt_obsc_destroy(bt_obscuration* o) { delete o; }
+
+extern "C" int bt_simple_coating_create(double reflectivity, double transmissivity, bt_coating** out) {
+    bt_coating* c = new bt_coating;
+    c->R = reflectivity;
+    c->T = transmissivity;
+    return make_out(out, c);
+}
+
+extern "C" void bt_coating_destroy(bt_coating* c) { delete c; }
+
+// ---------------------------------------------------------------------------
+// program packing
+// ---------------------------------------------------------------------------
+
+struct ProgBuilder {
+    std::vector<bt_stage> stages;
+    std::vector<bt_surf> surfs;
+    std::vector<bt_medium> media;
+    std::vector<const bt_medium_h*> media_src;
+    std::vector<bt_obsc> obsc;
+    std::vector<double> pool;
+
+    // Appends a surface's descriptors; returns the root index or -1 (error
+    // message set) when a bicubic table cannot be placed in device memory.
+    int add_surface(const bt_surface* s) {
+        const int32_t base_rec = (int32_t)surfs.size();
+        const int32_t base_pool = (int32_t)pool.size();
+        for (size_t i = 0; i < s->recs.size(); i++) {
+            bt_surf r = s->recs[i];
+            r.off += base_pool;
+            if (r.kind == BT_S_SUM) r.m += base_rec;
+            if (r.kind == BT_S_BICUBIC) {
+                cudaError_t e = table_device(s->tables[i], &r.tab);
+                if (e != cudaSuccess) {
+                    cuda_fail(e, "bicubic table upload");
+                    return -1;
+                }
+            }
+            surfs.push_back(r);
+        }
+        pool.insert(pool.end(), s->pool.begin(), s->pool.end());
+        return base_rec;
+    }
+
+    int add_medium(const bt_medium_h* m) {
+        for (size_t i = 0; i < media_src.size(); i++)
+            if (media_src[i] == m) return (int)i;
+        bt_medium r = m->rec;
+        r.off = (int32_t)pool.size();
+        pool.insert(pool.end(), m->pool.begin(), m->pool.end());
+        media.push_back(r);
+        media_src.push_back(m);
+        return (int)media.size() - 1;
+    }
+
+    void add_obsc(const bt_obscuration* o, int32_t* b, int32_t* e) {
+        *b = (int32_t)obsc.size();
+        const int32_t base = (int32_t)pool.size();
+        for (bt_obsc op : o->ops) {
+            if (op.op == BT_O_POLYGON) op.off += base;
+            obsc.push_back(op);
+        }
+        pool.insert(pool.end(), o->pool.begin(), o->pool.end());
+        *e = (int32_t)obsc.size();
+    }
+
+    static size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+    std::vector<unsigned char> blob() const {
+        bt_prog_header h;
+        memset(&h, 0, sizeof(h));
+        h.nstages = (int32_t)stages.size();
+        h.nsurf = (int32_t)surfs.size();
+        h.nmedia = (int32_t)media.size();
+        h.nobsc = (int32_t)obsc.size();
+        h.npool = (int32_t)pool.size();
+        size_t off = align16(sizeof(h));
+        h.off_stages = (int32_t)off;
+        off = align16(off + stages.size() * sizeof(bt_stage));
+        h.off_surfs = (int32_t)off;
+        off = align16(off + surfs.size() * sizeof(bt_surf));
+        h.off_media = (int32_t)off;
+        off = align16(off + media.size() * sizeof(bt_medium));
+        h.off_obsc = (int32_t)off;
+        off = align16(off + obsc.size() * sizeof(bt_obsc));
+        h.off_pool = (int32_t)off;
+        off = align16(off + pool.size() * sizeof(double));
+        h.total_bytes = (int32_t)off;
+        std::vector<unsigned char> b(off, 0);
+        memcpy(b.data(), &h, sizeof(h));
+        if (!stages.empty()) memcpy(b.data() + h.off_stages, stages.data(), stages.size() * sizeof(bt_stage));
+        if (!surfs.empty()) memcpy(b.data() + h.off_surfs, surfs.data(), surfs.size() * sizeof(bt_surf));
+        if (!media.empty()) memcpy(b.data() + h.off_media, media.data(), media.size() * sizeof(bt_medium));
+        if (!obsc.empty()) memcpy(b.data() + h.off_obsc, obsc.data(), obsc.size() * sizeof(bt_obsc));
+        if (!pool.empty()) memcpy(b.data() + h.off_pool, pool.data(), pool.size() * sizeof(double));
+        return b;
+    }
+};
+
+static const size_t kMaxBlobBytes = 200 * 1024;
+
+static bt_stage blank_stage(int kind) {
+    bt_stage st;
+    memset(&st, 0, sizeof(st));
+    st.kind = kind;
+    st.surf = -1;
+    st.medium = -1;
+    st.obsc_begin = 0;
+    st.obsc_end = 0;
+    st.identity = 1;
+    st.drot[0] = st.drot[4] = st.drot[8] = 1.0;
+    return st;
+}
+
+static void set_transform(bt_stage& st, const double* dr, const double* drot) {
+    if (!dr || !drot) return;
+    bool ident = true;
+    for (int i = 0; i < 3; i++) {
+        st.dr[i] = dr[i];
+        if (dr[i] != 0.0) ident = false;
+    }
+    for (int i = 0; i < 9; i++) {
+        st.drot[i] = drot[i];
+        const double want = (i % 4 == 0) ? 1.0 : 0.0;
+        if (drot[i] != want) ident = false;
+    }
+    st.identity = ident ? 1 : 0;
+}
+
+// A temporary device copy of a blob, freed stream-ordered.
+struct TempBlob {
+    unsigned char* d = nullptr;
+    int bytes = 0;
+    cudaStream_t stream = 0;
+    cudaError_t upload(const std::vector<unsigned char>& b, cudaStream_t s) {
+        stream = s;
+        bytes = (int)b.size();
+        cudaError_t e = cudaMallocAsync((void**)&d, b.size(), s);
+        if (e != cudaSuccess) { d = nullptr; return e; }
+        return cudaMemcpyAsync(d, b.data(), b.size(), cudaMemcpyHostToDevice, s);
+    }
+    ~TempBlob() {
+        if (d) cudaFreeAsync(d, stream);
+    }
+};
+
+static RV to_rv(const bt_rayvector* r) {
+    RV v;
+    v.x = r->x; v.y = r->y; v.z = r->z;
+    v.vx = r->vx; v.vy = r->vy; v.vz = r->vz;
+    v.t = r->t; v.w = r->wavelength; v.f = r->flux;
+    v.vig = r->vignetted; v.fail = r->failed;
+    v.n = (long long)r->size;
+    return v;
+}
+
+static int check_rv(const bt_rayvector* rv) {
+    if (!rv) return fail(BT_ERR_ARG, "null ray vector");
+    if (rv->size == 0) return BT_OK;
+    if (!rv->x || !rv->y || !rv->z || !rv->vx || !rv->vy || !rv->vz || !rv->t || !rv->wavelength || !rv->flux ||
+        !rv->vignetted || !rv->failed)
+        return fail(BT_ERR_ARG, "ray vector has a null array");
+    return BT_OK;
+}
+
+static int run_single(const ProgBuilder& pb, const bt_rayvector* rv, int niter, cudaStream_t stream,
+                      const char* what) {
+    std::vector<unsigned char> b = pb.blob();
+    if (b.size() > kMaxBlobBytes) return fail(BT_ERR_UNSUPPORTED, std::string(what) + ": descriptor too large");
+    TempBlob tb;
+    CUDA_TRY(tb.upload(b, stream), what);
+    RV v = to_rv(rv);
+    CUDA_TRY(bt_launch_trace(tb.d, tb.bytes, v, v, nullptr, 0, niter, stream), what);
+    return BT_OK;
+}
+
+static int surface_op(int kind, const bt_surface* s, const double* dr, const double* drot, const bt_medium_h* m2,
+                      const bt_rayvector* rv, const bt_coating* coating, int niter, void* stream, const char* what) {
+    if (!s) return fail(BT_ERR_ARG, std::string(what) + ": null surface");
+    int rc = check_rv(rv);
+    if (rc != BT_OK) return rc;
+    if (!dr || !drot) return fail(BT_ERR_ARG, std::string(what) + ": null transform");
+    if (niter < 0) return fail(BT_ERR_ARG, std::string(what) + ": negative niter");
+    if (rv->size == 0) return BT_OK;
+    ProgBuilder pb;
+    bt_stage st = blank_stage(kind);
+    set_transform(st, dr, drot);
+    st.surf = pb.add_surface(s);
+    if (st.surf < 0) return BT_ERR_CUDA;
+    if (kind == BT_ST_REFRACT) {
+        if (!m2) return fail(BT_ERR_ARG, "refract: null medium");
+        st.medium = pb.add_medium(m2);
+    }
+    if (coating) {
+        st.coated = 1;
+        st.coat_r = coating->R;
+        st.coat_t = coating->T;
+    }
+    pb.stages.push_back(st);
+    return run_single(pb, rv, niter, (cudaStream_t)stream, what);
+}
+
+extern "C" int bt_intersect(const bt_surface* s, const double dr[3], const double drot[9], const bt_rayvector* rv,
+                            const bt_coating* coating, int max_threads, int niter, void* stream) {
+    (void)max_threads;
+    return surface_op(BT_ST_INTERSECT, s, dr, drot, nullptr, rv, coating, niter, stream, "intersect");
+}
+
+extern "C" int bt_reflect(const bt_surface* s, const double dr[3], const double drot[9], const bt_rayvector* rv,
+                          const bt_coating* coating, int max_threads, int niter, void* stream) {
+    (void)max_threads;
+    return surface_op(BT_ST_REFLECT, s, dr, drot, nullptr, rv, coating, niter, stream, "reflect");
+}
+
+extern "C" int bt_refract(const bt_surface* s, const double dr[3], const double drot[9], const bt_medium_h* m1,
+                          const bt_medium_h* m2, const bt_rayvector* rv, const bt_coating* coating, int max_threads,
+                          int niter, void* stream) {
+    (void)max_threads;
+    (void)m1;  // n1 comes from |v| (src/batoid.cpp:454-458)
+    return surface_op(BT_ST_REFRACT, s, dr, drot, m2, rv, coating, niter, stream, "refract");
+}
+
+extern "C" int bt_obscure(const bt_obscuration* o, const bt_rayvector* rv, int max_threads, void* stream) {
+    (void)max_threads;
+    if (!o) return fail(BT_ERR_ARG, "obscure: null obscuration");
+    int rc = check_rv(rv);
+    if (rc != BT_OK || rv->size == 0) return rc;
+    ProgBuilder pb;
+    bt_stage st = blank_stage(BT_ST_OBSCURE);
+    pb.add_obsc(o, &st.obsc_begin, &st.obsc_end);
+    pb.stages.push_back(st);
+    std::vector<unsigned char> b = pb.blob();
+    TempBlob tb;
+    CUDA_TRY(tb.upload(b, (cudaStream_t)stream), "obscure");
+    RV v = to_rv(rv);
+    CUDA_TRY(bt_launch_obsc(tb.d, tb.bytes, nullptr, nullptr, nullptr, &v, v.n, (cudaStream_t)stream), "obscure");
+    return BT_OK;
+}
+
+extern "C" int bt_obsc_contains(const bt_obscuration* o, const double* x, const double* y, uint8_t* out, size_t n,
+                                void* stream) {
+    if (!o) return fail(BT_ERR_ARG, "contains: null obscuration");
+    if (n == 0) return BT_OK;
+    if (!x || !y || !out) return fail(BT_ERR_ARG, "contains: null array");
+    ProgBuilder pb;
+    bt_stage st = blank_stage(BT_ST_OBSCURE);
+    pb.add_obsc(o, &st.obsc_begin, &st.obsc_end);
+    pb.stages.push_back(st);
+    std::vector<unsigned char> b = pb.blob();
+    TempBlob tb;
+    CUDA_TRY(tb.upload(b, (cudaStream_t)stream), "contains");
+    CUDA_TRY(bt_launch_obsc(tb.d, tb.bytes, x, y, out, nullptr, (long long)n, (cudaStream_t)stream), "contains");
+    return BT_OK;
+}
+
+extern "C" int bt_surface_sag(const bt_surface* s, const double* x, const double* y, double* out, size_t n,
+                              void* stream) {
+    if (!s) return fail(BT_ERR_ARG, "sag: null surface");
+    if (n == 0) return BT_OK;
+    if (!x || !y || !out) return fail(BT_ERR_ARG, "sag: null array");
+    ProgBuilder pb;
+    bt_stage st = blank_stage(BT_ST_INTERSECT);
+    st.surf = pb.add_surface(s);
+    if (st.surf < 0) return BT_ERR_CUDA;
+    pb.stages.push_back(st);
+    TempBlob tb;
+    CUDA_TRY(tb.upload(pb.blob(), (cudaStream_t)stream), "sag");
+    CUDA_TRY(bt_launch_surface_eval(tb.d, tb.bytes, x, y, out, nullptr, (long long)n, (cudaStream_t)stream), "sag");
+    return BT_OK;
+}
+
+extern "C" int bt_surface_normal(const bt_surface* s, const double* x, const double* y, double* out, size_t n,
+                                 void* stream) {
+    if (!s) return fail(BT_ERR_ARG, "normal: null surface");
+    if (n == 0) return BT_OK;
+    if (!x || !y || !out) return fail(BT_ERR_ARG, "normal: null array");
+    ProgBuilder pb;
+    bt_stage st = blank_stage(BT_ST_INTERSECT);
+    st.surf = pb.add_surface(s);
+    if (st.surf < 0) return BT_ERR_CUDA;
+    pb.stages.push_back(st);
+    TempBlob tb;
+    CUDA_TRY(tb.upload(pb.blob(), (cudaStream_t)stream), "normal");
+    CUDA_TRY(bt_launch_surface_eval(tb.d, tb.bytes, x, y, nullptr, out, (long long)n, (cudaStream_t)stream),
+             "normal");
+    return BT_OK;
+}
+
+extern "C" int bt_medium_getN(const bt_medium_h* m, const double* w, double* out, size_t n, void* stream) {
+    if (!m) return fail(BT_ERR_ARG, "getN: null medium");
+    if (n == 0) return BT_OK;
+    if (!w || !out) return fail(BT_ERR_ARG, "getN: null array");
+    ProgBuilder pb;
+    pb.add_medium(m);
+    pb.stages.push_back(blank_stage(BT_ST_OBSCURE));
+    TempBlob tb;
+    CUDA_TRY(tb.upload(pb.blob(), (cudaStream_t)stream), "getN");
+    CUDA_TRY(bt_launch_getN(tb.d, tb.bytes, w, out, (long long)n, (cudaStream_t)stream), "getN");
+    return BT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// transforms and RayVector methods
+// ---------------------------------------------------------------------------
+
+extern "C" int bt_apply_forward_transform(const double dr[3], const double drot[9], const bt_rayvector* rv,
+                                          int max_threads, void* stream) {
+    (void)max_threads;
+    int rc = check_rv(rv);
+    if (rc != BT_OK) return rc;
+    if (!dr || !drot) return fail(BT_ERR_ARG, "transform: null transform");
+    CUDA_TRY(bt_launch_transform_rv(dr, drot, to_rv(rv), true, (cudaStream_t)stream), "applyForwardTransform");
+    return BT_OK;
+}
+
+extern "C" int bt_apply_reverse_transform(const double dr[3], const double drot[9], const bt_rayvector* rv,
+                                          int max_threads, void* stream) {
+    (void)max_threads;
+    int rc = check_rv(rv);
+    if (rc != BT_OK) return rc;
+    if (!dr || !drot) return fail(BT_ERR_ARG, "transform: null transform");
+    CUDA_TRY(bt_launch_transform_rv(dr, drot, to_rv(rv), false, (cudaStream_t)stream), "applyReverseTransform");
+    return BT_OK;
+}
+
+extern "C" int bt_apply_forward_transform_arrays(const double dr[3], const double drot[9], double* x, double* y,
+                                                 double* z, size_t n, int max_threads, void* stream) {
+    (void)max_threads;
+    if (n == 0) return BT_OK;
+    if (!dr || !drot || !x || !y || !z) return fail(BT_ERR_ARG, "transform arrays: null argument");
+    CUDA_TRY(bt_launch_transform_arrays(dr, drot, x, y, z, (long long)n, true, (cudaStream_t)stream),
+             "applyForwardTransformArrays");
+    return BT_OK;
+}
+
+extern "C" int bt_apply_reverse_transform_arrays(const double dr[3], const double drot[9], double* x, double* y,
+                                                 double* z, size_t n, int max_threads, void* stream) {
+    (void)max_threads;
+    if (n == 0) return BT_OK;
+    if (!dr || !drot || !x || !y || !z) return fail(BT_ERR_ARG, "transform arrays: null argument");
+    CUDA_TRY(bt_launch_transform_arrays(dr, drot, x, y, z, (long long)n, false, (cudaStream_t)stream),
+             "applyReverseTransformArrays");
+    return BT_OK;
+}
+
+extern "C" int bt_finish_parallel(const double dr[3], const double drot[9], const double vv[3], double* x,
+                                  double* y, double* z, size_t n, void* stream) {
+    if (n == 0) return BT_OK;
+    if (!dr || !drot || !vv || !x || !y || !z) return fail(BT_ERR_ARG, "finishParallel: null argument");
+    CUDA_TRY(bt_launch_finish_parallel(dr, drot, vv, x, y, z, (long long)n, (cudaStream_t)stream), "finishParallel");
+    return BT_OK;
+}
+
+extern "C" int bt_rv_position_at_time(const bt_rayvector* rv, double t, double* xo, double* yo, double* zo,
+                                      int max_threads, void* stream) {
+    (void)max_threads;
+    int rc = check_rv(rv);
+    if (rc != BT_OK || rv->size == 0) return rc;
+    if (!xo || !yo || !zo) return fail(BT_ERR_ARG, "positionAtTime: null output");
+    CUDA_TRY(bt_launch_position_at_time(to_rv(rv), t, xo, yo, zo, (cudaStream_t)stream), "positionAtTime");
+    return BT_OK;
+}
+
+extern "C" int bt_rv_propagate_in_place(const bt_rayvector* rv, double t, int max_threads, void* stream) {
+    (void)max_threads;
+    int rc = check_rv(rv);
+    if (rc != BT_OK || rv->size == 0) return rc;
+    CUDA_TRY(bt_launch_propagate(to_rv(rv), t, (cudaStream_t)stream), "propagateInPlace");
+    return BT_OK;
+}
+
+extern "C" int bt_rv_phase(const bt_rayvector* rv, double x, double y, double z, double t, double* out,
+                           int max_threads, void* stream) {
+    (void)max_threads;
+    int rc = check_rv(rv);
+    if (rc != BT_OK || rv->size == 0) return rc;
+    if (!out) return fail(BT_ERR_ARG, "phase: null output");
+    CUDA_TRY(bt_launch_phase(to_rv(rv), x, y, z, t, out, false, (cudaStream_t)stream), "phase");
+    return BT_OK;
+}
+
+extern "C" int bt_rv_amplitude(const bt_rayvector* rv, double x, double y, double z, double t, double* out,
+                               int max_threads, void* stream) {
+    (void)max_threads;
+    int rc = check_rv(rv);
+    if (rc != BT_OK || rv->size == 0) return rc;
+    if (!out) return fail(BT_ERR_ARG, "amplitude: null output");
+    CUDA_TRY(bt_launch_phase(to_rv(rv), x, y, z, t, out, true, (cudaStream_t)stream), "amplitude");
+    return BT_OK;
+}
+
+extern "C" int bt_rv_sum_amplitude(const bt_rayvector* rv, double x, double y, double z, double t,
+                                   int ignore_vignetted, int max_threads, double* out, void* stream) {
+    (void)max_threads;
+    int rc = check_rv(rv);
+    if (rc != BT_OK) return rc;
+    if (!out) return fail(BT_ERR_ARG, "sumAmplitude: null output");
+    out[0] = 0.0;
+    out[1] = 0.0;
+    if (rv->size == 0) return BT_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    double* d = nullptr;
+    CUDA_TRY(cudaMallocAsync((void**)&d, 2 * sizeof(double), s), "sumAmplitude");
+    cudaError_t e = bt_launch_sum_amplitude(to_rv(rv), x, y, z, t, ignore_vignetted != 0, d, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "sumAmplitude");
+    return BT_OK;
+}
+
+extern "C" int bt_rv_equal(const bt_rayvector* a, const bt_rayvector* b, int* out, void* stream) {
+    int rc = check_rv(a);
+    if (rc != BT_OK) return rc;
+    rc = check_rv(b);
+    if (rc != BT_OK) return rc;
+    if (!out) return fail(BT_ERR_ARG, "equal: null output");
+    if (a->size != b->size) { *out = 0; return BT_OK; }
+    if (a->size == 0) { *out = 1; return BT_OK; }
+    cudaStream_t s = (cudaStream_t)stream;
+    int* d = nullptr;
+    int one = 1;
+    CUDA_TRY(cudaMallocAsync((void**)&d, sizeof(int), s), "equal");
+    cudaError_t e = cudaMemcpyAsync(d, &one, sizeof(int), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = bt_launch_rv_equal(to_rv(a), to_rv(b), d, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "equal");
+    return BT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// fused optic
+// ---------------------------------------------------------------------------
+
+struct bt_optic {
+    int nstages;
+    int blob_bytes;
+    unsigned char* d_blob;
+    // host pipeline scratch for bt_optic_trace_host
+    std::mutex mu;
+    size_t host_chunk = 0;
+    unsigned char* d_chunk[2] = {nullptr, nullptr};
+    cudaStream_t streams[2] = {nullptr, nullptr};
+    cudaEvent_t done[2] = {nullptr, nullptr};
+};
+
+extern "C" int bt_optic_create(size_t nstages, const int* kinds, const bt_surface* const* surfaces, const double* dr,
+                               const double* drot, const bt_medium_h* const* media,
+                               const bt_obscuration* const* obscurations, const bt_coating* const* coatings,
+                               bt_optic** out) {
+    if (!out) return fail(BT_ERR_ARG, "optic: null output");
+    if (nstages > BT_MAX_STAGES) return fail(BT_ERR_UNSUPPORTED, "optic: too many stages");
+    if (nstages > 0 && (!kinds || !surfaces || !dr || !drot)) return fail(BT_ERR_ARG, "optic: null stage arrays");
+    ProgBuilder pb;
+    for (size_t k = 0; k < nstages; k++) {
+        const int kind = kinds[k];
+        if (kind != BT_ST_INTERSECT && kind != BT_ST_REFLECT && kind != BT_ST_REFRACT)
+            return fail(BT_ERR_ARG, "optic: bad stage kind");
+        if (!surfaces[k]) return fail(BT_ERR_ARG, "optic: null surface");
+        bt_stage st = blank_stage(kind);
+        set_transform(st, dr + 3 * k, drot + 9 * k);
+        st.surf = pb.add_surface(surfaces[k]);
+        if (st.surf < 0) return BT_ERR_CUDA;
+        if (kind == BT_ST_REFRACT) {
+            if (!media || !media[k]) return fail(BT_ERR_ARG, "optic: refracting stage without a medium");
+            st.medium = pb.add_medium(media[k]);
+        }
+        if (obscurations && obscurations[k]) pb.add_obsc(obscurations[k], &st.obsc_begin, &st.obsc_end);
+        if (coatings && coatings[k]) {
+            st.coated = 1;
+            st.coat_r = coatings[k]->R;
+            st.coat_t = coatings[k]->T;
+        }
+        pb.stages.push_back(st);
+    }
+    std::vector<unsigned char> b = pb.blob();
+    if (b.size() > kMaxBlobBytes) return fail(BT_ERR_UNSUPPORTED, "optic: descriptor too large");
+    bt_optic* o = new bt_optic;
+    o->nstages = (int)nstages;
+    o->blob_bytes = (int)b.size();
+    cudaError_t e = cudaMalloc((void**)&o->d_blob, b.size());
+    if (e != cudaSuccess) { delete o; return cuda_fail(e, "optic alloc"); }
+    e = cudaMemcpy(o->d_blob, b.data(), b.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { cudaFree(o->d_blob); delete o; return cuda_fail(e, "optic upload"); }
+    *out = o;
+    return BT_OK;
+}
+
+static void release_host_pipeline(bt_optic* o) {
+    for (int k = 0; k < 2; k++) {
+        if (o->d_chunk[k]) cudaFree(o->d_chunk[k]);
+        if (o->streams[k]) cudaStreamDestroy(o->streams[k]);
+        if (o->done[k]) cudaEventDestroy(o->done[k]);
+        o->d_chunk[k] = nullptr;
+        o->streams[k] = nullptr;
+        o->done[k] = nullptr;
+    }
+    o->host_chunk = 0;
+}
+
+extern "C" void bt_optic_destroy(bt_optic* o) {
+    if (!o) return;
+    release_host_pipeline(o);
+    if (o->d_blob) cudaFree(o->d_blob);
+    delete o;
+}
+
+extern "C" int bt_optic_nstages(const bt_optic* o, int* out) {
+    if (!o || !out) return fail(BT_ERR_ARG, "null argument");
+    *out = o->nstages;
+    return BT_OK;
+}
+
+extern "C" int bt_optic_trace(const bt_optic* o, const bt_rayvector* rv, int niter, void* stream) {
+    if (!o) return fail(BT_ERR_ARG, "trace: null optic");
+    int rc = check_rv(rv);
+    if (rc != BT_OK || rv->size == 0) return rc;
+    if (niter < 0) return fail(BT_ERR_ARG, "trace: negative niter");
+    RV v = to_rv(rv);
+    CUDA_TRY(bt_launch_trace(o->d_blob, o->blob_bytes, v, v, nullptr, 0, niter, (cudaStream_t)stream), "trace");
+    return BT_OK;
+}
+
+extern "C" int bt_optic_trace_full(const bt_optic* o, const bt_rayvector* rv, const bt_rayvector* snaps, int niter,
+                                   void* stream) {
+    if (!o) return fail(BT_ERR_ARG, "traceFull: null optic");
+    int rc = check_rv(rv);
+    if (rc != BT_OK) return rc;
+    if (!snaps && o->nstages > 0) return fail(BT_ERR_ARG, "traceFull: null snapshots");
+    if (rv->size == 0 || o->nstages == 0) return BT_OK;
+    SnapSet ss;
+    memset(&ss, 0, sizeof(ss));
+    for (int k = 0; k < o->nstages; k++) {
+        rc = check_rv(&snaps[k]);
+        if (rc != BT_OK) return rc;
+        if (snaps[k].size != rv->size) return fail(BT_ERR_ARG, "traceFull: snapshot size mismatch");
+        ss.s[k] = to_rv(&snaps[k]);
+    }
+    RV v = to_rv(rv);
+    CUDA_TRY(bt_launch_trace(o->d_blob, o->blob_bytes, v, v, &ss, o->nstages, niter, (cudaStream_t)stream),
+             "traceFull");
+    return BT_OK;
+}
+
+// Device chunk layout: 9 double arrays then 2 byte arrays, each `chunk` long.
+static RV chunk_rv(unsigned char* base, size_t chunk, long long n) {
+    RV v;
+    double* d = reinterpret_cast<double*>(base);
+    v.x = d; v.y = d + chunk; v.z = d + 2 * chunk;
+    v.vx = d + 3 * chunk; v.vy = d + 4 * chunk; v.vz = d + 5 * chunk;
+    v.t = d + 6 * chunk; v.w = d + 7 * chunk; v.f = d + 8 * chunk;
+    v.vig = base + 9 * chunk * sizeof(double);
+    v.fail = v.vig + chunk;
+    v.n = n;
+    return v;
+}
+
+extern "C" int bt_optic_trace_host(const bt_optic* oc, const bt_rayvector* h, int niter, size_t chunk,
+                                   void* stream) {
+    bt_optic* o = const_cast<bt_optic*>(oc);
+    if (!o) return fail(BT_ERR_ARG, "traceHost: null optic");
+    int rc = check_rv(h);
+    if (rc != BT_OK || h->size == 0) return rc;
+    if (chunk == 0) chunk = (size_t)1 << 22;
+    if (chunk > h->size) chunk = h->size;
+    std::lock_guard<std::mutex> lock(o->mu);
+    const size_t bytes = chunk * (9 * sizeof(double) + 2);
+    if (o->host_chunk != chunk) {
+        release_host_pipeline(o);
+        for (int k = 0; k < 2; k++) {
+            cudaError_t e = cudaMalloc((void**)&o->d_chunk[k], bytes);
+            if (e != cudaSuccess) { release_host_pipeline(o); return fail(BT_ERR_ALLOC, "traceHost: device scratch"); }
+            CUDA_TRY(cudaStreamCreateWithFlags(&o->streams[k], cudaStreamNonBlocking), "traceHost streams");
+            CUDA_TRY(cudaEventCreateWithFlags(&o->done[k], cudaEventDisableTiming), "traceHost events");
+        }
+        o->host_chunk = chunk;
+    }
+    // Order the pipeline after prior work on the caller's stream.
+    cudaStream_t user = (cudaStream_t)stream;
+    cudaEvent_t start;
+    CUDA_TRY(cudaEventCreateWithFlags(&start, cudaEventDisableTiming), "traceHost");
+    CUDA_TRY(cudaEventRecord(start, user), "traceHost");
+    for (int k = 0; k < 2; k++) CUDA_TRY(cudaStreamWaitEvent(o->streams[k], start, 0), "traceHost");
+    cudaEventDestroy(start);
+    const size_t n = h->size;
+    size_t nchunks = (n + chunk - 1) / chunk;
+    for (size_t c = 0; c < nchunks; c++) {
+        const int k = (int)(c & 1);
+        cudaStream_t s = o->streams[k];
+        const size_t i0 = c * chunk;
+        const size_t m = (n - i0) < chunk ? (n - i0) : chunk;
+        RV d = chunk_rv(o->d_chunk[k], chunk, (long long)m);
+        double* hd[9] = {h->x, h->y, h->z, h->vx, h->vy, h->vz, h->t, h->wavelength, h->flux};
+        double* dd[9] = {d.x, d.y, d.z, d.vx, d.vy, d.vz, d.t, d.w, d.f};
+        for (int a = 0; a < 9; a++)
+            CUDA_TRY(cudaMemcpyAsync(dd[a], hd[a] + i0, m * sizeof(double), cudaMemcpyHostToDevice, s), "traceHost H2D");
+        CUDA_TRY(cudaMemcpyAsync(d.vig, h->vignetted + i0, m, cudaMemcpyHostToDevice, s), "traceHost H2D");
+        CUDA_TRY(cudaMemcpyAsync(d.fail, h->failed + i0, m, cudaMemcpyHostToDevice, s), "traceHost H2D");
+        CUDA_TRY(bt_launch_trace(o->d_blob, o->blob_bytes, d, d, nullptr, 0, niter, s), "traceHost trace");
+        // wavelength is never modified by a trace: no copy back
+        double* ho[8] = {h->x, h->y, h->z, h->vx, h->vy, h->vz, h->t, h->flux};
+        double* dout[8] = {d.x, d.y, d.z, d.vx, d.vy, d.vz, d.t, d.f};
+        for (int a = 0; a < 8; a++)
+            CUDA_TRY(cudaMemcpyAsync(ho[a] + i0, dout[a], m * sizeof(double), cudaMemcpyDeviceToHost, s), "traceHost D2H");
+        CUDA_TRY(cudaMemcpyAsync(h->vignetted + i0, d.vig, m, cudaMemcpyDeviceToHost, s), "traceHost D2H");
+        CUDA_TRY(cudaMemcpyAsync(h->failed + i0, d.fail, m, cudaMemcpyDeviceToHost, s), "traceHost D2H");
+    }
+    for (int k = 0; k < 2; k++) {
+        CUDA_TRY(cudaEventRecord(o->done[k], o->streams[k]), "traceHost");
+        CUDA_TRY(cudaStreamWaitEvent(user, o->done[k], 0), "traceHost");
+    }
+    CUDA_TRY(cudaStreamSynchronize(user), "traceHost sync");
+    return BT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Huygens
+// ---------------------------------------------------------------------------
+
+extern "C" int bt_huygens_amplitudes(const bt_rayvector* rv, double px, double py, double pz, const double lat[4],
+                                     int na, int nb, double t0, int ignore_vignetted, double* out_re,
+                                     double* out_im, void* stream) {
+    int rc = check_rv(rv);
+    if (rc != BT_OK) return rc;
+    if (!lat || na < 0 || nb < 0) return fail(BT_ERR_ARG, "huygens: bad lattice");
+    if ((long long)na * nb == 0) return BT_OK;
+    if (!out_re || !out_im) return fail(BT_ERR_ARG, "huygens: null output");
+    CUDA_TRY(bt_launch_huygens(to_rv(rv), px, py, pz, lat, na, nb, t0, ignore_vignetted != 0, out_re, out_im,
+                               (cudaStream_t)stream),
+             "huygens");
+    return BT_OK;
+}
+
+extern "C" int bt_zernike_normal_equations(const double* x, const double* y, const double* v,
+                                           const long long* offsets, int nfits, const double* basis, int jmax,
+                                           int side, double* G, double* b, void* stream) {
+    if (nfits < 0 || jmax < 1 || side < 1) return fail(BT_ERR_ARG, "zernike fit: bad sizes");
+    if (jmax > 64 || side > 12) return fail(BT_ERR_UNSUPPORTED, "zernike fit: jmax <= 64 and order <= 11 supported");
+    if (nfits == 0) return BT_OK;
+    if (!x || !y || !v || !offsets || !basis || !G || !b) return fail(BT_ERR_ARG, "zernike fit: null array");
+    CUDA_TRY(bt_launch_zk_normal(x, y, v, offsets, nfits, basis, jmax, side, G, b, (cudaStream_t)stream),
+             "zernike fit");
+    return BT_OK;
+}
+
+// Test hook: reads and clears the device status word of the trace kernels
+// (BT_ERR_TIMEOUT if a bounded wait expired).  Synchronous.
+extern "C" int bt_check_device_status(void* stream) {
+    int st = 0;
+    CUDA_TRY(bt_read_device_status(&st, (cudaStream_t)stream), "device status");
+    if (st != 0) return fail(st, "a kernel's bounded wait expired");
+    return BT_OK;
+}

@@ -1,0 +1,223 @@
+// Huygens phasor sum over a pixel lattice (replaces the per-pixel Python loop
+// of huygensPSF calling RayVector.sumAmplitude, batoid/analysis.py:296-304 and
+// src/rayVector.cpp:169-222).
+//
+// The phase of ray r at lattice point P(a, b) = P0 + b'*p0 + a'*p1
+// (a' = a - na/2, b' = b - nb/2) is linear in (a', b'):
+//     phi = 2 pi [ phi0_r + b' alpha_r + a' beta_r ]        (in turns)
+// phi0, alpha, beta are formed once per ray in FP64 and reduced modulo one
+// turn into 32-bit fixed point, so phi(a, b) = th + b' A + a' B is evaluated
+// exactly modulo 2^32 with integer wrap-around.  Per ray-pixel pair the
+// kernel then needs one integer FMA, a fast FP32 sincos (or a complex
+// rotation by exp(2 pi i A) for neighbouring pixels) and one complex FMA.
+// Each thread owns HUY_PX consecutive pixels of one lattice row; sums over a
+// shared-memory tile of rays are plain FP32 and folded into Kahan-compensated
+// FP32 running sums.  Rays are split across blocks; the per-split partial
+// sums (device scratch) are reduced in FP64 in a fixed order.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "bt_internal.h"
+
+#define HUY_THREADS 256
+#define HUY_PX 4
+#define HUY_TILE 256
+
+struct __align__(16) HuyRec {
+    uint32_t th;   // phase at P0, turns * 2^32
+    uint32_t A;    // phase step per b, turns * 2^32
+    uint32_t B;    // phase step per a, turns * 2^32
+    float f;       // flux (0 for excluded rays)
+    float ca;      // cos(2 pi A / 2^32)
+    float sa;      // sin(2 pi A / 2^32)
+    float pad0, pad1;
+};
+
+__device__ __forceinline__ uint32_t turns_to_fix32(double turns) {
+    double fr = turns - floor(turns);           // [0, 1]
+    double s = rint(fr * 4294967296.0);         // [0, 2^32]
+    unsigned long long u = (unsigned long long)s;
+    return (uint32_t)(u & 0xffffffffull);
+}
+
+__global__ void k_huy_prep(RV rv, double px, double py, double pz, double l0, double l1, double l2, double l3,
+                           double t0, int ignore_vig, HuyRec* rec) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < rv.n;
+         i += (long long)gridDim.x * blockDim.x) {
+        HuyRec r;
+        r.pad0 = 0.f;
+        r.pad1 = 0.f;
+        const bool use = !rv.fail[i] && !(ignore_vig && rv.vig[i]);
+        if (use) {
+            const double vx = rv.vx[i], vy = rv.vy[i], vz = rv.vz[i];
+            const double v2 = vx * vx + vy * vy + vz * vz;
+            const double w = rv.w[i];
+            // same ordering as src/rayVector.cpp:208-214, in turns
+            double ph = (px - rv.x[i]) * vx;
+            ph += (py - rv.y[i]) * vy;
+            ph += (pz - rv.z[i]) * vz;
+            ph /= v2;
+            ph -= t0 - rv.t[i];
+            ph /= w;
+            const double al = (l0 * vx + l1 * vy) / v2 / w;
+            const double be = (l2 * vx + l3 * vy) / v2 / w;
+            r.th = turns_to_fix32(ph);
+            r.A = turns_to_fix32(al);
+            r.B = turns_to_fix32(be);
+            r.f = (float)rv.f[i];
+            double sd, cd;
+            sincospi((double)(int32_t)r.A * (2.0 / 4294967296.0), &sd, &cd);
+            r.ca = (float)cd;
+            r.sa = (float)sd;
+            if (!(ph == ph) || !(al == al) || !(be == be)) {
+                // non-finite phase: contributes NaN, as in the reference
+                r.f = __int_as_float(0x7fc00000);
+            }
+        } else {
+            r.th = 0u; r.A = 0u; r.B = 0u;
+            r.f = 0.f; r.ca = 1.f; r.sa = 0.f;
+        }
+        rec[i] = r;
+    }
+}
+
+__device__ __forceinline__ void kahan_add(float& sum, float& comp, float v) {
+    const float y = v - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+}
+
+// grid: (tiles, nsplit).  part_* : [nsplit][na*nb] doubles.
+__global__ void __launch_bounds__(HUY_THREADS)
+k_huy_main(const HuyRec* __restrict__ rec, long long nrays, int na, int nb, int ngroups_b,
+           long long rays_per_split, double* part_re, double* part_im) {
+    __shared__ HuyRec tile[HUY_TILE];
+    const long long g = (long long)blockIdx.x * HUY_THREADS + threadIdx.x;  // pixel group
+    const long long ngroups = (long long)na * ngroups_b;
+    const bool active = g < ngroups;
+    const int a = active ? (int)(g / ngroups_b) : 0;
+    const int b0 = active ? (int)(g % ngroups_b) * HUY_PX : 0;
+    const int ap = a - na / 2;
+    const int bp = b0 - nb / 2;
+
+    float sre[HUY_PX], cre[HUY_PX], sim[HUY_PX], cim[HUY_PX];
+#pragma unroll
+    for (int k = 0; k < HUY_PX; k++) { sre[k] = 0.f; cre[k] = 0.f; sim[k] = 0.f; cim[k] = 0.f; }
+
+    const long long r0 = (long long)blockIdx.y * rays_per_split;
+    long long r1 = r0 + rays_per_split;
+    if (r1 > nrays) r1 = nrays;
+    const float two_pi_over_2_32 = 1.4629180792671596e-09f;  // 2 pi / 2^32
+
+    for (long long base = r0; base < r1; base += HUY_TILE) {
+        const int cnt = (int)((r1 - base) < HUY_TILE ? (r1 - base) : HUY_TILE);
+        __syncthreads();
+        if (threadIdx.x < cnt) tile[threadIdx.x] = rec[base + threadIdx.x];
+        __syncthreads();
+        if (!active) continue;
+        float tre[HUY_PX], tim[HUY_PX];
+#pragma unroll
+        for (int k = 0; k < HUY_PX; k++) { tre[k] = 0.f; tim[k] = 0.f; }
+        for (int j = 0; j < cnt; j++) {
+            const HuyRec r = tile[j];
+            const uint32_t th = r.th + (uint32_t)bp * r.A + (uint32_t)ap * r.B;
+            float s, c;
+            __sincosf((float)(int32_t)th * two_pi_over_2_32, &s, &c);
+            tre[0] = fmaf(r.f, c, tre[0]);
+            tim[0] = fmaf(r.f, s, tim[0]);
+#pragma unroll
+            for (int k = 1; k < HUY_PX; k++) {
+                const float c2 = c * r.ca - s * r.sa;
+                const float s2 = s * r.ca + c * r.sa;
+                c = c2;
+                s = s2;
+                tre[k] = fmaf(r.f, c, tre[k]);
+                tim[k] = fmaf(r.f, s, tim[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < HUY_PX; k++) {
+            kahan_add(sre[k], cre[k], tre[k]);
+            kahan_add(sim[k], cim[k], tim[k]);
+        }
+    }
+    if (!active) return;
+    const long long npix = (long long)na * nb;
+    double* pr = part_re + (long long)blockIdx.y * npix;
+    double* pi = part_im + (long long)blockIdx.y * npix;
+#pragma unroll
+    for (int k = 0; k < HUY_PX; k++) {
+        const int b = b0 + k;
+        if (b < nb) {
+            pr[(long long)a * nb + b] = (double)sre[k] - (double)cre[k];
+            pi[(long long)a * nb + b] = (double)sim[k] - (double)cim[k];
+        }
+    }
+}
+
+__global__ void k_huy_reduce(const double* part_re, const double* part_im, int nsplit, long long npix,
+                             double* out_re, double* out_im) {
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix;
+         p += (long long)gridDim.x * blockDim.x) {
+        double re = 0.0, im = 0.0;
+        for (int s = 0; s < nsplit; s++) {
+            re += part_re[(long long)s * npix + p];
+            im += part_im[(long long)s * npix + p];
+        }
+        out_re[p] = re;
+        out_im[p] = im;
+    }
+}
+
+cudaError_t bt_launch_huygens(const RV& rv, double px, double py, double pz, const double lat[4], int na,
+                              int nb, double t0, bool ignore_vig, double* out_re, double* out_im,
+                              cudaStream_t stream) {
+    const long long npix = (long long)na * nb;
+    if (npix <= 0) return cudaSuccess;
+    if (rv.n <= 0) {
+        cudaError_t e = cudaMemsetAsync(out_re, 0, npix * sizeof(double), stream);
+        if (e != cudaSuccess) return e;
+        return cudaMemsetAsync(out_im, 0, npix * sizeof(double), stream);
+    }
+    const int ngroups_b = (nb + HUY_PX - 1) / HUY_PX;
+    const long long ngroups = (long long)na * ngroups_b;
+    const long long tiles = (ngroups + HUY_THREADS - 1) / HUY_THREADS;
+    const int sms = bt_sm_count();
+    long long nsplit = (4LL * sms + tiles - 1) / tiles;
+    long long max_split = (rv.n + HUY_TILE - 1) / HUY_TILE;
+    if (nsplit > max_split) nsplit = max_split;
+    if (nsplit > 65535) nsplit = 65535;
+    if (nsplit < 1) nsplit = 1;
+    long long per = (rv.n + nsplit - 1) / nsplit;
+    per = ((per + HUY_TILE - 1) / HUY_TILE) * HUY_TILE;
+    nsplit = (rv.n + per - 1) / per;
+
+    // scratch: ray records and per-split partial sums
+    const size_t rec_bytes = (size_t)rv.n * sizeof(HuyRec);
+    const size_t part_bytes = (size_t)nsplit * npix * sizeof(double);
+    char* scratch = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&scratch, rec_bytes + 2 * part_bytes, stream);
+    if (e != cudaSuccess) return e;
+    HuyRec* rec = reinterpret_cast<HuyRec*>(scratch);
+    double* pre = reinterpret_cast<double*>(scratch + rec_bytes);
+    double* pim = reinterpret_cast<double*>(scratch + rec_bytes + part_bytes);
+
+    long long pg = (rv.n + 255) / 256;
+    if (pg > (long long)sms * 16) pg = (long long)sms * 16;
+    k_huy_prep<<<(int)pg, 256, 0, stream>>>(rv, px, py, pz, lat[0], lat[1], lat[2], lat[3], t0,
+                                            ignore_vig ? 1 : 0, rec);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        dim3 grid((unsigned)tiles, (unsigned)nsplit);
+        k_huy_main<<<grid, HUY_THREADS, 0, stream>>>(rec, rv.n, na, nb, ngroups_b, per, pre, pim);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        long long rg = (npix + 255) / 256;
+        if (rg > (long long)sms * 8) rg = (long long)sms * 8;
+        k_huy_reduce<<<(int)rg, 256, 0, stream>>>(pre, pim, (int)nsplit, npix, out_re, out_im);
+        e = cudaGetLastError();
+    }
+    cudaError_t e2 = cudaFreeAsync(scratch, stream);
+    return e != cudaSuccess ? e : e2;
+}

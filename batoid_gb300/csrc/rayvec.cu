@@ -1,0 +1,248 @@
+// Element-wise RayVector kernels: coordinate transforms, propagation, phase
+// and amplitude (src/batoid.cpp:8-148, src/rayVector.cpp:26-238).  These are
+// HBM-bound streaming kernels: one thread per ray, grid-stride, coalesced
+// FP64 loads.
+#include <cuda_runtime.h>
+#include "bt_internal.h"
+
+#define RV_THREADS 256
+
+static int rv_grid(long long n) {
+    long long need = (n + RV_THREADS - 1) / RV_THREADS;
+    long long cap = (long long)bt_sm_count() * 8;
+    if (need > cap) need = cap;
+    return need < 1 ? 1 : (int)need;
+}
+
+struct Xform {
+    double dr[3];
+    double r[9];
+};
+
+static Xform make_xf(const double dr[3], const double drot[9]) {
+    Xform f;
+    for (int i = 0; i < 3; i++) f.dr[i] = dr[i];
+    for (int i = 0; i < 9; i++) f.r[i] = drot[i];
+    return f;
+}
+
+#define GRID_LOOP(i, n)                                                                   \
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < (n);         \
+         i += (long long)gridDim.x * blockDim.x)
+
+// src/batoid.cpp:71-148 (positions and velocities of every ray, failed or not)
+__global__ void k_xform_rv(Xform f, RV rv, int forward) {
+    GRID_LOOP(i, rv.n) {
+        const double x = rv.x[i], y = rv.y[i], z = rv.z[i];
+        const double vx = rv.vx[i], vy = rv.vy[i], vz = rv.vz[i];
+        if (forward) {
+            const double dx = x - f.dr[0], dy = y - f.dr[1], dz = z - f.dr[2];
+            rv.x[i] = dx * f.r[0] + dy * f.r[3] + dz * f.r[6];
+            rv.y[i] = dx * f.r[1] + dy * f.r[4] + dz * f.r[7];
+            rv.z[i] = dx * f.r[2] + dy * f.r[5] + dz * f.r[8];
+            rv.vx[i] = vx * f.r[0] + vy * f.r[3] + vz * f.r[6];
+            rv.vy[i] = vx * f.r[1] + vy * f.r[4] + vz * f.r[7];
+            rv.vz[i] = vx * f.r[2] + vy * f.r[5] + vz * f.r[8];
+        } else {
+            rv.x[i] = x * f.r[0] + y * f.r[1] + z * f.r[2] + f.dr[0];
+            rv.y[i] = x * f.r[3] + y * f.r[4] + z * f.r[5] + f.dr[1];
+            rv.z[i] = x * f.r[6] + y * f.r[7] + z * f.r[8] + f.dr[2];
+            rv.vx[i] = vx * f.r[0] + vy * f.r[1] + vz * f.r[2];
+            rv.vy[i] = vx * f.r[3] + vy * f.r[4] + vz * f.r[5];
+            rv.vz[i] = vx * f.r[6] + vy * f.r[7] + vz * f.r[8];
+        }
+    }
+}
+
+cudaError_t bt_launch_transform_rv(const double dr[3], const double drot[9], const RV& rv, bool forward,
+                                   cudaStream_t stream) {
+    if (rv.n <= 0) return cudaSuccess;
+    k_xform_rv<<<rv_grid(rv.n), RV_THREADS, 0, stream>>>(make_xf(dr, drot), rv, forward ? 1 : 0);
+    return cudaGetLastError();
+}
+
+// src/batoid.cpp:8-38
+__global__ void k_xform_arrays(Xform f, double* X, double* Y, double* Z, long long n, int forward) {
+    GRID_LOOP(i, n) {
+        const double x = X[i], y = Y[i], z = Z[i];
+        if (forward) {
+            const double dx = x - f.dr[0], dy = y - f.dr[1], dz = z - f.dr[2];
+            X[i] = dx * f.r[0] + dy * f.r[3] + dz * f.r[6];
+            Y[i] = dx * f.r[1] + dy * f.r[4] + dz * f.r[7];
+            Z[i] = dx * f.r[2] + dy * f.r[5] + dz * f.r[8];
+        } else {
+            X[i] = x * f.r[0] + y * f.r[1] + z * f.r[2] + f.dr[0];
+            Y[i] = x * f.r[3] + y * f.r[4] + z * f.r[5] + f.dr[1];
+            Z[i] = x * f.r[6] + y * f.r[7] + z * f.r[8] + f.dr[2];
+        }
+    }
+}
+
+cudaError_t bt_launch_transform_arrays(const double dr[3], const double drot[9], double* x, double* y,
+                                       double* z, long long n, bool forward, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    k_xform_arrays<<<rv_grid(n), RV_THREADS, 0, stream>>>(make_xf(dr, drot), x, y, z, n, forward ? 1 : 0);
+    return cudaGetLastError();
+}
+
+// src/batoid.cpp:40-69: rotate into the back-propagation frame, move each
+// point along -v onto that frame's z=0 plane, rotate back.
+__global__ void k_finish_parallel(Xform f, double vxl, double vyl, double vzl, double* X, double* Y, double* Z,
+                                  long long n) {
+    GRID_LOOP(i, n) {
+        const double dx = X[i] - f.dr[0], dy = Y[i] - f.dr[1], dz = Z[i] - f.dr[2];
+        double x = dx * f.r[0] + dy * f.r[3] + dz * f.r[6];
+        double y = dx * f.r[1] + dy * f.r[4] + dz * f.r[7];
+        double z = dx * f.r[2] + dy * f.r[5] + dz * f.r[8];
+        const double dt = -z / vzl;
+        x += dt * vxl;
+        y += dt * vyl;
+        z += dt * vzl;
+        X[i] = x * f.r[0] + y * f.r[1] + z * f.r[2] + f.dr[0];
+        Y[i] = x * f.r[3] + y * f.r[4] + z * f.r[5] + f.dr[1];
+        Z[i] = x * f.r[6] + y * f.r[7] + z * f.r[8] + f.dr[2];
+    }
+}
+
+cudaError_t bt_launch_finish_parallel(const double dr[3], const double drot[9], const double vv[3],
+                                      double* x, double* y, double* z, long long n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    const double vxl = -vv[0] * drot[0] - vv[1] * drot[3] - vv[2] * drot[6];
+    const double vyl = -vv[0] * drot[1] - vv[1] * drot[4] - vv[2] * drot[7];
+    const double vzl = -vv[0] * drot[2] - vv[1] * drot[5] - vv[2] * drot[8];
+    k_finish_parallel<<<rv_grid(n), RV_THREADS, 0, stream>>>(make_xf(dr, drot), vxl, vyl, vzl, x, y, z, n);
+    return cudaGetLastError();
+}
+
+// src/rayVector.cpp:26-54
+__global__ void k_position_at_time(RV rv, double t, double* xo, double* yo, double* zo) {
+    GRID_LOOP(i, rv.n) {
+        const double dt = t - rv.t[i];
+        xo[i] = rv.x[i] + rv.vx[i] * dt;
+        yo[i] = rv.y[i] + rv.vy[i] * dt;
+        zo[i] = rv.z[i] + rv.vz[i] * dt;
+    }
+}
+
+cudaError_t bt_launch_position_at_time(const RV& rv, double t, double* xo, double* yo, double* zo,
+                                       cudaStream_t stream) {
+    if (rv.n <= 0) return cudaSuccess;
+    k_position_at_time<<<rv_grid(rv.n), RV_THREADS, 0, stream>>>(rv, t, xo, yo, zo);
+    return cudaGetLastError();
+}
+
+// src/rayVector.cpp:56-82
+__global__ void k_propagate(RV rv, double t) {
+    GRID_LOOP(i, rv.n) {
+        const double dt = t - rv.t[i];
+        rv.x[i] += rv.vx[i] * dt;
+        rv.y[i] += rv.vy[i] * dt;
+        rv.z[i] += rv.vz[i] * dt;
+        rv.t[i] = t;
+    }
+}
+
+cudaError_t bt_launch_propagate(const RV& rv, double t, cudaStream_t stream) {
+    if (rv.n <= 0) return cudaSuccess;
+    k_propagate<<<rv_grid(rv.n), RV_THREADS, 0, stream>>>(rv, t);
+    return cudaGetLastError();
+}
+
+// phi = 2 pi / lambda * ((r0 - r).v / |v|^2 - (t0 - t))  (src/rayVector.cpp:110-121)
+__device__ __forceinline__ double ray_phase(const RV& rv, long long i, double x, double y, double z, double t) {
+    const double PI = 3.14159265358979323846;
+    const double vx = rv.vx[i], vy = rv.vy[i], vz = rv.vz[i];
+    const double v2 = vx * vx + vy * vy + vz * vz;
+    double p = (x - rv.x[i]) * vx;
+    p += (y - rv.y[i]) * vy;
+    p += (z - rv.z[i]) * vz;
+    p /= v2;
+    p -= t - rv.t[i];
+    p *= 2 * PI / rv.w[i];
+    return p;
+}
+
+__global__ void k_phase(RV rv, double x, double y, double z, double t, double* out, int amplitude) {
+    GRID_LOOP(i, rv.n) {
+        const double p = ray_phase(rv, i, x, y, z, t);
+        if (amplitude) {
+            double s, c;
+            sincos(p, &s, &c);
+            out[2 * i] = c;
+            out[2 * i + 1] = s;
+        } else {
+            out[i] = p;
+        }
+    }
+}
+
+cudaError_t bt_launch_phase(const RV& rv, double x, double y, double z, double t, double* out,
+                            bool amplitude, cudaStream_t stream) {
+    if (rv.n <= 0) return cudaSuccess;
+    k_phase<<<rv_grid(rv.n), RV_THREADS, 0, stream>>>(rv, x, y, z, t, out, amplitude ? 1 : 0);
+    return cudaGetLastError();
+}
+
+// src/rayVector.cpp:169-222: sum of flux * exp(i phi) over rays that are not
+// failed (and not vignetted when ignore_vig).  FP64 block reduction, one
+// atomic add per block into d_out2 (zeroed by the caller).
+__global__ void k_sum_amplitude(RV rv, double x, double y, double z, double t, int ignore_vig, double* out2) {
+    double re = 0.0, im = 0.0;
+    GRID_LOOP(i, rv.n) {
+        if (!rv.fail[i] && !(ignore_vig && rv.vig[i])) {
+            const double p = ray_phase(rv, i, x, y, z, t);
+            double s, c;
+            sincos(p, &s, &c);
+            re += c * rv.f[i];
+            im += s * rv.f[i];
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        re += __shfl_down_sync(0xffffffffu, re, o);
+        im += __shfl_down_sync(0xffffffffu, im, o);
+    }
+    __shared__ double sre[RV_THREADS / 32], sim[RV_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { sre[warp] = re; sim[warp] = im; }
+    __syncthreads();
+    if (warp == 0) {
+        re = lane < RV_THREADS / 32 ? sre[lane] : 0.0;
+        im = lane < RV_THREADS / 32 ? sim[lane] : 0.0;
+        for (int o = 4; o > 0; o >>= 1) {
+            re += __shfl_down_sync(0xffffffffu, re, o);
+            im += __shfl_down_sync(0xffffffffu, im, o);
+        }
+        if (lane == 0) {
+            atomicAdd(out2, re);
+            atomicAdd(out2 + 1, im);
+        }
+    }
+}
+
+cudaError_t bt_launch_sum_amplitude(const RV& rv, double x, double y, double z, double t, bool ignore_vig,
+                                    double* d_out2, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(d_out2, 0, 2 * sizeof(double), stream);
+    if (e != cudaSuccess || rv.n <= 0) return e;
+    k_sum_amplitude<<<rv_grid(rv.n), RV_THREADS, 0, stream>>>(rv, x, y, z, t, ignore_vig ? 1 : 0, d_out2);
+    return cudaGetLastError();
+}
+
+// src/rayVector.cpp:224-238 and src/dualView.cpp:291-311: bitwise equality of
+// every field (NaN never compares equal).  d_flag must be 1 on entry; any
+// mismatch clears it.
+__global__ void k_rv_equal(RV a, RV b, int* flag) {
+    bool ok = true;
+    GRID_LOOP(i, a.n) {
+        ok &= (a.x[i] == b.x[i]) && (a.y[i] == b.y[i]) && (a.z[i] == b.z[i]);
+        ok &= (a.vx[i] == b.vx[i]) && (a.vy[i] == b.vy[i]) && (a.vz[i] == b.vz[i]);
+        ok &= (a.t[i] == b.t[i]) && (a.w[i] == b.w[i]) && (a.f[i] == b.f[i]);
+        ok &= (a.vig[i] == b.vig[i]) && (a.fail[i] == b.fail[i]);
+    }
+    if (!__all_sync(0xffffffffu, ok) && (threadIdx.x & 31) == 0) atomicExch(flag, 0);
+}
+
+cudaError_t bt_launch_rv_equal(const RV& a, const RV& b, int* d_flag, cudaStream_t stream) {
+    if (a.n <= 0) return cudaSuccess;
+    k_rv_equal<<<rv_grid(a.n), RV_THREADS, 0, stream>>>(a, b, d_flag);
+    return cudaGetLastError();
+}

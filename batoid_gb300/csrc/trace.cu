@@ -1,0 +1,290 @@
+// Fused sequential trace: one thread carries one ray through every stage of
+// an optic, in registers.  Replaces the per-surface OpenMP passes of the
+// reference (src/batoid.cpp:151-506) driven by CompoundOptic.trace
+// (batoid/optic.py:1013-1083): instead of reading and writing all 74 bytes
+// per ray once per surface, each ray is loaded once and stored once.
+#include <cuda_runtime.h>
+#include "bt_internal.h"
+#include "bt_device.cuh"
+#include "bt_stage_smem.cuh"
+
+cudaError_t bt_read_device_status(int* status, cudaStream_t stream) {
+    int zero = 0;
+    cudaError_t e = cudaMemcpyFromSymbolAsync(status, bt_dev_status, sizeof(int), 0,
+                                              cudaMemcpyDeviceToHost, stream);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return e;
+    if (*status != 0) {
+        e = cudaMemcpyToSymbolAsync(bt_dev_status, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
+        if (e != cudaSuccess) return e;
+        e = cudaStreamSynchronize(stream);
+    }
+    return e;
+}
+
+#define TRACE_THREADS 128
+
+struct RayState {
+    double x, y, z, vx, vy, vz, t, w, f;
+    bool vig, fail;
+};
+
+__device__ __forceinline__ void store_ray(const RV& o, long long i, const RayState& r) {
+    o.x[i] = r.x;
+    o.y[i] = r.y;
+    o.z[i] = r.z;
+    o.vx[i] = r.vx;
+    o.vy[i] = r.vy;
+    o.vz[i] = r.vz;
+    o.t[i] = r.t;
+    o.w[i] = r.w;
+    o.f[i] = r.f;
+    o.vig[i] = r.vig;
+    o.fail[i] = r.fail;
+}
+
+// One stage of the trace for one ray.  Semantics of src/batoid.cpp:175-506:
+// failed rays are skipped and keep their coordinates in the previous frame;
+// a ray that misses the surface is flagged failed+vignetted and likewise
+// keeps its previous coordinates; TIR writes the position, NaN velocity.
+__device__ __forceinline__ void run_stage(const Prog& P, const bt_stage& st, RayState& r, int niter,
+                                          int& cached_medium, double& cached_n) {
+    if (st.kind != BT_ST_OBSCURE && !r.fail) {
+        double x, y, z, vx, vy, vz;
+        if (st.identity) {
+            x = r.x; y = r.y; z = r.z; vx = r.vx; vy = r.vy; vz = r.vz;
+        } else {
+            const double dx = r.x - st.dr[0], dy = r.y - st.dr[1], dz = r.z - st.dr[2];
+            x = dx * st.drot[0] + dy * st.drot[3] + dz * st.drot[6];
+            y = dx * st.drot[1] + dy * st.drot[4] + dz * st.drot[7];
+            z = dx * st.drot[2] + dy * st.drot[5] + dz * st.drot[8];
+            vx = r.vx * st.drot[0] + r.vy * st.drot[3] + r.vz * st.drot[6];
+            vy = r.vx * st.drot[1] + r.vy * st.drot[4] + r.vz * st.drot[7];
+            vz = r.vx * st.drot[2] + r.vy * st.drot[5] + r.vz * st.drot[8];
+        }
+        double dt = 0.0, ux = 0.0, uy = 0.0;
+        bool slope_ok = false;
+        const bool ok = bt_surf_tti(P, st.surf, x, y, z, vx, vy, vz, dt, niter, &ux, &uy, &slope_ok);
+        if (ok) {
+            x += vx * dt;
+            y += vy * dt;
+            z += vz * dt;
+            const double t = r.t + dt;
+            if (st.kind == BT_ST_INTERSECT) {
+                if (st.coated) r.f *= st.coat_t;
+            } else {
+                double nx, ny, nz;
+                const int kind = P.surfs[st.surf].kind;
+                if (slope_ok && kind != BT_S_TILTED) bt_normal_from_slope(ux, uy, &nx, &ny, &nz);
+                else bt_surf_normal(P, st.surf, x, y, &nx, &ny, &nz);
+                if (st.kind == BT_ST_REFLECT) {
+                    // src/batoid.cpp:343-353
+                    const double alpha = vx * nx + vy * ny + vz * nz;
+                    vx -= 2 * alpha * nx;
+                    vy -= 2 * alpha * ny;
+                    vz -= 2 * alpha * nz;
+                    if (st.coated) r.f *= st.coat_r;
+                } else {
+                    // src/batoid.cpp:453-499
+                    const double n1 = 1 / sqrt(vx * vx + vy * vy + vz * vz);
+                    const double nvx = vx * n1, nvy = vy * n1, nvz = vz * n1;
+                    double alpha = nvx * nx + nvy * ny + nvz * nz;
+                    if (alpha > 0.) {
+                        nx = -nx; ny = -ny; nz = -nz;
+                        alpha = -alpha;
+                    }
+                    double n2;
+                    const int mi = st.medium;
+                    if (P.media[mi].kind == BT_M_CONST) {
+                        n2 = P.media[mi].p[0];
+                    } else if (mi == cached_medium) {
+                        n2 = cached_n;   // same medium, same wavelength: same value
+                    } else {
+                        n2 = bt_getN(P, mi, r.w);
+                        cached_medium = mi;
+                        cached_n = n2;
+                    }
+                    const double eta = n1 / n2;
+                    const double sinsqr = eta * eta * (1 - alpha * alpha);
+                    if (sinsqr > 1.0) {
+                        vx = NAN; vy = NAN; vz = NAN;
+                        r.fail = true;
+                        r.vig = true;
+                    } else {
+                        const double nfactor = eta * alpha + sqrt(1 - sinsqr);
+                        vx = (eta * nvx - nfactor * nx) / n2;
+                        vy = (eta * nvy - nfactor * ny) / n2;
+                        vz = (eta * nvz - nfactor * nz) / n2;
+                    }
+                    if (st.coated) r.f *= st.coat_t;
+                }
+            }
+            r.x = x; r.y = y; r.z = z;
+            r.vx = vx; r.vy = vy; r.vz = vz;
+            r.t = t;
+        } else {
+            r.fail = true;
+            r.vig = true;
+        }
+    }
+    if (st.obsc_end > st.obsc_begin) {
+        // src/batoid.cpp:169-171: vignetted |= contains(x, y), for every ray
+        if (bt_obsc_run(P, st.obsc_begin, st.obsc_end, r.x, r.y)) r.vig = true;
+    }
+}
+
+__global__ void __launch_bounds__(TRACE_THREADS)
+k_trace(const unsigned char* __restrict__ gblob, int blob_bytes, RV in, RV out,
+        const __grid_constant__ SnapSet snaps, int nsnaps, int niter) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bar;
+    if (!bt_stage_blob(smem, gblob, blob_bytes, &bar)) return;
+    const Prog P = prog_from_blob(smem);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < in.n; i += stride) {
+        RayState r;
+        r.x = in.x[i];
+        r.y = in.y[i];
+        r.z = in.z[i];
+        r.vx = in.vx[i];
+        r.vy = in.vy[i];
+        r.vz = in.vz[i];
+        r.t = in.t[i];
+        r.w = in.w[i];
+        r.f = in.f[i];
+        r.vig = in.vig[i] != 0;
+        r.fail = in.fail[i] != 0;
+        int cached_medium = -1;
+        double cached_n = 0.0;
+        for (int s = 0; s < P.nstages; s++) {
+            run_stage(P, P.stages[s], r, niter, cached_medium, cached_n);
+            if (s < nsnaps) store_ray(snaps.s[s], i, r);
+        }
+        if (nsnaps == 0) store_ray(out, i, r);
+    }
+}
+
+static int g_sm_count = 0;
+
+int bt_sm_count() {
+    if (g_sm_count == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sm_count <= 0) g_sm_count = 1;
+    }
+    return g_sm_count;
+}
+
+static int grid_for(long long n, int threads, int per_sm) {
+    long long need = (n + threads - 1) / threads;
+    long long cap = (long long)bt_sm_count() * per_sm;
+    if (need > cap) need = cap;
+    if (need < 1) need = 1;
+    return (int)need;
+}
+
+cudaError_t bt_launch_trace(const unsigned char* d_blob, int blob_bytes, const RV& in, const RV& out,
+                            const SnapSet* snaps, int nsnaps, int niter, cudaStream_t stream) {
+    if (in.n <= 0) return cudaSuccess;
+    static SnapSet empty;
+    const SnapSet& ss = snaps ? *snaps : empty;
+    if (blob_bytes > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_trace, cudaFuncAttributeMaxDynamicSharedMemorySize, blob_bytes);
+        if (e != cudaSuccess) return e;
+    }
+    // Persistent grid: the blob is staged once per block and amortised over
+    // the grid-stride loop.
+    const int grid = grid_for(in.n, TRACE_THREADS, 16);
+    k_trace<<<grid, TRACE_THREADS, blob_bytes, stream>>>(d_blob, blob_bytes, in, out, ss, nsnaps, niter);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Surface sag / normal, medium index and obscuration evaluated on arrays.
+// Each takes a one-surface / one-medium / one-obscuration program.
+// ---------------------------------------------------------------------------
+
+__global__ void k_surface_eval(const unsigned char* __restrict__ gblob, int blob_bytes, const double* x,
+                               const double* y, double* sag, double* normal, long long n) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bar;
+    if (!bt_stage_blob(smem, gblob, blob_bytes, &bar)) return;
+    const Prog P = prog_from_blob(smem);
+    const int si = P.stages[0].surf;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double xx = x[i], yy = y[i];
+        if (sag) {
+            double s, ux, uy;
+            bt_surf_eval(P, si, xx, yy, true, false, &s, &ux, &uy);
+            sag[i] = s;
+        }
+        if (normal) {
+            double nx, ny, nz;
+            bt_surf_normal(P, si, xx, yy, &nx, &ny, &nz);
+            normal[i] = nx;
+            normal[i + n] = ny;
+            normal[i + 2 * n] = nz;
+        }
+    }
+}
+
+cudaError_t bt_launch_surface_eval(const unsigned char* d_blob, int blob_bytes, const double* x,
+                                   const double* y, double* sag, double* normal, long long n,
+                                   cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    if (blob_bytes > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_surface_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, blob_bytes);
+        if (e != cudaSuccess) return e;
+    }
+    k_surface_eval<<<grid_for(n, 256, 8), 256, blob_bytes, stream>>>(d_blob, blob_bytes, x, y, sag, normal, n);
+    return cudaGetLastError();
+}
+
+__global__ void k_getN(const unsigned char* __restrict__ gblob, int blob_bytes, const double* w, double* out,
+                       long long n) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bar;
+    if (!bt_stage_blob(smem, gblob, blob_bytes, &bar)) return;
+    const Prog P = prog_from_blob(smem);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        out[i] = bt_getN(P, 0, w[i]);
+}
+
+cudaError_t bt_launch_getN(const unsigned char* d_blob, int blob_bytes, const double* w, double* out,
+                           long long n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    k_getN<<<grid_for(n, 256, 8), 256, blob_bytes, stream>>>(d_blob, blob_bytes, w, out, n);
+    return cudaGetLastError();
+}
+
+// Either fills out[i] = contains(x[i], y[i]) or, given a ray bundle, applies
+// vignetted |= contains(x, y) (src/batoid.cpp:151-172).
+__global__ void k_obsc(const unsigned char* __restrict__ gblob, int blob_bytes, const double* x, const double* y,
+                       uint8_t* out, RV rv, int use_rv, long long n) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bar;
+    if (!bt_stage_blob(smem, gblob, blob_bytes, &bar)) return;
+    const Prog P = prog_from_blob(smem);
+    const bt_stage& st = P.stages[0];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (use_rv) {
+            if (bt_obsc_run(P, st.obsc_begin, st.obsc_end, rv.x[i], rv.y[i])) rv.vig[i] = 1;
+        } else {
+            out[i] = bt_obsc_run(P, st.obsc_begin, st.obsc_end, x[i], y[i]) ? 1 : 0;
+        }
+    }
+}
+
+cudaError_t bt_launch_obsc(const unsigned char* d_blob, int blob_bytes, const double* x, const double* y,
+                           uint8_t* out, const RV* rv, long long n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    RV dummy = {};
+    k_obsc<<<grid_for(n, 256, 8), 256, blob_bytes, stream>>>(d_blob, blob_bytes, x, y, out, rv ? *rv : dummy,
+                                                             rv ? 1 : 0, n);
+    return cudaGetLastError();
+}

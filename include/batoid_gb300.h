@@ -1,0 +1,235 @@
+/*
+ * batoid_gb300 — C-ABI of the GB300-native sequential ray tracer.
+ *
+ * This header is the drop-in boundary that replaces the reference's pybind11
+ * module `batoid._batoid` (pysrc/batoid.cpp:31-154 of jmeyers314/batoid).  Each
+ * entry point below names the reference interface it replaces.
+ *
+ * Conventions
+ *  - Every function returns an int status: BT_OK (0) or one of BT_ERR_*;
+ *    bt_last_error() returns a message for the last failure in this thread.
+ *  - Ray arrays and output arrays are DEVICE pointers (CUDA global memory of
+ *    the current device) unless a function says "host".  The library never
+ *    takes ownership of them (the reference's DualView also wraps caller
+ *    memory: src/dualView.cpp:5-10).
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *    stream).  Launches are stream-ordered and asynchronous; functions that
+ *    return a host value synchronise the stream first.
+ *  - `max_threads` is accepted for signature compatibility with the
+ *    reference and ignored; `niter` is the Newton iteration cap
+ *    (batoid/global_vars.py:9).
+ *  - Per-ray failures are data, as in the reference: the `failed` and
+ *    `vignetted` flags and NaN directions (src/batoid.cpp:264-267, 482-487).
+ *  - Rotation matrices `drot` are 9 doubles, column-major, exactly as the
+ *    reference passes `CoordTransform.drot.ravel()` (include/batoid.h:13).
+ */
+#ifndef BATOID_GB300_H
+#define BATOID_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BT_OK 0
+#define BT_ERR_ARG 1          /* invalid argument */
+#define BT_ERR_CUDA 2         /* CUDA runtime error */
+#define BT_ERR_UNSUPPORTED 3  /* valid but unsupported configuration */
+#define BT_ERR_RANK 4         /* rank-deficient least-squares system */
+#define BT_ERR_TIMEOUT 5      /* a bounded device wait expired */
+#define BT_ERR_ALLOC 6        /* device allocation failed */
+
+/* Structure-of-arrays ray bundle, 74 bytes per ray.
+ * Replaces CPPRayVector(x, y, z, vx, vy, vz, t, wavelength, flux, vignetted,
+ * failed, N) (pysrc/rayVector.cpp:32-62; include/rayVector.h:8-39).
+ * Flags are one byte each (C/C++ bool). */
+typedef struct bt_rayvector {
+    double* x;
+    double* y;
+    double* z;
+    double* vx;
+    double* vy;
+    double* vz;
+    double* t;
+    double* wavelength;
+    double* flux;
+    uint8_t* vignetted;
+    uint8_t* failed;
+    size_t size;
+} bt_rayvector;
+
+typedef struct bt_surface bt_surface;
+typedef struct bt_table bt_table;
+typedef struct bt_medium_h bt_medium_h;
+typedef struct bt_obscuration bt_obscuration;
+typedef struct bt_coating bt_coating;
+typedef struct bt_optic bt_optic;
+
+/* ---- library ----------------------------------------------------------- */
+const char* bt_last_error(void);
+int bt_version(void);
+/* Number of SMs of the current device (used to size persistent grids). */
+int bt_device_sm_count(int* out);
+
+/* ---- surfaces (pysrc/{plane,tilted,sphere,paraboloid,quadric,asphere,
+ *      polynomialSurface,table,bicubic,sum}.cpp) ----------------------------- */
+int bt_plane_create(bt_surface** out);                                /* CPPPlane()            pysrc/plane.cpp */
+int bt_tilted_create(double tanx, double tany, bt_surface** out);     /* CPPTilted(tanx, tany) pysrc/tilted.cpp */
+int bt_sphere_create(double R, bt_surface** out);                     /* CPPSphere(R)          pysrc/sphere.cpp */
+int bt_paraboloid_create(double R, bt_surface** out);                 /* CPPParaboloid(R)      pysrc/paraboloid.cpp */
+int bt_quadric_create(double R, double conic, bt_surface** out);      /* CPPQuadric(R, conic)  pysrc/quadric.cpp */
+/* CPPAsphere(R, conic, coef_ptr, n) (pysrc/asphere.cpp:11-24); coefs are the
+ * padded host array whose entry i multiplies r^(2i+2). */
+int bt_asphere_create(double R, double conic, const double* coefs, size_t n, bt_surface** out);
+/* CPPPolynomialSurface(coefs, gradx, grady, xorigin, yorigin, xsize, ysize)
+ * (pysrc/polynomialSurface.cpp:10-28); host arrays, coefs [ysize][xsize],
+ * gradients [(ysize-1)][(xsize-1)]. */
+int bt_polynomial_create(const double* coefs, const double* gradx, const double* grady,
+                         double xorigin, double yorigin, size_t xsize, size_t ysize,
+                         bt_surface** out);
+/* CPPTable(x0, y0, dx, dy, z, dzdx, dzdy, d2zdxdy, nx, ny, use_nan)
+ * (pysrc/table.cpp:10-33); host arrays [ny][nx], copied to device memory
+ * owned by the table. */
+int bt_table_create(double x0, double y0, double dx, double dy,
+                    const double* z, const double* dzdx, const double* dzdy, const double* d2zdxdy,
+                    size_t nx, size_t ny, int use_nan, bt_table** out);
+void bt_table_destroy(bt_table* table);
+/* CPPBicubic(table) (pysrc/bicubic.cpp); the table must outlive the surface. */
+int bt_bicubic_create(const bt_table* table, bt_surface** out);
+/* CPPSum(list) (pysrc/sum.cpp:11-19); children are copied by value, so they
+ * may be destroyed afterwards.  Children may not themselves be Sums. */
+int bt_sum_create(const bt_surface* const* surfaces, size_t n, bt_surface** out);
+void bt_surface_destroy(bt_surface* s);
+/* Surface.sag (pysrc/surface.cpp:10; py::vectorize(&Surface::sag)): device arrays. */
+int bt_surface_sag(const bt_surface* s, const double* x, const double* y, double* out, size_t n, void* stream);
+/* Surface.normal (pysrc/surface.cpp:11-21): out holds nx[0..n), ny[0..n), nz[0..n). */
+int bt_surface_normal(const bt_surface* s, const double* x, const double* y, double* out, size_t n, void* stream);
+
+/* ---- media (pysrc/medium.cpp; src/medium.cpp) ---------------------------- */
+int bt_const_medium_create(double n, bt_medium_h** out);                                   /* CPPConstMedium */
+int bt_table_medium_create(const double* wavelengths, const double* ns, size_t n, bt_medium_h** out); /* CPPTableMedium */
+int bt_sellmeier_medium_create(double B1, double B2, double B3, double C1, double C2, double C3,
+                               bt_medium_h** out);                                         /* CPPSellmeierMedium */
+int bt_sumita_medium_create(double A0, double A1, double A2, double A3, double A4, double A5,
+                            bt_medium_h** out);                                            /* CPPSumitaMedium */
+int bt_air_create(double pressure, double temperature, double h2o_pressure, bt_medium_h** out); /* CPPAir */
+void bt_medium_destroy(bt_medium_h* m);
+/* Medium.getN over a device array of wavelengths. */
+int bt_medium_getN(const bt_medium_h* m, const double* wavelength, double* out, size_t n, void* stream);
+
+/* ---- obscurations (pysrc/obscuration.cpp; src/obscuration.cpp) ---------- */
+int bt_obsc_circle_create(double radius, double x0, double y0, bt_obscuration** out);
+int bt_obsc_annulus_create(double inner, double outer, double x0, double y0, bt_obscuration** out);
+int bt_obsc_rectangle_create(double width, double height, double x0, double y0, double theta, bt_obscuration** out);
+int bt_obsc_ray_create(double width, double theta, double x0, double y0, bt_obscuration** out);
+int bt_obsc_polygon_create(const double* xs, const double* ys, size_t n, bt_obscuration** out);
+int bt_obsc_negation_create(const bt_obscuration* original, bt_obscuration** out);
+int bt_obsc_union_create(const bt_obscuration* const* items, size_t n, bt_obscuration** out);
+int bt_obsc_intersection_create(const bt_obscuration* const* items, size_t n, bt_obscuration** out);
+void bt_obsc_destroy(bt_obscuration* o);
+/* Obscuration.contains over device arrays; out is one byte per point. */
+int bt_obsc_contains(const bt_obscuration* o, const double* x, const double* y, uint8_t* out, size_t n, void* stream);
+
+/* ---- coatings (pysrc/coating.cpp) ---------------------------------------- */
+int bt_simple_coating_create(double reflectivity, double transmissivity, bt_coating** out);
+void bt_coating_destroy(bt_coating* c);
+
+/* ---- per-surface trace operations (include/batoid.h:15-42;
+ *      src/batoid.cpp:8-506) -------------------------------------------------- */
+int bt_apply_forward_transform(const double dr[3], const double drot[9], const bt_rayvector* rv,
+                               int max_threads, void* stream);           /* src/batoid.cpp:71-108 */
+int bt_apply_reverse_transform(const double dr[3], const double drot[9], const bt_rayvector* rv,
+                               int max_threads, void* stream);           /* src/batoid.cpp:111-148 */
+int bt_apply_forward_transform_arrays(const double dr[3], const double drot[9],
+                                      double* x, double* y, double* z, size_t n,
+                                      int max_threads, void* stream);    /* src/batoid.cpp:8-22 */
+int bt_apply_reverse_transform_arrays(const double dr[3], const double drot[9],
+                                      double* x, double* y, double* z, size_t n,
+                                      int max_threads, void* stream);    /* src/batoid.cpp:24-38 */
+int bt_finish_parallel(const double dr[3], const double drot[9], const double vv[3],
+                       double* x, double* y, double* z, size_t n, void* stream); /* src/batoid.cpp:40-69 */
+int bt_obscure(const bt_obscuration* o, const bt_rayvector* rv, int max_threads, void* stream); /* src/batoid.cpp:151-172 */
+int bt_intersect(const bt_surface* s, const double dr[3], const double drot[9], const bt_rayvector* rv,
+                 const bt_coating* coating, int max_threads, int niter, void* stream); /* src/batoid.cpp:175-270 */
+int bt_reflect(const bt_surface* s, const double dr[3], const double drot[9], const bt_rayvector* rv,
+               const bt_coating* coating, int max_threads, int niter, void* stream);   /* src/batoid.cpp:273-378 */
+int bt_refract(const bt_surface* s, const double dr[3], const double drot[9],
+               const bt_medium_h* m1, const bt_medium_h* m2, const bt_rayvector* rv,
+               const bt_coating* coating, int max_threads, int niter, void* stream);   /* src/batoid.cpp:381-506 */
+
+/* ---- RayVector methods (include/rayVector.h:10-25; src/rayVector.cpp) ---- */
+int bt_rv_position_at_time(const bt_rayvector* rv, double t, double* xout, double* yout, double* zout,
+                           int max_threads, void* stream);   /* src/rayVector.cpp:26-54 */
+int bt_rv_propagate_in_place(const bt_rayvector* rv, double t, int max_threads, void* stream); /* :56-82 */
+int bt_rv_phase(const bt_rayvector* rv, double x, double y, double z, double t, double* out,
+                int max_threads, void* stream);              /* :84-122 */
+/* out: interleaved (re, im) doubles, 2n entries (std::complex<double> layout). */
+int bt_rv_amplitude(const bt_rayvector* rv, double x, double y, double z, double t, double* out,
+                    int max_threads, void* stream);          /* :124-166 */
+/* Synchronous; host out[2] = (re, im).  src/rayVector.cpp:169-222 */
+int bt_rv_sum_amplitude(const bt_rayvector* rv, double x, double y, double z, double t,
+                        int ignore_vignetted, int max_threads, double* out, void* stream);
+/* Synchronous; host *out = 1 if every field of every ray is bitwise equal (:224-238). */
+int bt_rv_equal(const bt_rayvector* a, const bt_rayvector* b, int* out, void* stream);
+
+/* ---- fused optic trace (replaces the per-surface Python loop of
+ *      CompoundOptic.trace/traceFull, batoid/optic.py:1013-1182) ------------ */
+#define BT_STAGE_INTERSECT 0   /* Detector, Baffle, Interface (batoid/optic.py:541-546) */
+#define BT_STAGE_REFLECT 1     /* Mirror (batoid/optic.py:814-816) */
+#define BT_STAGE_REFRACT 2     /* RefractiveInterface (batoid/optic.py:776-781) */
+/* Packs nstages interfaces, in trace order, into a device-resident program.
+ * Per stage: kind, surface, transform from the previous stage's frame
+ * (dr 3 doubles, drot 9 doubles column-major), outgoing medium (REFRACT
+ * only, else NULL), obscuration (nullable) and coating (nullable). */
+int bt_optic_create(size_t nstages, const int* kinds, const bt_surface* const* surfaces,
+                    const double* dr, const double* drot,
+                    const bt_medium_h* const* media, const bt_obscuration* const* obscurations,
+                    const bt_coating* const* coatings, bt_optic** out);
+void bt_optic_destroy(bt_optic* o);
+int bt_optic_nstages(const bt_optic* o, int* out);
+/* In-place trace of all stages in one launch (CompoundOptic.trace). */
+int bt_optic_trace(const bt_optic* o, const bt_rayvector* rv, int niter, void* stream);
+/* traceFull: rv is read only; snaps[k] receives the rays after stage k
+ * (CompoundOptic.traceFull's per-interface 'out' copies). */
+int bt_optic_trace_full(const bt_optic* o, const bt_rayvector* rv, const bt_rayvector* snaps,
+                        int niter, void* stream);
+/* End-to-end trace of HOST arrays (pinned for overlap): copies in, traces
+ * and copies out, pipelined in chunks of `chunk` rays over device scratch
+ * buffers that the library allocates.  Synchronous. */
+int bt_optic_trace_host(const bt_optic* o, const bt_rayvector* host_rv, int niter, size_t chunk,
+                        void* stream);
+
+/* ---- Huygens PSF (replaces the per-pixel sumAmplitude loop of huygensPSF,
+ *      batoid/analysis.py:296-304) --------------------------------------------
+ * Amplitude at lattice points P(a, b) = (px, py, pz) + (b - nb/2)*p0 + (a - na/2)*p1
+ * (integer division; p0 = (lat[0], lat[1], 0), p1 = (lat[2], lat[3], 0)),
+ * a in [0, na), b in [0, nb), as the reference's transposed Lattice coords.
+ * Phases are reduced modulo 2*pi in FP64 per ray; the per-pixel phasor
+ * sum runs in FP32 with compensated summation.  Outputs: device arrays of
+ * na*nb doubles (re, im), row-major [a][b]. */
+int bt_huygens_amplitudes(const bt_rayvector* rv, double px, double py, double pz,
+                          const double lat[4], int na, int nb, double t0, int ignore_vignetted,
+                          double* out_re, double* out_im, void* stream);
+
+/* ---- Zernike wavefront fit (batoid/analysis.py:563-573) ------------------
+ * Normal equations of nfits independent least-squares fits, one CUDA block
+ * per fit.  Fit f uses points [offsets[f], offsets[f+1]) of x, y (pupil
+ * coordinates) and v (wavefront values).  basis: jmax polynomials, each a
+ * side x side array C[a][b] of x^a y^b coefficients (Z_1..Z_jmax).
+ * Outputs G (nfits x jmax x jmax, symmetric) and b (nfits x jmax).  All
+ * pointers are device pointers; offsets are int64.  jmax <= 64, side <= 12. */
+int bt_zernike_normal_equations(const double* x, const double* y, const double* v, const long long* offsets,
+                                int nfits, const double* basis, int jmax, int side, double* G, double* b,
+                                void* stream);
+
+/* Reads and clears the device status word of the blob-staging kernels:
+ * BT_ERR_TIMEOUT if a kernel's bounded wait for its descriptor copy expired
+ * (that kernel then left every ray untouched).  Synchronous. */
+int bt_check_device_status(void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BATOID_GB300_H */

@@ -1,0 +1,254 @@
+"""Generate the golden fixtures in tests/golden/ by running the REFERENCE.
+
+Run in a container that has the reference sources and its compiled module
+(oracle/Makefile.ref builds oracle/_ref/_batoid*.so from them):
+
+    make -f oracle/Makefile.ref -j8
+    python tests/golden/make_golden.py [/path/to/reference]
+
+Every fixture stores seeded inputs and the reference's outputs for them.
+The inputs are regenerated from the same seeds by the tests, so only the
+outputs strictly need storing; the inputs are stored too so that a test
+can tell an input-generation drift from a compute mismatch.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from ref_import import import_reference  # noqa: E402
+from batoid_gb300 import workloads as W  # noqa: E402
+from batoid_gb300 import zpoly as ZK  # noqa: E402
+
+FIELDS = ("x", "y", "z", "vx", "vy", "vz", "t", "wavelength", "flux", "vignetted", "failed")
+
+
+def ref_zernike_factory(batoid):
+    """A reference PolynomialSurface holding the same Cartesian arrays this
+    package builds (GalSim, which the reference's Zernike needs, is absent)."""
+    def make(coef, R_outer, R_inner):
+        C = ZK.zernike_xy(coef, R_outer, R_inner)
+        gx, gy = ZK.grad_xy(C)
+        z = batoid.Zernike.__new__(batoid.Zernike)
+        z.coef = np.asarray(coef, dtype=float)
+        z.R_outer, z.R_inner, z.x_origin, z.y_origin = R_outer, R_inner, 0.0, 0.0
+        z._xycoef = np.ascontiguousarray(C)
+        z._xycoef_gradx = np.ascontiguousarray(gx)
+        z._xycoef_grady = np.ascontiguousarray(gy)
+        z._surface = batoid._batoid.CPPPolynomialSurface(
+            z._xycoef.ctypes.data, z._xycoef_gradx.ctypes.data, z._xycoef_grady.ctypes.data, 0.0, 0.0,
+            C.shape[0], C.shape[1])
+        return z
+    return make
+
+
+def rv_to_dict(rv, prefix):
+    return {f"{prefix}_{k}": np.array(getattr(rv, k)) for k in FIELDS}
+
+
+def make_rv(batoid, arrs):
+    return batoid.RayVector(*[np.array(a) for a in arrs])
+
+
+def workload_fixtures(batoid):
+    out = {}
+    # f/4 paraboloid: full trace and traceFull
+    opt = W.paraboloid_optic(batoid)
+    arrs = W.paraboloid_rays(4096, seed=57721)
+    rv = make_rv(batoid, arrs)
+    tf = opt.traceFull(rv)
+    for k, v in tf.items():
+        out.update(rv_to_dict(v["out"], f"paraboloid_{k}"))
+    rv2 = make_rv(batoid, arrs)
+    opt.trace(rv2)
+    out.update(rv_to_dict(rv2, "paraboloid_final"))
+    # sumAmplitude / phase at a few points on the traced rays
+    pts = np.array([[0.0, 0.0, 0.0], [1e-5, -2e-5, 0.0], [3e-4, 1e-4, 1e-6]])
+    t0 = float(rv2.t[0])
+    out["paraboloid_amp_points"] = pts
+    out["paraboloid_amp_t0"] = np.array(t0)
+    out["paraboloid_sumamp"] = np.array([rv2.sumAmplitude(p, t0) for p in pts])
+    out["paraboloid_sumamp_all"] = np.array([rv2.sumAmplitude(p, t0, ignoreVignetted=False) for p in pts])
+    out["paraboloid_phase"] = rv2.phase(pts[1], t0)
+    out["paraboloid_amplitude"] = rv2.amplitude(pts[1], t0)
+    out["paraboloid_pos_at_time"] = rv2.positionAtTime(t0 + 0.01)
+
+    # 12-surface system
+    opt = W.tma_optic(batoid, zernike_factory=ref_zernike_factory(batoid))
+    arrs = W.tma_rays(2048, seed=8675309)
+    rv = make_rv(batoid, arrs)
+    tf = opt.traceFull(rv)
+    out["tma_names"] = np.array(list(tf.keys()))
+    for k, v in tf.items():
+        out.update(rv_to_dict(v["out"], f"tma_{k}"))
+    return out
+
+
+def huygens_fixture(batoid):
+    """Reference Huygens amplitudes on a small lattice (the per-pixel
+    sumAmplitude loop of batoid/analysis.py:296-304)."""
+    out = {}
+    opt = W.tma_optic(batoid, zernike_factory=ref_zernike_factory(batoid))
+    for case, (tx, ty, w, nx, npix) in enumerate([(0.0, 0.0, 500e-9, 64, 24), (0.01, -0.015, 870e-9, 48, 16)]):
+        dirCos = batoid.utils.fieldToDirCos(tx, ty)
+        rays = batoid.RayVector.asGrid(optic=opt, wavelength=w, dirCos=dirCos, nx=nx)
+        opt.trace(rays)
+        cridx = (nx // 2) * nx + nx // 2
+        point = rays.r[cridx]
+        prim = np.array([[2e-6, 0.0], [0.0, 2e-6]])
+        lat = batoid.Lattice(np.zeros((npix, npix)), prim)
+        xs = lat.coords[..., 0].T + point[0]
+        ys = lat.coords[..., 1].T + point[1]
+        t0 = rays.t[0]
+        amps = np.zeros((npix, npix), dtype=np.complex128)
+        for idx in np.ndindex(amps.shape):
+            amps[idx] = rays.sumAmplitude(np.array([xs[idx], ys[idx], 0.0]), t0)
+        p = f"huy{case}"
+        out[f"{p}_params"] = np.array([tx, ty, w, nx, npix])
+        out[f"{p}_point"] = point
+        out[f"{p}_t0"] = np.array(t0)
+        out[f"{p}_amps"] = amps
+        out.update(rv_to_dict(rays, f"{p}_rays"))
+    return out
+
+
+def surfaces(batoid, rng):
+    """(name, surface) pairs covering every surface kind."""
+    zf = ref_zernike_factory(batoid)
+    xs = np.linspace(-1.1, 1.1, 40)
+    ys = np.linspace(-1.2, 1.2, 44)
+    X, Y = np.meshgrid(xs, ys)
+    Zt = 0.01 * np.cos(1.3 * X) * np.sin(0.9 * Y) + 0.003 * X * X
+    bic = batoid.Bicubic(xs, ys, Zt)
+    bic0 = batoid.Bicubic(xs, ys, Zt, nanpolicy='zero')
+    zc = np.zeros(23)
+    zc[4:] = rng.normal(0, 1e-4, 19)
+    return [
+        ("plane", batoid.Plane()),
+        ("tilted", batoid.Tilted(0.01, -0.02)),
+        ("sphere", batoid.Sphere(5.3)),
+        ("sphere_neg", batoid.Sphere(-4.1)),
+        ("paraboloid", batoid.Paraboloid(3.7)),
+        ("quadric", batoid.Quadric(6.1, -0.7)),
+        ("quadric_obl", batoid.Quadric(-8.2, 0.4)),
+        ("asphere", batoid.Asphere(7.5, -1.1, [1e-4, -2e-5, 3e-7, -1e-8])),
+        ("zernike", zf(zc, 1.3, 0.4)),
+        ("bicubic", bic),
+        ("bicubic_zero", bic0),
+        ("sum_asphere_zernike", batoid.Sum([batoid.Asphere(9.0, -0.9, [2e-5, -1e-7]), zf(zc, 1.5, 0.0)])),
+        ("sum_quadric_bicubic", batoid.Sum([batoid.Quadric(8.0, -0.5), bic])),
+        ("sum_tilted_sphere", batoid.Sum([batoid.Tilted(0.005, 0.003), batoid.Sphere(20.0)])),
+    ]
+
+
+def primitive_fixtures(batoid):
+    rng = np.random.default_rng(31415)
+    out = {}
+    silica = batoid.SellmeierMedium(*W.SILICA)
+    vac = batoid.ConstMedium(1.0)
+    coat = batoid.SimpleCoating(0.2, 0.7)
+    for name, s in surfaces(batoid, rng):
+        n = 256
+        x = rng.uniform(-0.9, 0.9, n)
+        y = rng.uniform(-0.9, 0.9, n)
+        out[f"surf_{name}_xy"] = np.stack([x, y])
+        out[f"surf_{name}_sag"] = s.sag(x, y)
+        out[f"surf_{name}_normal"] = s.normal(x, y)
+        # rays from above with mild tilt, some steep ones to fail
+        vx = rng.normal(0, 0.1, n)
+        vy = rng.normal(0, 0.1, n)
+        vx[:12] = rng.uniform(0.9, 0.99, 12)
+        vy[:12] = 0.0
+        vz = -np.sqrt(1 - vx * vx - vy * vy)
+        z = np.full(n, 1.0)
+        wl = rng.choice(W.WAVELENGTHS, n)
+        origin = rng.normal(0, 0.01, 3)
+        rot = batoid.RotX(rng.normal(0, 0.01)) @ batoid.RotY(rng.normal(0, 0.01))
+        cs = batoid.CoordSys(origin=origin, rot=rot)
+        out[f"surf_{name}_cs"] = np.concatenate([origin, rot.ravel()])
+        inputs = (x, y, z, vx, vy, vz, np.zeros(n), wl, np.ones(n), np.zeros(n, bool), np.zeros(n, bool))
+        for k, f in enumerate(FIELDS):
+            out[f"surf_{name}_in_{f}"] = np.array(inputs[k])
+        for op in ("intersect", "reflect", "refract", "reflect_coated", "refract_rev"):
+            rv = make_rv(batoid, inputs)
+            if op == "intersect":
+                s.intersect(rv, coordSys=cs)
+            elif op == "reflect":
+                s.reflect(rv, coordSys=cs)
+            elif op == "reflect_coated":
+                s.reflect(rv, coordSys=cs, coating=coat)
+            elif op == "refract":
+                s.refract(rv, vac, silica, coordSys=cs)
+            else:
+                # from glass into vacuum at steep incidence: exercises TIR
+                rv2 = make_rv(batoid, inputs)
+                rv2 = batoid.RayVector(rv2.x, rv2.y, rv2.z, rv2.vx / 1.45, rv2.vy / 1.45, rv2.vz / 1.45,
+                                       rv2.t, rv2.wavelength, rv2.flux)
+                rv = rv2
+                s.refract(rv, silica, vac, coordSys=cs)
+            out.update(rv_to_dict(rv, f"surf_{name}_{op}"))
+    # obscurations
+    pts = rng.uniform(-1.5, 1.5, (2, 5000))
+    obscs = {
+        "circle": batoid.ObscCircle(0.7, 0.1, -0.2),
+        "annulus": batoid.ObscAnnulus(0.3, 0.9, -0.05, 0.02),
+        "rectangle": batoid.ObscRectangle(1.1, 0.4, 0.1, 0.2, 0.3),
+        "ray": batoid.ObscRay(0.2, 0.7, -0.1, 0.05),
+        "polygon": batoid.ObscPolygon([0.0, 1.0, 0.3, -0.8, -0.4], [-1.0, 0.2, 1.1, 0.6, -0.5]),
+        "negation": batoid.ObscNegation(batoid.ObscCircle(0.5)),
+        "union": batoid.ObscUnion([batoid.ObscCircle(0.3, 0.5, 0.5), batoid.ObscRectangle(0.5, 2.0),
+                                   batoid.ObscRay(0.1, 2.0)]),
+        "intersection": batoid.ObscIntersection([batoid.ObscCircle(1.0), batoid.ObscNegation(batoid.ObscCircle(0.4)),
+                                                 batoid.ObscRectangle(1.6, 1.2, 0.0, 0.0, -0.2)]),
+    }
+    out["obsc_pts"] = pts
+    for k, o in obscs.items():
+        out[f"obsc_{k}"] = np.array([o.contains(a, b) for a, b in zip(pts[0], pts[1])])
+    # media
+    wl = np.concatenate([np.linspace(300e-9, 1100e-9, 50), W.WAVELENGTHS])
+    out["media_wavelengths"] = wl
+    out["media_sellmeier"] = silica.getN(wl)
+    sumita = batoid.SumitaMedium(2.2705778, -0.010059376, 0.010414999, 0.00028872517, -2.2214495e-05,
+                                 1.4258559e-06)
+    out["media_sumita"] = sumita.getN(wl)
+    air = batoid.Air()
+    out["media_air"] = air.getN(wl)
+    air2 = batoid.Air(pressure=60.0, temperature=280.0, h2o_pressure=0.5)
+    out["media_air2"] = air2.getN(wl)
+    tw = np.linspace(320e-9, 1080e-9, 17)
+    tn = 1.45 + 0.01 * np.cos(tw * 1e7)
+    table = batoid.TableMedium(tw, tn)
+    out["media_table_args"] = np.stack([tw, tn])
+    out["media_table"] = np.array([table.getN(w) for w in wl])
+    return out
+
+
+def sellmeier_csv_fixture(ref_root):
+    """The reference's known-answer vectors for Sellmeier silica
+    (tests/test_Medium.py:66-102, testdata/silicaDispersion.csv)."""
+    path = os.path.join(ref_root, "tests", "testdata", "silicaDispersion.csv")
+    wmicron, ncsv = np.loadtxt(path, delimiter=',').T
+    return {"csv_wmicron": wmicron, "csv_n": ncsv}
+
+
+def main():
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    os.environ["BATOID_REF"] = ref_root
+    batoid = import_reference(ref_root)
+    batoid.global_vars._batoid_max_threads = 1
+    np.savez_compressed(os.path.join(HERE, "workloads.npz"), **workload_fixtures(batoid))
+    np.savez_compressed(os.path.join(HERE, "primitives.npz"), **primitive_fixtures(batoid))
+    np.savez_compressed(os.path.join(HERE, "huygens.npz"), **huygens_fixture(batoid))
+    np.savez_compressed(os.path.join(HERE, "sellmeier_csv.npz"), **sellmeier_csv_fixture(ref_root))
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()
