@@ -116,11 +116,13 @@ _SIGS = [
     ("bt_optic_destroy", None, [_P]),
     ("bt_optic_nstages", c_int, [_P, ctypes.POINTER(c_int)]),
     ("bt_optic_trace", c_int, [_P, ctypes.POINTER(BtRayVector), c_int, _P]),
+    ("bt_optic_trace_into", c_int, [_P, ctypes.POINTER(BtRayVector), ctypes.POINTER(BtRayVector), c_int, _P]),
     ("bt_optic_trace_full", c_int, [_P, ctypes.POINTER(BtRayVector), ctypes.POINTER(BtRayVector), c_int, _P]),
     ("bt_optic_trace_host", c_int, [_P, ctypes.POINTER(BtRayVector), c_int, c_size_t, _P]),
     ("bt_huygens_amplitudes", c_int, [ctypes.POINTER(BtRayVector), c_double, c_double, c_double, c_double_p,
                                       c_int, c_int, c_double, c_int, _P, _P, _P]),
     ("bt_zernike_normal_equations", c_int, [_P, _P, _P, _P, c_int, _P, c_int, c_int, _P, _P, _P]),
+    ("bt_measure_fp64_peak", c_int, [c_int, c_double_p, _P]),
     ("bt_check_device_status", c_int, [_P]),
 ]
 

@@ -429,6 +429,7 @@ __device__ __forceinline__ double bt_getN(const Prog& P, int mi, double w) {
         const double* vals = args + m.n;
         if (w < args[0]) return NAN;
         if (w > args[m.n - 1]) return NAN;
+        if (m.n < 2) return vals[0];  // single entry and w == args[0]
         int u;
         for (u = 1; u < m.n; u++)
             if (w < args[u]) break;

@@ -58,6 +58,7 @@ cudaError_t bt_launch_phase(const RV& rv, double x, double y, double z, double t
 cudaError_t bt_launch_sum_amplitude(const RV& rv, double x, double y, double z, double t, bool ignore_vig,
                                     double* d_out2, cudaStream_t stream);
 cudaError_t bt_launch_rv_equal(const RV& a, const RV& b, int* d_flag, cudaStream_t stream);
+cudaError_t bt_launch_dfma_probe(int iters, double* sink, float* ms, double* flops, cudaStream_t stream);
 
 // huygens.cu
 cudaError_t bt_launch_huygens(const RV& rv, double px, double py, double pz, const double lat[4], int na,

@@ -953,6 +953,22 @@ extern "C" int bt_optic_trace(const bt_optic* o, const bt_rayvector* rv, int nit
     return BT_OK;
 }
 
+extern "C" int bt_optic_trace_into(const bt_optic* o, const bt_rayvector* in, const bt_rayvector* out, int niter,
+                                   void* stream) {
+    if (!o) return fail(BT_ERR_ARG, "trace: null optic");
+    int rc = check_rv(in);
+    if (rc != BT_OK) return rc;
+    rc = check_rv(out);
+    if (rc != BT_OK) return rc;
+    if (in->size != out->size) return fail(BT_ERR_ARG, "trace: input and output sizes differ");
+    if (in->size == 0) return BT_OK;
+    if (niter < 0) return fail(BT_ERR_ARG, "trace: negative niter");
+    CUDA_TRY(bt_launch_trace(o->d_blob, o->blob_bytes, to_rv(in), to_rv(out), nullptr, 0, niter,
+                             (cudaStream_t)stream),
+             "trace");
+    return BT_OK;
+}
+
 extern "C" int bt_optic_trace_full(const bt_optic* o, const bt_rayvector* rv, const bt_rayvector* snaps, int niter,
                                    void* stream) {
     if (!o) return fail(BT_ERR_ARG, "traceFull: null optic");
@@ -1072,6 +1088,21 @@ extern "C" int bt_zernike_normal_equations(const double* x, const double* y, con
     if (!x || !y || !v || !offsets || !basis || !G || !b) return fail(BT_ERR_ARG, "zernike fit: null array");
     CUDA_TRY(bt_launch_zk_normal(x, y, v, offsets, nfits, basis, jmax, side, G, b, (cudaStream_t)stream),
              "zernike fit");
+    return BT_OK;
+}
+
+extern "C" int bt_measure_fp64_peak(int iters, double* tflops, void* stream) {
+    if (!tflops || iters < 8) return fail(BT_ERR_ARG, "fp64 probe: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    double* sink = nullptr;
+    CUDA_TRY(cudaMallocAsync((void**)&sink, sizeof(double), s), "fp64 probe");
+    float ms = 0.f;
+    double flops = 0.0;
+    cudaError_t e = bt_launch_dfma_probe(iters, sink, &ms, &flops, s);
+    cudaFreeAsync(sink, s);
+    cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "fp64 probe");
+    *tflops = flops / (ms * 1e-3) / 1e12;
     return BT_OK;
 }
 

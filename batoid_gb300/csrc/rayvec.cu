@@ -246,3 +246,44 @@ cudaError_t bt_launch_rv_equal(const RV& a, const RV& b, int* d_flag, cudaStream
     k_rv_equal<<<rv_grid(a.n), RV_THREADS, 0, stream>>>(a, b, d_flag);
     return cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------
+// FP64 throughput probe: independent DFMA chains, used by the benchmark to
+// state the FP64-pipe peak this device reaches (the denominator of the
+// tracer's FP64 roofline).
+// ---------------------------------------------------------------------------
+
+#define PROBE_CHAINS 8
+
+__global__ void k_dfma_probe(int iters, double b, double c, double* sink) {
+    double a[PROBE_CHAINS];
+#pragma unroll
+    for (int k = 0; k < PROBE_CHAINS; k++) a[k] = threadIdx.x * 1e-3 + k;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < PROBE_CHAINS; k++) a[k] = fma(a[k], b, c);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < PROBE_CHAINS; k++) s += a[k];
+    if (s == 12345.678) sink[0] = s;  // keeps the chains live
+}
+
+cudaError_t bt_launch_dfma_probe(int iters, double* sink, float* ms, double* flops, cudaStream_t stream) {
+    const int blocks = bt_sm_count() * 8, threads = 256;
+    cudaEvent_t e0, e1;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e != cudaSuccess) return e;
+    cudaEventCreate(&e1);
+    k_dfma_probe<<<blocks, threads, 0, stream>>>(iters / 8, 0.999999, 1e-7, sink);  // warm-up
+    cudaEventRecord(e0, stream);
+    k_dfma_probe<<<blocks, threads, 0, stream>>>(iters, 0.999999, 1e-7, sink);
+    cudaEventRecord(e1, stream);
+    e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+    *flops = 2.0 * PROBE_CHAINS * (double)iters * blocks * threads;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return e;
+}

@@ -1,0 +1,309 @@
+#!/usr/bin/env python
+"""Benchmark: fused FP64 sequential trace of the 12-surface TMA + corrector
+system (16M rays, 6 wavelengths) on one GB300, in ray-surface ops/s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+One step = one out-of-place trace of the whole ray batch (inputs resident in
+HBM, 1.2 GB > L2, so no L2 flush is needed).  Prints one JSON line (rank 0).
+Under torchrun each rank traces its own batch (weak scaling, no collective
+on the data path); the reported time is the max over ranks.
+
+``--impl reference`` times the reference algorithm on the host cores instead:
+the oracle's C restatement of the reference trace (oracle/), all threads, on a
+bounded sample of the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ray-surface ops/s (FP64 trace)"
+UNIT = "ray-surface/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="tma_corrector")
+    p.add_argument("--nrays", type=int, default=16 * 1024 * 1024)
+    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = [r for r in self.rows if len(r) >= 9]
+        sm = [float(r[1]) for r in rows if r[1].replace('.', '', 1).isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace('.', '', 1).isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def time_cpu(workload, nrays, threads=None):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as ora
+    import batoid_gb300 as bt
+    from batoid_gb300 import workloads as W
+    build_optic, make_rays, nsurf = W.WORKLOADS[workload]
+    opt = build_optic(bt)
+    threads = threads or ora.threads()
+    rays = ora.Rays(*make_rays(nrays, seed=1000))
+    t1 = time.perf_counter()
+    ora.trace(opt, rays, nthreads=threads)
+    dt = time.perf_counter() - t1
+    return nrays * nsurf / dt, dt, threads
+
+
+def cpu_baseline(workload, target_s=12.0):
+    """Bounded CPU sample: grow the ray count until one trace takes ~1 s,
+    then repeat to ~target_s of CPU work; report the median throughput."""
+    n = 1 << 16
+    rate, dt, threads = time_cpu(workload, n)
+    while dt < 1.0 and n < (1 << 23):
+        n *= 2
+        rate, dt, threads = time_cpu(workload, n)
+    rates = [rate]
+    spent = dt
+    while spent < target_s:
+        r, d, _ = time_cpu(workload, n, threads)
+        rates.append(r)
+        spent += d
+    return {"value": statistics.median(rates), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{workload}: {n} rays x {len(rates)} repeats ({spent:.1f} s of CPU trace), "
+                      f"oracle C restatement of the reference trace, OpenMP {threads} threads"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    from batoid_gb300 import workloads as W
+    _, _, nsurf = W.WORKLOADS[args.workload]
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as ora
+    # bounded per-step sample sized to ~1-2 s of CPU work
+    n = 1 << 16
+    rate, dt, threads = time_cpu(args.workload, n)
+    while dt < 0.8 and n < (1 << 23):
+        n *= 2
+        rate, dt, threads = time_cpu(args.workload, n)
+    for _ in range(args.warmup):
+        time_cpu(args.workload, n, threads)
+    total = 0.0
+    for _ in range(args.steps):
+        _, d, _ = time_cpu(args.workload, n, threads)
+        total += d
+    value = n * nsurf * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload} (sample of {n} rays per step; full batch {args.nrays})",
+                   "surfaces": nsurf, "l2": "inputs > L2 (host)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n} rays per step, oracle C restatement of the reference trace"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def load_traffic(workload):
+    """Per-ray DRAM traffic of the trace kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "trace_kernel_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d[workload]["dram_bytes_per_ray"]
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import batoid_gb300 as bt
+    from batoid_gb300 import _lib, _device as D, workloads as W, workcount as WC
+    build_optic, make_rays, nsurf = W.WORKLOADS[args.workload]
+    opt = build_optic(bt)
+    n = args.nrays
+    arrs = make_rays(n, seed=4242 + rank)
+    rv_in = bt.RayVector(*arrs)
+    rv_out = bt.RayVector._empty(n)
+    prog = opt._program(rv_in.coordSys)
+    L = _lib.lib()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    niter = bt.global_vars._batoid_niter
+    a, b = rv_in._rv, rv_out._rv
+
+    def step():
+        _lib.check(L.bt_optic_trace_into(prog._optic.ptr, a, b, niter, sp))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    total_rays = n * world
+    value = total_rays * nsurf * args.steps / (ms * 1e-3)
+
+    # sanity: the benchmark traced real rays
+    vig = float(rv_out.field("vignetted").float().mean().item())
+
+    # FP64 roofline of the fused trace kernel (one launch per step)
+    fpeak = ctypes.c_double(0.0)
+    _lib.check(L.bt_measure_fp64_peak(1 << 14, ctypes.byref(fpeak), sp))
+    flops_per_ray = WC.optic_flops_per_ray(opt, niter)
+    achieved_tflops = flops_per_ray * n / (ms_per_step * 1e-3) / 1e12
+    bytes_per_ray = WC.READ_BYTES_PER_RAY + WC.WRITE_BYTES_PER_RAY
+    hbm_gbs = bytes_per_ray * n / (ms_per_step * 1e-3) / 1e9
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    traffic_per_ray = load_traffic(args.workload)
+
+    # end to end through the C-ABI with pinned host buffers
+    host = [torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).pin_memory() for x in arrs[:9]]
+    hflags = [torch.from_numpy(np.ascontiguousarray(x, dtype=np.uint8)).pin_memory() for x in arrs[9:]]
+    pristine = [h.clone() for h in host] + [f.clone() for f in hflags]
+    hrv = _lib.BtRayVector(*[h.data_ptr() for h in host], *[f.data_ptr() for f in hflags], n)
+    chunk = 1 << 21
+    e2e_ms = 0.0
+    for it in range(1 + args.e2e_steps):
+        for dst, src in zip(host + hflags, pristine):
+            dst.copy_(src)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        _lib.check(L.bt_optic_trace_host(prog._optic.ptr, ctypes.byref(hrv), niter, chunk, sp))
+        dt = (time.perf_counter() - t1) * 1e3
+        if it > 0:
+            e2e_ms += dt
+    e2e_ms /= max(args.e2e_steps, 1)
+    e2e_value = total_rays * nsurf / (e2e_ms * 1e-3)
+    h2d = n * (9 * 8 + 2)
+    d2h = n * (8 * 8 + 2)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.workload)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded rays and optic)",
+            "config": {"workload": f"{args.workload}: {nsurf}-surface trace of {n} rays per GPU, "
+                                   "6 wavelengths 350-1000 nm, Sellmeier silica",
+                       "rays_per_gpu": n, "surfaces": nsurf, "niter": niter,
+                       "l2": "inputs larger than L2 (1.2 GB per step), no flush",
+                       "vignetted_fraction": vig},
+            "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": fpeak.value, "unit": "TFLOP/s",
+                         "frac": achieved_tflops / fpeak.value if fpeak.value else None,
+                         "traffic": (traffic_per_ray * n if traffic_per_ray else None),
+                         "peak_source": "DFMA loop measured in this run (bt_measure_fp64_peak)",
+                         "flops_per_ray": flops_per_ray,
+                         "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s",
+                                 "frac": hbm_gbs / hbm_peak, "bytes_per_ray": bytes_per_ray,
+                                 "peak_source": "MEASURED_PEAKS.json hbm_gbs"}},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": e2e_ms, "path": "bt_optic_trace_host, pinned host arrays, 2-stream chunks"},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

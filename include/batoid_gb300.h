@@ -191,6 +191,11 @@ void bt_optic_destroy(bt_optic* o);
 int bt_optic_nstages(const bt_optic* o, int* out);
 /* In-place trace of all stages in one launch (CompoundOptic.trace). */
 int bt_optic_trace(const bt_optic* o, const bt_rayvector* rv, int niter, void* stream);
+/* Out-of-place trace: reads `in`, writes the traced rays to `out` (same
+ * size; may not partially overlap `in`).  Equivalent to copying then
+ * tracing in place (CompoundOptic.trace on rv.copy()). */
+int bt_optic_trace_into(const bt_optic* o, const bt_rayvector* in, const bt_rayvector* out, int niter,
+                        void* stream);
 /* traceFull: rv is read only; snaps[k] receives the rays after stage k
  * (CompoundOptic.traceFull's per-interface 'out' copies). */
 int bt_optic_trace_full(const bt_optic* o, const bt_rayvector* rv, const bt_rayvector* snaps,
@@ -223,6 +228,11 @@ int bt_huygens_amplitudes(const bt_rayvector* rv, double px, double py, double p
 int bt_zernike_normal_equations(const double* x, const double* y, const double* v, const long long* offsets,
                                 int nfits, const double* basis, int jmax, int side, double* G, double* b,
                                 void* stream);
+
+/* Measures the device's FP64 FMA throughput (TFLOP/s, 2 flops per FMA)
+ * with independent DFMA chains; `iters` FMAs per chain (e.g. 1 << 14).
+ * The denominator of the tracer's FP64 roofline.  Synchronous. */
+int bt_measure_fp64_peak(int iters, double* tflops, void* stream);
 
 /* Reads and clears the device status word of the blob-staging kernels:
  * BT_ERR_TIMEOUT if a kernel's bounded wait for its descriptor copy expired

@@ -392,6 +392,7 @@ double ora_getN(const ora_medium* m, double w) {
         /* :89-105 */
         if (w < m->args[0]) return NAN;
         if (w > m->args[m->n - 1]) return NAN;
+        if (m->n < 2) return m->vals[0];
         int u;
         for (u = 1; u < m->n; u++)
             if (w < m->args[u]) break;
