@@ -22,8 +22,8 @@ def _lib_built():
 def _build_native():
     """Build the CUDA library and the oracle if they are missing."""
     if not _lib_built():
-        from batoid_gb300 import build
-        build.build()
+        import __graft_entry__
+        __graft_entry__.build()
     if not os.path.exists(os.path.join(ROOT, "oracle", "liboracle.so")):
         import oracle as ora
         ora.build()
