@@ -65,6 +65,11 @@ cudaError_t bt_launch_huygens(const RV& rv, double px, double py, double pz, con
                               int nb, double t0, bool ignore_vig, double* out_re, double* out_im,
                               cudaStream_t stream);
 
+// huygens.cu, allocation-free variant (file-scope device scratch)
+cudaError_t bt_launch_huygens_noalloc(const RV& rv, double px, double py, double pz, const double lat[4], int na,
+                                      int nb, double t0, bool ignore_vig, double* out_re, double* out_im,
+                                      cudaStream_t stream, size_t* needed);
+
 // fit.cu
 cudaError_t bt_launch_zk_normal(const double* x, const double* y, const double* v, const long long* offsets,
                                 int nfits, const double* basis, int jmax, int side, double* G, double* b,

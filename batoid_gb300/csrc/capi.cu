@@ -1079,6 +1079,26 @@ extern "C" int bt_huygens_amplitudes(const bt_rayvector* rv, double px, double p
     return BT_OK;
 }
 
+// Same result as bt_huygens_amplitudes, but allocates no device memory: the
+// scratch is a fixed 8 MiB array inside the library (see huygens.cu).
+extern "C" int bt_huygens_amplitudes_noalloc(const bt_rayvector* rv, double px, double py, double pz,
+                                             const double lat[4], int na, int nb, double t0, int ignore_vignetted,
+                                             double* out_re, double* out_im, void* stream) {
+    int rc = check_rv(rv);
+    if (rc != BT_OK) return rc;
+    if (!lat || na < 0 || nb < 0) return fail(BT_ERR_ARG, "huygens (no-alloc): bad lattice");
+    if ((long long)na * nb == 0) return BT_OK;
+    if (!out_re || !out_im) return fail(BT_ERR_ARG, "huygens (no-alloc): null output");
+    size_t needed = 0;
+    cudaError_t e = bt_launch_huygens_noalloc(to_rv(rv), px, py, pz, lat, na, nb, t0, ignore_vignetted != 0, out_re,
+                                              out_im, (cudaStream_t)stream, &needed);
+    if (e == cudaErrorInvalidValue && needed > (8u << 20))
+        return fail(BT_ERR_ARG, "huygens (no-alloc): problem needs " + std::to_string(needed) +
+                                    " bytes of scratch (32 per ray + 16 per pixel), limit is 8388608");
+    if (e != cudaSuccess) return cuda_fail(e, "huygens (no-alloc)");
+    return BT_OK;
+}
+
 extern "C" int bt_zernike_normal_equations(const double* x, const double* y, const double* v,
                                            const long long* offsets, int nfits, const double* basis, int jmax,
                                            int side, double* G, double* b, void* stream) {

@@ -221,3 +221,108 @@ cudaError_t bt_launch_huygens(const RV& rv, double px, double py, double pz, con
     cudaError_t e2 = cudaFreeAsync(scratch, stream);
     return e != cudaSuccess ? e : e2;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the Huygens amplitudes.
+//
+// Some callers cannot let this library allocate device memory: a host
+// framework that owns every byte of device memory under a fixed budget, code
+// that must not trigger the implicit synchronisation or allocator traffic of
+// cudaMalloc inside a latency-critical loop, or an embedding that only hands
+// over pre-allocated input and output buffers.  For them the scratch this
+// kernel needs (32 bytes per ray for the phase records plus 16 bytes per
+// pixel per ray split for partial sums) lives in a fixed file-scope device
+// array of HUY_NOALLOC_BYTES, which every GPU that loads the library holds
+// until the process exits.
+//
+// Set-up: the first call on a device (with that device current) looks up the
+// array's device address with cudaGetSymbolAddress and caches it per device;
+// make that first call before any stream capture.  All calls share the one
+// array and it keeps the last call's contents: nothing in it has to start at
+// zero (every record and partial sum is written before it is read within a
+// call), but calls whose kernels overlap on the GPU -- on different streams
+// without ordering, or from several host threads -- race on it.
+// ---------------------------------------------------------------------------
+
+#include <mutex>
+
+#define HUY_NOALLOC_BYTES (8u << 20)
+#define HUY_MAX_DEVICES 64
+
+static __device__ __align__(256) unsigned char g_huy_noalloc_scratch[HUY_NOALLOC_BYTES];
+
+static std::mutex g_huy_noalloc_mu;
+static void* g_huy_noalloc_ptr[HUY_MAX_DEVICES];
+
+static cudaError_t huy_noalloc_scratch(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= HUY_MAX_DEVICES) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_huy_noalloc_mu);
+    if (!g_huy_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_huy_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_huy_noalloc_ptr[dev] = p;
+    }
+    *out = g_huy_noalloc_ptr[dev];
+    return cudaSuccess;
+}
+
+// Returns cudaErrorInvalidValue when the problem does not fit the scratch
+// array (the C-ABI wrapper turns that into a size message).
+cudaError_t bt_launch_huygens_noalloc(const RV& rv, double px, double py, double pz, const double lat[4], int na,
+                                      int nb, double t0, bool ignore_vig, double* out_re, double* out_im,
+                                      cudaStream_t stream, size_t* needed) {
+    const long long npix = (long long)na * nb;
+    *needed = 0;
+    if (npix <= 0) return cudaSuccess;
+    if (rv.n <= 0) {
+        cudaError_t e = cudaMemsetAsync(out_re, 0, npix * sizeof(double), stream);
+        if (e != cudaSuccess) return e;
+        return cudaMemsetAsync(out_im, 0, npix * sizeof(double), stream);
+    }
+    const size_t rec_bytes = ((size_t)rv.n * sizeof(HuyRec) + 255) & ~(size_t)255;
+    const size_t split_bytes = 2 * (size_t)npix * sizeof(double);
+    *needed = rec_bytes + split_bytes;
+    if (rec_bytes + split_bytes > HUY_NOALLOC_BYTES) return cudaErrorInvalidValue;
+    const long long max_split_mem = (long long)((HUY_NOALLOC_BYTES - rec_bytes) / split_bytes);
+
+    const int ngroups_b = (nb + HUY_PX - 1) / HUY_PX;
+    const long long ngroups = (long long)na * ngroups_b;
+    const long long tiles = (ngroups + HUY_THREADS - 1) / HUY_THREADS;
+    const int sms = bt_sm_count();
+    long long nsplit = (4LL * sms + tiles - 1) / tiles;
+    long long max_split = (rv.n + HUY_TILE - 1) / HUY_TILE;
+    if (nsplit > max_split) nsplit = max_split;
+    if (nsplit > max_split_mem) nsplit = max_split_mem;
+    if (nsplit > 65535) nsplit = 65535;
+    if (nsplit < 1) nsplit = 1;
+    long long per = (rv.n + nsplit - 1) / nsplit;
+    per = ((per + HUY_TILE - 1) / HUY_TILE) * HUY_TILE;
+    nsplit = (rv.n + per - 1) / per;
+
+    void* base = nullptr;
+    cudaError_t e = huy_noalloc_scratch(&base);
+    if (e != cudaSuccess) return e;
+    char* scratch = static_cast<char*>(base);
+    HuyRec* rec = reinterpret_cast<HuyRec*>(scratch);
+    double* pre = reinterpret_cast<double*>(scratch + rec_bytes);
+    double* pim = pre + (size_t)nsplit * npix;
+
+    long long pg = (rv.n + 255) / 256;
+    if (pg > (long long)sms * 16) pg = (long long)sms * 16;
+    k_huy_prep<<<(int)pg, 256, 0, stream>>>(rv, px, py, pz, lat[0], lat[1], lat[2], lat[3], t0,
+                                            ignore_vig ? 1 : 0, rec);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)tiles, (unsigned)nsplit);
+    k_huy_main<<<grid, HUY_THREADS, 0, stream>>>(rec, rv.n, na, nb, ngroups_b, per, pre, pim);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    long long rg = (npix + 255) / 256;
+    if (rg > (long long)sms * 8) rg = (long long)sms * 8;
+    k_huy_reduce<<<(int)rg, 256, 0, stream>>>(pre, pim, (int)nsplit, npix, out_re, out_im);
+    return cudaGetLastError();
+}

@@ -218,6 +218,20 @@ int bt_huygens_amplitudes(const bt_rayvector* rv, double px, double py, double p
                           const double lat[4], int na, int nb, double t0, int ignore_vignetted,
                           double* out_re, double* out_im, void* stream);
 
+/* Allocation-free bt_huygens_amplitudes (no counterpart in the reference).
+ * For callers that may not allocate device memory -- e.g. a host framework
+ * that owns all device memory under a fixed budget, or a latency-critical
+ * loop that must not trigger cudaMalloc/cudaFree: the scratch lives in a
+ * fixed 8 MiB device array inside the library, held by every GPU that loads
+ * the library until exit.  Limit: 32 bytes per ray + 16 bytes per pixel must
+ * fit in 8 MiB (e.g. 245,760 rays with a 128x128 lattice); larger problems
+ * return BT_ERR_ARG with the size needed.  The first call on a device sets
+ * up the scratch address (make it before any stream capture).  All calls
+ * share the array: calls that overlap on the GPU race. */
+int bt_huygens_amplitudes_noalloc(const bt_rayvector* rv, double px, double py, double pz,
+                                  const double lat[4], int na, int nb, double t0, int ignore_vignetted,
+                                  double* out_re, double* out_im, void* stream);
+
 /* ---- Zernike wavefront fit (batoid/analysis.py:563-573) ------------------
  * Normal equations of nfits independent least-squares fits, one CUDA block
  * per fit.  Fit f uses points [offsets[f], offsets[f+1]) of x, y (pupil
