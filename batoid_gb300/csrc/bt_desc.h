@@ -34,9 +34,12 @@ enum bt_surf_kind {
 //  PARABOLOID: p0=R p1=1/R p2=1/2/R
 //  QUADRIC/ASPHERE: p0=R p1=conic p2=R*R p3=1/R/R p4=conic+1 p5=1/(conic+1)
 //              p6=R/(conic+1) p7=R*R/(conic+1)/(conic+1) p8=(conic+1)/R/R
-//              ASPHERE: n coefs at pool[off], n dz/dr coefs at pool[off+n]
+//              p9=1/R (0 if R == 0) p10=1 if the sag may use (1-q)*R/(conic+1)
+//              ASPHERE: n coefs at pool[off], n dz/dr coefs at pool[off+n],
+//              then both again as float-float pairs (one double slot each)
 //  POLY:       p0=xorigin p1=yorigin; n=xsize m=ysize;
-//              coefs pool[off .. off+n*m), gradx then grady ((n-1)*(m-1) each)
+//              coefs pool[off .. off+n*m), gradx then grady ((n-1)*(m-1) each),
+//              then the three arrays again as float-float pairs
 //  BICUBIC:    p0=x0 p1=y0 p2=dx p3=dy p4=use_nan; n=nx m=ny; tab = 4 arrays
 //              (z, dzdx, dzdy, d2zdxdy), each nx*ny, row-major [iy][ix]
 //  SUM:        n=#children m=index of first child (children are contiguous)
@@ -45,10 +48,10 @@ typedef struct bt_surf {
     int32_t n;
     int32_t m;
     int32_t off;
-    double p[10];
+    double p[12];
     const double* tab;
     double pad_;
-} bt_surf;  // 112 bytes
+} bt_surf;  // 128 bytes
 
 enum bt_medium_kind {
     BT_M_CONST = 0,
@@ -101,7 +104,7 @@ typedef struct bt_stage {
     int32_t medium;      // refract: outgoing medium index; else -1
     int32_t obsc_begin;  // postfix program [obsc_begin, obsc_end), empty = none
     int32_t obsc_end;
-    int32_t identity;    // dr == 0 and drot == I
+    int32_t identity;    // 1: dr == 0 and drot == I; 2: drot == I (translation); 0: general
     int32_t coated;      // 1: multiply flux by coat_r (reflect) / coat_t
     int32_t pad_;
     double dr[3];
@@ -126,7 +129,7 @@ typedef struct bt_prog_header {
 } bt_prog_header;  // 64 bytes
 
 #ifdef __cplusplus
-static_assert(sizeof(bt_surf) == 112, "bt_surf layout");
+static_assert(sizeof(bt_surf) == 128, "bt_surf layout");
 static_assert(sizeof(bt_medium) == 64, "bt_medium layout");
 static_assert(sizeof(bt_obsc) == 64, "bt_obsc layout");
 static_assert(sizeof(bt_stage) == 144, "bt_stage layout");

@@ -545,3 +545,323 @@ __device__ __forceinline__ bool bt_obsc_run(const Prog& P, int begin, int end, d
     }
     return sp > 0 ? (bool)((stack >> (sp - 1)) & 1u) : false;
 }
+
+// ===========================================================================
+// Trace-kernel evaluation (mixed precision).
+//
+// Newton needs the residual F = sag(x + vx dt, y + vy dt) - (z + vz dt) to
+// FP64 accuracy, but its derivative only approximately: with a derivative of
+// relative error d, each step shrinks the error by ~d, so an FP32 slope
+// (d ~ 1e-7) converges in the same 2-3 steps as the exact one.  So:
+//  * sags: conic part in FP64 (one rsqrt, no division where that is exact
+//    enough), polynomial perturbations (asphere terms, Zernike / Cartesian
+//    polynomials) in float-float on the FP32 pipe;
+//  * Newton slopes: FP32;
+//  * the normal used for reflection / refraction: FP64 conic slope plus
+//    float-float polynomial slope.
+// Pool layout (host packer): ASPHERE [c n][dc n][c ff n][dc ff n];
+// POLY [coefs][gx][gy] in FP64 then the same three arrays as float-float.
+// p[9] = 1/R (0 when R == 0); p[10] = 1 when the conic sag may use
+// (1 - q) * R/(1+k), i.e. |R/(1+k)| <= 100 (absolute error <= 100 ulp(1)).
+// ===========================================================================
+#include "bt_ff.cuh"
+
+// sqrt(w) from w * rsqrt(w), exact for w == 0 and NaN for w < 0.
+__device__ __forceinline__ void bt_sqrt_rsqrt(double w, double* q, double* rs) {
+    if (w > 0.0) {
+        const double r = rsqrt(w);
+        *rs = r;
+        *q = w * r;
+    } else {
+        *q = sqrt(w);
+        *rs = 1.0 / *q;
+    }
+}
+
+// Conic of a QUADRIC / ASPHERE record: sag and (dz/dr)/r, FP64.
+__device__ __forceinline__ void bt_conic(const bt_surf& s, double r2, double* sag, double* k) {
+    if (s.p[0] == 0.0) {
+        *sag = 0.0;
+        *k = 0.0;
+        return;
+    }
+    const double w = 1. - r2 * s.p[8];
+    double q, rs;
+    bt_sqrt_rsqrt(w, &q, &rs);
+    *sag = (s.p[10] != 0.0) ? (1. - q) * s.p[6] : r2 / (s.p[0] * (1. + q));
+    *k = rs * s.p[9];
+}
+
+__device__ __forceinline__ void bt_sphere_conic(const bt_surf& s, double r2, double* sag, double* k) {
+    if (s.p[0] == 0.0) {
+        *sag = 0.0;
+        *k = 0.0;
+        return;
+    }
+    const double w = 1. - r2 * s.p[3];
+    double q, rs;
+    bt_sqrt_rsqrt(w, &q, &rs);
+    *sag = s.p[0] * (1. - q);
+    *k = rs * s.p[2];
+}
+
+// FP64-accurate sag with an FP32 slope (Newton iterations).
+__device__ __forceinline__ void bt_leaf_newton_eval(const bt_surf& s, const double* pool, double x, double y,
+                                                    double* sag, float* ux, float* uy) {
+    switch (s.kind) {
+    case BT_S_PLANE:
+        *sag = 0.0; *ux = 0.f; *uy = 0.f;
+        return;
+    case BT_S_TILTED:
+        *sag = x * s.p[0] + y * s.p[1];
+        *ux = (float)(-s.p[0] / s.p[2]);
+        *uy = (float)(-s.p[1] / s.p[2]);
+        return;
+    case BT_S_SPHERE: {
+        double k;
+        bt_sphere_conic(s, x * x + y * y, sag, &k);
+        *ux = (float)(-x * k);
+        *uy = (float)(-y * k);
+        return;
+    }
+    case BT_S_PARABOLOID:
+        if (s.p[0] == 0.0) { *sag = 0.0; *ux = 0.f; *uy = 0.f; return; }
+        *sag = (x * x + y * y) * s.p[2];
+        *ux = (float)(-x * s.p[1]);
+        *uy = (float)(-y * s.p[1]);
+        return;
+    case BT_S_QUADRIC:
+    case BT_S_ASPHERE: {
+        const double r2 = x * x + y * y;
+        double z, k;
+        bt_conic(s, r2, &z, &k);
+        float kf = (float)k;
+        if (s.kind == BT_S_ASPHERE && s.n > 0) {
+            const ff r2f = ff_from(r2);
+            const ff* c = ff_ptr(pool, s.off + 2 * s.n);
+            const ff* dc = c + s.n;
+            const ff a = ff_mul(ff_horner(r2f, c, s.n), r2f);
+            z += ff_to_double(a);
+            float da = 0.f;
+            for (int i = s.n - 1; i >= 0; i--) da = fmaf(da, r2f.hi, dc[i].hi);
+            kf += da;
+        }
+        *sag = z;
+        *ux = (float)(-x) * kf;
+        *uy = (float)(-y) * kf;
+        return;
+    }
+    case BT_S_POLY: {
+        const double xx = x - s.p[0], yy = y - s.p[1];
+        const int nx = s.n, ny = s.m;
+        const int g = (nx - 1) * (ny - 1);
+        const ff* c = ff_ptr(pool, s.off + nx * ny + 2 * g);
+        *sag = ff_to_double(ff_horner2d(ff_from(xx), ff_from(yy), c, nx, ny));
+        const float fx = (float)xx, fy = (float)yy;
+        *ux = -f_horner2d(fx, fy, c + nx * ny, nx - 1, ny - 1);
+        *uy = -f_horner2d(fx, fy, c + nx * ny + g, nx - 1, ny - 1);
+        return;
+    }
+    default: {
+        double z, gx, gy;
+        bt_leaf_eval(s, pool, x, y, true, true, &z, &gx, &gy);
+        *sag = z;
+        *ux = (float)gx;
+        *uy = (float)gy;
+        return;
+    }
+    }
+}
+
+__device__ __forceinline__ void bt_surf_newton_eval(const Prog& P, int si, double x, double y, double* sag,
+                                                    float* ux, float* uy) {
+    const bt_surf& s = P.surfs[si];
+    if (s.kind != BT_S_SUM) {
+        bt_leaf_newton_eval(s, P.pool, x, y, sag, ux, uy);
+        return;
+    }
+    double z = 0.0;
+    float gx = 0.f, gy = 0.f;
+    for (int c = 0; c < s.n; c++) {
+        double cz;
+        float cx, cy;
+        bt_leaf_newton_eval(P.surfs[s.m + c], P.pool, x, y, &cz, &cx, &cy);
+        z += cz;
+        gx += cx;
+        gy += cy;
+    }
+    *sag = z;
+    *ux = gx;
+    *uy = gy;
+}
+
+// Slope (nx/nz, ny/nz) at full accuracy for the interaction normal.
+__device__ __forceinline__ void bt_leaf_slope_precise(const bt_surf& s, const double* pool, double x, double y,
+                                                      double* ux, double* uy) {
+    switch (s.kind) {
+    case BT_S_SPHERE: {
+        double z, k;
+        bt_sphere_conic(s, x * x + y * y, &z, &k);
+        *ux = -x * k;
+        *uy = -y * k;
+        return;
+    }
+    case BT_S_QUADRIC:
+    case BT_S_ASPHERE: {
+        const double r2 = x * x + y * y;
+        double z, k;
+        bt_conic(s, r2, &z, &k);
+        if (s.kind == BT_S_ASPHERE && s.n > 0) {
+            const ff* dc = ff_ptr(pool, s.off + 3 * s.n);
+            k += ff_to_double(ff_horner(ff_from(r2), dc, s.n));
+        }
+        *ux = -x * k;
+        *uy = -y * k;
+        return;
+    }
+    case BT_S_POLY: {
+        const int nx = s.n, ny = s.m;
+        const int g = (nx - 1) * (ny - 1);
+        const ff* c = ff_ptr(pool, s.off + nx * ny + 2 * g);
+        const ff xf = ff_from(x - s.p[0]), yf = ff_from(y - s.p[1]);
+        *ux = -ff_to_double(ff_horner2d(xf, yf, c + nx * ny, nx - 1, ny - 1));
+        *uy = -ff_to_double(ff_horner2d(xf, yf, c + nx * ny + g, nx - 1, ny - 1));
+        return;
+    }
+    default: {
+        double z;
+        bt_leaf_eval(s, pool, x, y, false, true, &z, ux, uy);
+        return;
+    }
+    }
+}
+
+__device__ __forceinline__ void bt_surf_slope_precise(const Prog& P, int si, double x, double y, double* ux,
+                                                      double* uy) {
+    const bt_surf& s = P.surfs[si];
+    if (s.kind != BT_S_SUM) {
+        bt_leaf_slope_precise(s, P.pool, x, y, ux, uy);
+        return;
+    }
+    double gx = 0.0, gy = 0.0;
+    for (int c = 0; c < s.n; c++) {
+        double cx, cy;
+        bt_leaf_slope_precise(P.surfs[s.m + c], P.pool, x, y, &cx, &cy);
+        gx += cx;
+        gy += cy;
+    }
+    *ux = gx;
+    *uy = gy;
+}
+
+// Unit normal at the intersection (reference conventions, incl. Tilted).
+__device__ __forceinline__ void bt_normal_precise(const Prog& P, int si, double x, double y, double* nx,
+                                                  double* ny, double* nz) {
+    const bt_surf& s = P.surfs[si];
+    if (s.kind == BT_S_TILTED) { *nx = -s.p[0]; *ny = -s.p[1]; *nz = s.p[2]; return; }
+    if (s.kind == BT_S_PLANE) { *nx = 0.0; *ny = 0.0; *nz = 1.0; return; }
+    double ux, uy;
+    bt_surf_slope_precise(P, si, x, y, &ux, &uy);
+    const double k = rsqrt(ux * ux + uy * uy + 1.0);
+    *nx = ux * k;
+    *ny = uy * k;
+    *nz = k;
+}
+
+// Newton in correction form: dt += F / F'(approx).  Stops at an exact fixed
+// point, or once a correction below 1e-11 has been applied and the surface
+// re-evaluated there (the next correction would be < 1e-11 times the FP32
+// derivative's relative error), or after niter steps as the reference.
+__device__ __forceinline__ bool bt_newton_mixed(const Prog& P, int si, double x, double y, double z, double vx,
+                                                double vy, double vz, double& dt, int niter) {
+    double rPx = x + vx * dt;
+    double rPy = y + vy * dt;
+    double rPz = z + vz * dt;
+    double sz;
+    float gx, gy;
+    bt_surf_newton_eval(P, si, rPx, rPy, &sz, &gx, &gy);
+    const float fvx = (float)vx, fvy = (float)vy, fvz = (float)vz;
+    for (int it = 0; it < niter; it++) {
+        const float den = fmaf(gx, fvx, fmaf(gy, fvy, fvz));
+        const double ddt = (sz - rPz) * (double)(1.0f / den);
+        const double dtn = dt + ddt;
+        if (dtn == dt) break;
+        dt = dtn;
+        rPx = x + vx * dt;
+        rPy = y + vy * dt;
+        rPz = z + vz * dt;
+        bt_surf_newton_eval(P, si, rPx, rPy, &sz, &gx, &gy);
+        if (fabs(ddt) < 1e-11) break;
+    }
+    return fabs(sz - rPz) < 1e-12;
+}
+
+// One root of a*t^2 + b*t + c = 0 with one division: `plus` selects
+// (-b + sqrt(D)) / 2a, else (-b - sqrt(D)) / 2a; each in its cancellation-
+// free form (the reference's dt1 / dt2 pair, src/sphere.cpp:51-58).
+__device__ __forceinline__ bool bt_one_root(double a, double b, double c, bool plus, double* t) {
+    const double disc = b * b - 4 * a * c;
+    if (disc < 0) return false;
+    double s, rs;
+    bt_sqrt_rsqrt(disc, &s, &rs);
+    if (b > 0) *t = plus ? 2 * c / (-b - s) : (-b - s) / (2 * a);
+    else *t = plus ? (-b + s) / (2 * a) : 2 * c / (-b + s);
+    return true;
+}
+
+// Time to intersect for the trace kernel.
+__device__ __forceinline__ bool bt_leaf_tti_fast(const Prog& P, int si, double x, double y, double z, double vx,
+                                                 double vy, double vz, double& dt, int niter) {
+    const bt_surf& s = P.surfs[si];
+    switch (s.kind) {
+    case BT_S_SPHERE: {
+        const double R = s.p[0];
+        const double z0 = z - R;
+        const double a = vz * vz + (vx * vx + vy * vy);
+        const double b = 2 * vz * z0 + 2 * (vx * x + vy * y);
+        const double c = z0 * z0 - s.p[1] + (x * x + y * y);
+        // the reference takes max(dt1, dt2) when vz*R < 0, else min; the
+        // larger root is the "+sqrt" one when a > 0
+        const bool want_max = (vz * R < 0);
+        return bt_one_root(a, b, c, want_max == (a > 0), &dt);
+    }
+    case BT_S_PARABOLOID: {
+        const double a = (vx * vx + vy * vy) * s.p[2];
+        const double b = (x * vx + y * vy) * s.p[1] - vz;
+        const double c = (x * x + y * y) * s.p[2] - z;
+        if (a == 0) { dt = -c / b; return true; }
+        const bool want_max = (vz * s.p[0] < 0);
+        return bt_one_root(a, b, c, want_max == (a > 0), &dt);
+    }
+    case BT_S_QUADRIC:
+    case BT_S_ASPHERE: {
+        // conic start (src/quadric.cpp:41-71): root with the smaller |z|
+        const double z0 = z - s.p[6];
+        const double vrr0 = vx * x + vy * y;
+        const double a = vz * vz + (vx * vx + vy * vy) * s.p[5];
+        const double b = 2 * (vz * z0 + vrr0 * s.p[5]);
+        const double c = z0 * z0 - s.p[7] + (x * x + y * y) * s.p[5];
+        double t1, t2;
+        if (!bt_quad_roots(a, b, c, &t1, &t2)) return false;
+        dt = (fabs(z + vz * t1) < fabs(z + vz * t2)) ? t1 : t2;
+        if (s.kind == BT_S_QUADRIC) return true;
+        return bt_newton_mixed(P, si, x, y, z, vx, vy, vz, dt, niter);
+    }
+    case BT_S_POLY:
+    case BT_S_BICUBIC:
+        return bt_newton_mixed(P, si, x, y, z, vx, vy, vz, dt, niter);
+    default: {
+        double ux, uy;
+        bool slope_ok;
+        return bt_leaf_tti(P, si, x, y, z, vx, vy, vz, dt, niter, &ux, &uy, &slope_ok);
+    }
+    }
+}
+
+__device__ __forceinline__ bool bt_surf_tti_fast(const Prog& P, int si, double x, double y, double z, double vx,
+                                                 double vy, double vz, double& dt, int niter) {
+    const bt_surf& s = P.surfs[si];
+    if (s.kind != BT_S_SUM) return bt_leaf_tti_fast(P, si, x, y, z, vx, vy, vz, dt, niter);
+    if (!bt_leaf_tti_fast(P, s.m, x, y, z, vx, vy, vz, dt, niter)) return false;
+    return bt_newton_mixed(P, si, x, y, z, vx, vy, vz, dt, niter);
+}

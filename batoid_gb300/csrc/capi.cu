@@ -153,6 +153,20 @@ extern "C" int bt_paraboloid_create(double R, bt_surface** out) {
     return make_out(out, s);
 }
 
+// A double's float-float split (hi, lo) stored in one double slot.
+static double ff_slot(double v) {
+    float pair[2];
+    pair[0] = (float)v;
+    pair[1] = (float)(v - (double)pair[0]);
+    double out;
+    memcpy(&out, pair, sizeof(out));
+    return out;
+}
+
+static void append_ff(std::vector<double>& pool, size_t begin, size_t n) {
+    for (size_t i = 0; i < n; i++) pool.push_back(ff_slot(pool[begin + i]));
+}
+
 static void fill_quadric(bt_surf& r, double R, double conic) {
     // src/quadric.cpp:9-14
     const double cp1 = conic + 1;
@@ -165,6 +179,11 @@ static void fill_quadric(bt_surf& r, double R, double conic) {
     r.p[6] = R / cp1;
     r.p[7] = R * R / cp1 / cp1;
     r.p[8] = cp1 / R / R;
+    r.p[9] = (R != 0.0) ? 1. / R : 0.0;
+    // (1 - q) * R/(1+k) replaces r^2 / (R (1 + q)) when R/(1+k) is moderate:
+    // its absolute rounding error is ~|R/(1+k)| ulp(1)
+    const double rc = R / cp1;
+    r.p[10] = (R != 0.0 && cp1 != 0.0 && isfinite(rc) && fabs(rc) <= 100.0) ? 1.0 : 0.0;
 }
 
 extern "C" int bt_quadric_create(double R, double conic, bt_surface** out) {
@@ -186,6 +205,7 @@ extern "C" int bt_asphere_create(double R, double conic, const double* coefs, si
     // dz/dr coefficients: entry j multiplies r^(2j+1) with factor 2(j+1)
     // (src/asphere.cpp:10-16)
     for (size_t j = 0; j < n; j++) s->pool.push_back(coefs[j] * (double)(2 * (j + 1)));
+    append_ff(s->pool, 0, 2 * n);
     push_rec(s, r);
     return make_out(out, s);
 }
@@ -208,6 +228,7 @@ extern "C" int bt_polynomial_create(const double* coefs, const double* gradx, co
         s->pool.insert(s->pool.end(), gradx, gradx + gsz);
         s->pool.insert(s->pool.end(), grady, grady + gsz);
     }
+    append_ff(s->pool, 0, xsize * ysize + 2 * gsz);
     push_rec(s, r);
     return make_out(out, s);
 }
@@ -281,6 +302,7 @@ static bt_medium_h* new_medium(int kind) {
 extern "C" int bt_const_medium_create(double n, bt_medium_h** out) {
     bt_medium_h* m = new_medium(BT_M_CONST);
     m->rec.p[0] = n;
+    m->rec.p[1] = 1.0 / n;  // reciprocal used by the refraction kernels
     return make_out(out, m);
 }
 
@@ -544,17 +566,17 @@ static bt_stage blank_stage(int kind) {
 
 static void set_transform(bt_stage& st, const double* dr, const double* drot) {
     if (!dr || !drot) return;
-    bool ident = true;
+    bool zero_shift = true, unit_rot = true;
     for (int i = 0; i < 3; i++) {
         st.dr[i] = dr[i];
-        if (dr[i] != 0.0) ident = false;
+        if (dr[i] != 0.0) zero_shift = false;
     }
     for (int i = 0; i < 9; i++) {
         st.drot[i] = drot[i];
         const double want = (i % 4 == 0) ? 1.0 : 0.0;
-        if (drot[i] != want) ident = false;
+        if (drot[i] != want) unit_rot = false;
     }
-    st.identity = ident ? 1 : 0;
+    st.identity = unit_rot ? (zero_shift ? 1 : 2) : 0;
 }
 
 // A temporary device copy of a blob, freed stream-ordered.

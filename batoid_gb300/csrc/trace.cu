@@ -48,12 +48,18 @@ __device__ __forceinline__ void store_ray(const RV& o, long long i, const RaySta
 // failed rays are skipped and keep their coordinates in the previous frame;
 // a ray that misses the surface is flagged failed+vignetted and likewise
 // keeps its previous coordinates; TIR writes the position, NaN velocity.
+// A medium's index and its reciprocal depend only on the ray's wavelength,
+// so they are computed once per ray per medium.
 __device__ __forceinline__ void run_stage(const Prog& P, const bt_stage& st, RayState& r, int niter,
-                                          int& cached_medium, double& cached_n) {
+                                          int& cached_medium, double& cached_n, double& cached_inv_n) {
     if (st.kind != BT_ST_OBSCURE && !r.fail) {
         double x, y, z, vx, vy, vz;
-        if (st.identity) {
+        if (st.identity == 1) {
             x = r.x; y = r.y; z = r.z; vx = r.vx; vy = r.vy; vz = r.vz;
+        } else if (st.identity == 2) {
+            // rotation is the identity: dx*1 + dy*0 + dz*0 == dx exactly
+            x = r.x - st.dr[0]; y = r.y - st.dr[1]; z = r.z - st.dr[2];
+            vx = r.vx; vy = r.vy; vz = r.vz;
         } else {
             const double dx = r.x - st.dr[0], dy = r.y - st.dr[1], dz = r.z - st.dr[2];
             x = dx * st.drot[0] + dy * st.drot[3] + dz * st.drot[6];
@@ -63,9 +69,8 @@ __device__ __forceinline__ void run_stage(const Prog& P, const bt_stage& st, Ray
             vy = r.vx * st.drot[1] + r.vy * st.drot[4] + r.vz * st.drot[7];
             vz = r.vx * st.drot[2] + r.vy * st.drot[5] + r.vz * st.drot[8];
         }
-        double dt = 0.0, ux = 0.0, uy = 0.0;
-        bool slope_ok = false;
-        const bool ok = bt_surf_tti(P, st.surf, x, y, z, vx, vy, vz, dt, niter, &ux, &uy, &slope_ok);
+        double dt = 0.0;
+        const bool ok = bt_surf_tti_fast(P, st.surf, x, y, z, vx, vy, vz, dt, niter);
         if (ok) {
             x += vx * dt;
             y += vy * dt;
@@ -75,9 +80,7 @@ __device__ __forceinline__ void run_stage(const Prog& P, const bt_stage& st, Ray
                 if (st.coated) r.f *= st.coat_t;
             } else {
                 double nx, ny, nz;
-                const int kind = P.surfs[st.surf].kind;
-                if (slope_ok && kind != BT_S_TILTED) bt_normal_from_slope(ux, uy, &nx, &ny, &nz);
-                else bt_surf_normal(P, st.surf, x, y, &nx, &ny, &nz);
+                bt_normal_precise(P, st.surf, x, y, &nx, &ny, &nz);
                 if (st.kind == BT_ST_REFLECT) {
                     // src/batoid.cpp:343-353
                     const double alpha = vx * nx + vy * ny + vz * nz;
@@ -87,25 +90,31 @@ __device__ __forceinline__ void run_stage(const Prog& P, const bt_stage& st, Ray
                     if (st.coated) r.f *= st.coat_r;
                 } else {
                     // src/batoid.cpp:453-499
-                    const double n1 = 1 / sqrt(vx * vx + vy * vy + vz * vz);
+                    const double n1 = rsqrt(vx * vx + vy * vy + vz * vz);
                     const double nvx = vx * n1, nvy = vy * n1, nvz = vz * n1;
                     double alpha = nvx * nx + nvy * ny + nvz * nz;
                     if (alpha > 0.) {
                         nx = -nx; ny = -ny; nz = -nz;
                         alpha = -alpha;
                     }
-                    double n2;
+                    double n2, inv_n2;
                     const int mi = st.medium;
                     if (P.media[mi].kind == BT_M_CONST) {
                         n2 = P.media[mi].p[0];
+                        inv_n2 = P.media[mi].p[1];
                     } else if (mi == cached_medium) {
                         n2 = cached_n;   // same medium, same wavelength: same value
+                        inv_n2 = cached_inv_n;
                     } else {
                         n2 = bt_getN(P, mi, r.w);
-                        cached_medium = mi;
-                        cached_n = n2;
+                        inv_n2 = 1.0 / n2;
+                        if (P.media[mi].kind != BT_M_CONST) {
+                            cached_medium = mi;
+                            cached_n = n2;
+                            cached_inv_n = inv_n2;
+                        }
                     }
-                    const double eta = n1 / n2;
+                    const double eta = n1 * inv_n2;
                     const double sinsqr = eta * eta * (1 - alpha * alpha);
                     if (sinsqr > 1.0) {
                         vx = NAN; vy = NAN; vz = NAN;
@@ -113,9 +122,9 @@ __device__ __forceinline__ void run_stage(const Prog& P, const bt_stage& st, Ray
                         r.vig = true;
                     } else {
                         const double nfactor = eta * alpha + sqrt(1 - sinsqr);
-                        vx = (eta * nvx - nfactor * nx) / n2;
-                        vy = (eta * nvy - nfactor * ny) / n2;
-                        vz = (eta * nvz - nfactor * nz) / n2;
+                        vx = (eta * nvx - nfactor * nx) * inv_n2;
+                        vy = (eta * nvy - nfactor * ny) * inv_n2;
+                        vz = (eta * nvz - nfactor * nz) * inv_n2;
                     }
                     if (st.coated) r.f *= st.coat_t;
                 }
@@ -156,9 +165,9 @@ k_trace(const unsigned char* __restrict__ gblob, int blob_bytes, RV in, RV out,
         r.vig = in.vig[i] != 0;
         r.fail = in.fail[i] != 0;
         int cached_medium = -1;
-        double cached_n = 0.0;
+        double cached_n = 0.0, cached_inv_n = 0.0;
         for (int s = 0; s < P.nstages; s++) {
-            run_stage(P, P.stages[s], r, niter, cached_medium, cached_n);
+            run_stage(P, P.stages[s], r, niter, cached_medium, cached_n, cached_inv_n);
             if (s < nsnaps) store_ray(snaps.s[s], i, r);
         }
         if (nsnaps == 0) store_ray(out, i, r);
