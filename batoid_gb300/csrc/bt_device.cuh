@@ -491,6 +491,17 @@ __device__ __forceinline__ bool bt_polygon_contains(const double* xp, const doub
     return inside;
 }
 
+// hypot(dx, dy) < r (the reference's test, src/obscuration.cpp:32-34, 80-83),
+// decided from dx^2 + dy^2 vs r^2 unless the two are within a relative
+// 1e-13 of each other, where hypot itself decides.
+__device__ __forceinline__ bool bt_radius_less(double dx, double dy, double r, bool) {
+    const double h2 = dx * dx + dy * dy;
+    const double r2 = r * r;
+    if (h2 < r2 * (1.0 - 1e-13)) return r > 0.0;
+    if (h2 > r2 * (1.0 + 1e-13)) return false;
+    return hypot(dx, dy) < r;
+}
+
 __device__ __forceinline__ bool bt_obsc_run(const Prog& P, int begin, int end, double x, double y) {
     uint32_t stack = 0;  // bit k = entry k
     int sp = 0;
@@ -499,11 +510,11 @@ __device__ __forceinline__ bool bt_obsc_run(const Prog& P, int begin, int end, d
         bool v = false;
         switch (o.op) {
         case BT_O_CIRCLE:
-            v = hypot(x - o.p[1], y - o.p[2]) < o.p[0];
+            v = bt_radius_less(x - o.p[1], y - o.p[2], o.p[0], false);
             break;
         case BT_O_ANNULUS: {
-            double h = hypot(x - o.p[2], y - o.p[3]);
-            v = (o.p[0] <= h) && (h < o.p[1]);
+            const double dx = x - o.p[2], dy = y - o.p[3];
+            v = !bt_radius_less(dx, dy, o.p[0], false) && bt_radius_less(dx, dy, o.p[1], false);
             break;
         }
         case BT_O_RECT: {
@@ -760,6 +771,16 @@ __device__ __forceinline__ void bt_normal_precise(const Prog& P, int si, double 
     const bt_surf& s = P.surfs[si];
     if (s.kind == BT_S_TILTED) { *nx = -s.p[0]; *ny = -s.p[1]; *nz = s.p[2]; return; }
     if (s.kind == BT_S_PLANE) { *nx = 0.0; *ny = 0.0; *nz = 1.0; return; }
+    if (s.kind == BT_S_SPHERE && s.p[0] != 0.0) {
+        // (-x k, -y k, 1) / |.| with k = 1/(R q), q = sqrt(1 - r^2/R^2): the
+        // norm is 1/q, so the unit normal is (-x/R, -y/R, q)
+        double q, rs;
+        bt_sqrt_rsqrt(1. - (x * x + y * y) * s.p[3], &q, &rs);
+        *nx = -x * s.p[2];
+        *ny = -y * s.p[2];
+        *nz = q;
+        return;
+    }
     double ux, uy;
     bt_surf_slope_precise(P, si, x, y, &ux, &uy);
     const double k = rsqrt(ux * ux + uy * uy + 1.0);

@@ -121,7 +121,9 @@ __device__ __forceinline__ void run_stage(const Prog& P, const bt_stage& st, Ray
                         r.fail = true;
                         r.vig = true;
                     } else {
-                        const double nfactor = eta * alpha + sqrt(1 - sinsqr);
+                        double cosr, rs;
+                        bt_sqrt_rsqrt(1 - sinsqr, &cosr, &rs);
+                        const double nfactor = eta * alpha + cosr;
                         vx = (eta * nvx - nfactor * nx) * inv_n2;
                         vy = (eta * nvy - nfactor * ny) * inv_n2;
                         vz = (eta * nvz - nfactor * nz) * inv_n2;
