@@ -42,6 +42,7 @@ def parse():
     p.add_argument("--nrays", type=int, default=16 * 1024 * 1024)
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-huygens", action="store_true")
     return p.parse_args()
 
 
@@ -171,6 +172,81 @@ def load_traffic(workload):
         return None
 
 
+HUYGENS_FIELDS = [(fx, fy) for fy in (-1.2, 0.0, 1.2) for fx in (-1.2, 0.0, 1.2)]  # degrees
+
+
+def bench_huygens(bt, opt, nx=256, npix=128, pitch=2e-6, wavelength=620e-9, check_pixels=48, cpu=True):
+    """Huygens PSF of the 12-surface system: 9 field points (3x3 grid over
+    +-1.2 deg), 256x256 pupil grid, 128x128 pixels at 2 um around the chief
+    ray.  Device-timed: trace + phasor sums for all fields.  Error: PSF on
+    sampled pixels vs the FP64 per-pixel sum (device sumAmplitude kernel,
+    the reference's algorithm), relative to the PSF peak."""
+    import torch
+    from batoid_gb300 import analysis as A
+    lat = np.array([[pitch, 0.0], [0.0, pitch]])
+    rng = np.random.default_rng(5)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    sums = {"ms_trace_and_psf": 0.0, "ms_psf_kernels": 0.0}
+    max_err = 0.0
+    pairs = 0
+    kept = []
+    for fx, fy in HUYGENS_FIELDS:
+        rays = bt.RayVector.asGrid(optic=opt, wavelength=wavelength, theta_x=np.deg2rad(fx),
+                                   theta_y=np.deg2rad(fy), nx=nx)
+        torch.cuda.synchronize()
+        e0.record()
+        opt.trace(rays)
+        e1.record()
+        torch.cuda.synchronize()
+        sums["ms_trace_and_psf"] += e0.elapsed_time(e1)
+        point = rays.r[(nx // 2) * nx + nx // 2]
+        t0 = float(rays.t[0])
+        e0.record()
+        re, im = A.huygens_amplitudes(rays, (point[0], point[1], 0.0), lat, npix, npix, t0)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)   # includes the two device-to-host copies of the result
+        sums["ms_psf_kernels"] += ms
+        sums["ms_trace_and_psf"] += ms
+        valid = int((~rays.failed & ~rays.vignetted).sum())
+        pairs += valid * npix * npix
+        psf = re * re + im * im
+        peak = psf.max()
+        idx = rng.integers(0, npix, (check_pixels, 2))
+        for a, b in idx:
+            P = (point[0] + (b - npix // 2) * pitch, point[1] + (a - npix // 2) * pitch, 0.0)
+            ref = rays.sumAmplitude(P, t0)
+            err = abs(abs(ref) ** 2 - psf[a, b]) / peak
+            max_err = max(max_err, err)
+        kept.append((rays, point, t0))
+    out = {
+        "workload": f"{len(HUYGENS_FIELDS)} fields x {nx}x{nx} pupil rays x {npix}x{npix} px at {pitch*1e6:.0f} um, "
+                    f"{wavelength*1e9:.0f} nm, tma_corrector",
+        "fields_per_s": len(HUYGENS_FIELDS) / (sums["ms_trace_and_psf"] * 1e-3),
+        "ray_pixel_pairs_per_s": pairs / (sums["ms_psf_kernels"] * 1e-3),
+        "ms_total": sums["ms_trace_and_psf"], "ms_psf": sums["ms_psf_kernels"],
+        "psf_max_err_rel_peak": max_err,
+        "err_reference": "FP64 per-pixel phasor sum (bt_rv_sum_amplitude) on sampled pixels",
+    }
+    if cpu:
+        # oracle (C, all threads): per-pixel sumAmplitude on a pixel sample, extrapolated
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as ora
+        rays, point, t0 = kept[4]
+        host = ora.Rays(*[getattr(rays, k) for k in ora.Rays.FIELDS], rays.vignetted, rays.failed)
+        npx = 64
+        t1 = time.perf_counter()
+        for k in range(npx):
+            ora.sum_amplitude(host, (point[0] + k * pitch, point[1], 0.0), t0)
+        per_px = (time.perf_counter() - t1) / npx
+        out["cpu_baseline"] = {"s_per_pixel": per_px, "cores": ora.threads(),
+                               "extrapolated_s_total": per_px * npix * npix * len(HUYGENS_FIELDS),
+                               "sample": f"{npx} pixels of one field, oracle sumAmplitude (reference algorithm)"}
+        out["speedup_vs_cpu"] = out["cpu_baseline"]["extrapolated_s_total"] / (sums["ms_psf_kernels"] * 1e-3)
+    return out
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -267,6 +343,10 @@ def run_gpu(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.workload)
+    huygens = None
+    if rank == 0 and not args.no_huygens:
+        del rv_in, rv_out
+        huygens = bench_huygens(bt, opt, cpu=not args.no_cpu_baseline)
 
     if rank == 0:
         line = {
@@ -291,6 +371,7 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": args.steps,
+            "huygens_psf": huygens,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
