@@ -236,6 +236,61 @@ def sellmeier_csv_fixture(ref_root):
     return {"csv_wmicron": wmicron, "csv_n": ncsv}
 
 
+def _zemax_lsst(path):
+    """Hx, Hy, Px, Py and the per-surface rows of a Zemax 'Real Ray Trace
+    Data' export (UTF-16), as read by the reference's tests/test_zemax.py:424-428."""
+    with open(path, encoding='utf-16-le') as f:
+        hp = np.genfromtxt(f, skip_header=13, max_rows=4, usecols=(6,))
+    with open(path, encoding='utf-16-le') as f:
+        arr = np.genfromtxt(f, skip_header=22, max_rows=18, usecols=list(range(1, 12)))
+    return hp, arr
+
+
+def zemax_fixture(batoid, ref_root):
+    """Zemax golden traces of the reference's tests (tests/test_zemax.py:16-63
+    HSC at 1e-9, :413-462 LSST at 1e-10) plus the reference's own traces of the
+    same rays; optics stored as the parsed YAML configuration."""
+    import copy
+    import json
+    from batoid_gb300.parse import yaml_load
+    out = {}
+    data = os.path.join(ref_root, "batoid", "data")
+    testdata = os.path.join(ref_root, "tests", "testdata")
+    # LSST, g band at 500 nm in vacuum
+    cfg = yaml_load(open(os.path.join(data, "LSST", "LSST_g_500.yaml")).read())
+    out["lsst_config"] = np.array(json.dumps(cfg))
+    tel = batoid.parse.parse_optic(copy.deepcopy(cfg["opticalSystem"]))
+    for k in range(3):
+        hp, arr = _zemax_lsst(os.path.join(testdata, f"LSST_trace_{k}.txt"))
+        out[f"lsst{k}_hp"] = hp
+        out[f"lsst{k}_zemax"] = arr
+        Hx, Hy, Px, Py = hp
+        ray = batoid.RayVector.fromStop(Px * 4.18, Py * 4.18, optic=tel, wavelength=500e-9,
+                                        theta_x=np.deg2rad(Hx * 1.75), theta_y=np.deg2rad(Hy * 1.75),
+                                        projection='zemax')
+        out.update(rv_to_dict(ray, f"lsst{k}_in"))
+        tf = tel.traceFull(ray)
+        out[f"lsst{k}_names"] = np.array(list(tf.keys()))
+        for name, v in tf.items():
+            r = v["out"].toCoordSys(batoid.CoordSys())
+            out.update(rv_to_dict(r, f"lsst{k}_{name}"))
+    # HSC (old prescription)
+    cfg = yaml_load(open(os.path.join(data, "HSC", "HSC_old.yaml")).read())
+    out["hsc_config"] = np.array(json.dumps(cfg))
+    tel = batoid.parse.parse_optic(copy.deepcopy(cfg["opticalSystem"]))
+    for k in (1, 2, 3):
+        with open(os.path.join(testdata, f"HSC_raytrace_{k}.txt")) as f:
+            arr = np.loadtxt(f, skiprows=22, usecols=list(range(0, 12)))
+        out[f"hsc{k}_zemax"] = arr
+        a0 = arr[0]
+        rv = batoid.RayVector(a0[1] / 1000, a0[2] / 1000, 16.0, a0[4], a0[5], -a0[6], t=0, wavelength=750e-9)
+        tf = tel.traceFull(rv)
+        for name, v in tf.items():
+            r = v["out"].toCoordSys(batoid.CoordSys())
+            out.update(rv_to_dict(r, f"hsc{k}_{name}"))
+    return out
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     os.environ["BATOID_REF"] = ref_root
@@ -245,6 +300,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "primitives.npz"), **primitive_fixtures(batoid))
     np.savez_compressed(os.path.join(HERE, "huygens.npz"), **huygens_fixture(batoid))
     np.savez_compressed(os.path.join(HERE, "sellmeier_csv.npz"), **sellmeier_csv_fixture(ref_root))
+    np.savez_compressed(os.path.join(HERE, "zemax.npz"), **zemax_fixture(batoid, ref_root))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
