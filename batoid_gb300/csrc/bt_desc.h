@@ -25,7 +25,8 @@ enum bt_surf_kind {
     BT_S_ASPHERE = 5,
     BT_S_POLY = 6,
     BT_S_BICUBIC = 7,
-    BT_S_SUM = 8
+    BT_S_SUM = 8,
+    BT_S_MODAL = 9
 };
 
 // Surface parameter slots (p[]):
@@ -43,6 +44,13 @@ enum bt_surf_kind {
 //  BICUBIC:    p0=x0 p1=y0 p2=dx p3=dy p4=use_nan; n=nx m=ny; tab = 4 arrays
 //              (z, dzdx, dzdy, d2zdxdy), each nx*ny, row-major [iy][ix]
 //  SUM:        n=#children m=index of first child (children are contiguous)
+//  MODAL:      sum_m a_m * table_m of nmodes bicubic tables on one grid, the
+//              amplitudes a_m supplied per job by the batched kernel:
+//              p0=x0 p1=y0 p2=dx p3=dy p4=use_nan p5=nmodes (multiple of 4);
+//              n=nx m=ny; off = pool index of the nmodes amplitudes, stored
+//              as float-float pairs; tab = FP32 mode data laid out
+//              [iy][ix][q][mode] with q = z, dz/dx, dz/dy, d2z/dxdy.
+//              Only the batched wavefront kernel evaluates it.
 typedef struct bt_surf {
     int32_t kind;
     int32_t n;

@@ -15,6 +15,7 @@
 #include <stdint.h>
 #include <math.h>
 #include "bt_desc.h"
+#include "bt_ff.cuh"
 
 struct Prog {
     const bt_stage* stages;
@@ -24,6 +25,13 @@ struct Prog {
     const double* pool;
     int nstages;
     int nmedia;
+    // Per-thread cache of the combined corner values of a MODAL surface
+    // (batched kernel only; null elsewhere).  Element k of the cache lives at
+    // mc[k * mstride] (interleaved across the block's threads).
+    double* mc;
+    float* mcf;
+    int* mcell;
+    int mstride;
 };
 
 __device__ __forceinline__ Prog prog_from_blob(const unsigned char* b) {
@@ -36,6 +44,10 @@ __device__ __forceinline__ Prog prog_from_blob(const unsigned char* b) {
     p.pool = reinterpret_cast<const double*>(b + h->off_pool);
     p.nstages = h->nstages;
     p.nmedia = h->nmedia;
+    p.mc = nullptr;
+    p.mcf = nullptr;
+    p.mcell = nullptr;
+    p.mstride = 0;
     return p;
 }
 
@@ -62,16 +74,61 @@ __device__ __forceinline__ double bt_horner2d(double x, double y, const double* 
 // Bicubic table (src/table.cpp:42-158)
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ double bt_spline1(double x, double v0, double v1, double d0, double d1) {
-    double a = 2 * (v0 - v1) + d0 + d1;
-    double b = 3 * (v1 - v0) - 2 * d0 - d1;
+template <typename T>
+__device__ __forceinline__ T bt_spline1(T x, T v0, T v1, T d0, T d1) {
+    T a = 2 * (v0 - v1) + d0 + d1;
+    T b = 3 * (v1 - v0) - 2 * d0 - d1;
     return v0 + x * (d0 + x * (b + x * a));
 }
 
-__device__ __forceinline__ double bt_spline1_grad(double x, double v0, double v1, double d0, double d1) {
-    double a = 2 * (v0 - v1) + d0 + d1;
-    double b = 3 * (v1 - v0) - 2 * d0 - d1;
+template <typename T>
+__device__ __forceinline__ T bt_spline1_grad(T x, T v0, T v1, T d0, T d1) {
+    T a = 2 * (v0 - v1) + d0 + d1;
+    T b = 3 * (v1 - v0) - 2 * d0 - d1;
     return d0 + x * (2 * b + x * 3 * a);
+}
+
+// Hermite bicubic patch from its 16 corner values; corner k of z/zx/zy/c is
+// 0 = (ix, iy), 1 = (ix+1, iy), 2 = (ix, iy+1), 3 = (ix+1, iy+1)
+// (src/table.cpp:64-158).
+template <typename T>
+__device__ __forceinline__ void bt_hermite(T xfrac, T yfrac, T dx, T dy, const T* z, const T* zx, const T* zy,
+                                           const T* c, T* val, T* gx, T* gy, bool want_val, bool want_grad) {
+    if (want_val) {
+        T v0 = bt_spline1(xfrac, z[0], z[1], zx[0] * dx, zx[1] * dx);
+        T v1 = bt_spline1(xfrac, z[2], z[3], zx[2] * dx, zx[3] * dx);
+        T d0 = bt_spline1(xfrac, zy[0], zy[1], c[0] * dx, c[1] * dx);
+        T d1 = bt_spline1(xfrac, zy[2], zy[3], c[2] * dx, c[3] * dx);
+        *val = bt_spline1(yfrac, v0, v1, d0 * dy, d1 * dy);
+    }
+    if (want_grad) {
+        T v0 = bt_spline1_grad(xfrac, z[0], z[1], zx[0] * dx, zx[1] * dx);
+        T v1 = bt_spline1_grad(xfrac, z[2], z[3], zx[2] * dx, zx[3] * dx);
+        T d0 = bt_spline1_grad(xfrac, zy[0], zy[1], c[0] * dx, c[1] * dx);
+        T d1 = bt_spline1_grad(xfrac, zy[2], zy[3], c[2] * dx, c[3] * dx);
+        *gx = bt_spline1(yfrac, v0, v1, d0 * dy, d1 * dy) / dx;
+        v0 = bt_spline1_grad(yfrac, z[0], z[2], zy[0] * dy, zy[2] * dy);
+        v1 = bt_spline1_grad(yfrac, z[1], z[3], zy[1] * dy, zy[3] * dy);
+        d0 = bt_spline1_grad(yfrac, zx[0], zx[2], c[0] * dy, c[2] * dy);
+        d1 = bt_spline1_grad(yfrac, zx[1], zx[3], c[1] * dy, c[3] * dy);
+        *gy = bt_spline1(xfrac, v0, v1, d0 * dx, d1 * dx) / dy;
+    }
+}
+
+// Cell of a table lookup; false outside the grid or for NaN input
+// (src/table.cpp:42-62).
+__device__ __forceinline__ bool bt_table_cell(const bt_surf& s, double x, double y, int* ix, int* iy,
+                                              double* xfrac, double* yfrac) {
+    const double x0 = s.p[0], y0 = s.p[1], dx = s.p[2], dy = s.p[3];
+    const int nx = s.n, ny = s.m;
+    const double fx = floor((x - x0) / dx);
+    const double fy = floor((y - y0) / dy);
+    if (!(fx >= 0.0) || !(fy >= 0.0) || fx >= (double)(nx - 1) || fy >= (double)(ny - 1)) return false;
+    *ix = (int)fx;
+    *iy = (int)fy;
+    *xfrac = (x - (x0 + *ix * dx)) / dx;
+    *yfrac = (y - (y0 + *iy * dy)) / dy;
+    return true;
 }
 
 // Evaluates the Hermite bicubic patch value and gradient.  Returns false
@@ -79,15 +136,10 @@ __device__ __forceinline__ double bt_spline1_grad(double x, double v0, double v1
 __device__ __forceinline__ bool bt_table_eval(const bt_surf& s, double x, double y,
                                               double* val, double* gx, double* gy,
                                               bool want_val, bool want_grad) {
-    const double x0 = s.p[0], y0 = s.p[1], dx = s.p[2], dy = s.p[3];
+    int ix, iy;
+    double xfrac, yfrac;
+    if (!bt_table_cell(s, x, y, &ix, &iy, &xfrac, &yfrac)) return false;
     const int nx = s.n, ny = s.m;
-    const double fx = floor((x - x0) / dx);
-    const double fy = floor((y - y0) / dy);
-    // NaN or out-of-range cell index: outside the grid (src/table.cpp:61-62)
-    if (!(fx >= 0.0) || !(fy >= 0.0) || fx >= (double)(nx - 1) || fy >= (double)(ny - 1)) return false;
-    const int ix = (int)fx, iy = (int)fy;
-    const double xfrac = (x - (x0 + ix * dx)) / dx;
-    const double yfrac = (y - (y0 + iy * dy)) / dy;
     const size_t plane = (size_t)nx * (size_t)ny;
     const double* Z = s.tab;
     const double* ZX = s.tab + plane;
@@ -95,29 +147,11 @@ __device__ __forceinline__ bool bt_table_eval(const bt_surf& s, double x, double
     const double* ZXY = s.tab + 3 * plane;
     const size_t i00 = (size_t)nx * iy + ix, i01 = i00 + 1;
     const size_t i10 = i00 + nx, i11 = i10 + 1;
-    const double z00 = __ldg(Z + i00), z01 = __ldg(Z + i01), z10 = __ldg(Z + i10), z11 = __ldg(Z + i11);
-    const double zx00 = __ldg(ZX + i00), zx01 = __ldg(ZX + i01), zx10 = __ldg(ZX + i10), zx11 = __ldg(ZX + i11);
-    const double zy00 = __ldg(ZY + i00), zy01 = __ldg(ZY + i01), zy10 = __ldg(ZY + i10), zy11 = __ldg(ZY + i11);
-    const double c00 = __ldg(ZXY + i00), c01 = __ldg(ZXY + i01), c10 = __ldg(ZXY + i10), c11 = __ldg(ZXY + i11);
-    if (want_val) {
-        double v0 = bt_spline1(xfrac, z00, z01, zx00 * dx, zx01 * dx);
-        double v1 = bt_spline1(xfrac, z10, z11, zx10 * dx, zx11 * dx);
-        double d0 = bt_spline1(xfrac, zy00, zy01, c00 * dx, c01 * dx);
-        double d1 = bt_spline1(xfrac, zy10, zy11, c10 * dx, c11 * dx);
-        *val = bt_spline1(yfrac, v0, v1, d0 * dy, d1 * dy);
-    }
-    if (want_grad) {
-        double v0 = bt_spline1_grad(xfrac, z00, z01, zx00 * dx, zx01 * dx);
-        double v1 = bt_spline1_grad(xfrac, z10, z11, zx10 * dx, zx11 * dx);
-        double d0 = bt_spline1_grad(xfrac, zy00, zy01, c00 * dx, c01 * dx);
-        double d1 = bt_spline1_grad(xfrac, zy10, zy11, c10 * dx, c11 * dx);
-        *gx = bt_spline1(yfrac, v0, v1, d0 * dy, d1 * dy) / dx;
-        v0 = bt_spline1_grad(yfrac, z00, z10, zy00 * dy, zy10 * dy);
-        v1 = bt_spline1_grad(yfrac, z01, z11, zy01 * dy, zy11 * dy);
-        d0 = bt_spline1_grad(yfrac, zx00, zx10, c00 * dy, c10 * dy);
-        d1 = bt_spline1_grad(yfrac, zx01, zx11, c01 * dy, c11 * dy);
-        *gy = bt_spline1(xfrac, v0, v1, d0 * dx, d1 * dx) / dy;
-    }
+    const double z[4] = {__ldg(Z + i00), __ldg(Z + i01), __ldg(Z + i10), __ldg(Z + i11)};
+    const double zx[4] = {__ldg(ZX + i00), __ldg(ZX + i01), __ldg(ZX + i10), __ldg(ZX + i11)};
+    const double zy[4] = {__ldg(ZY + i00), __ldg(ZY + i01), __ldg(ZY + i10), __ldg(ZY + i11)};
+    const double c[4] = {__ldg(ZXY + i00), __ldg(ZXY + i01), __ldg(ZXY + i10), __ldg(ZXY + i11)};
+    bt_hermite<double>(xfrac, yfrac, s.p[2], s.p[3], z, zx, zy, c, val, gx, gy, want_val, want_grad);
     return true;
 }
 
@@ -233,11 +267,118 @@ __device__ __forceinline__ void bt_leaf_eval(const bt_surf& s, const double* poo
     }
 }
 
+// ---------------------------------------------------------------------------
+// MODAL surface: sum_m a_m * table_m over bicubic tables sharing one grid.
+// The Hermite patch is linear in its 16 corner values, so the patch of the
+// weighted sum is the patch of the weighted corner values.  Those are formed
+// once per (ray, cell) in float-float (FP32 mode data, amplitudes as
+// float-float pairs, ~44-bit sums) and cached per thread; Newton iterates of
+// one ray nearly always stay in one cell.  The cache is invalidated (cell
+// -1) whenever the amplitudes change.
+// ---------------------------------------------------------------------------
+
+// a * b for float-float a and float b; the pair is left unnormalised (the
+// following ff_add renormalises).
+__device__ __forceinline__ ff ff_mulf(ff a, float b) {
+    const float p = a.hi * b;
+    float e = fmaf(a.hi, b, -p);
+    e = fmaf(a.lo, b, e);
+    return ff{p, e};
+}
+
+__device__ __forceinline__ bool bt_modal_locate(const Prog& P, const bt_surf& s, double x, double y,
+                                                double* xfrac, double* yfrac) {
+    int ix, iy;
+    if (!bt_table_cell(s, x, y, &ix, &iy, xfrac, yfrac)) return false;
+    const int nx = s.n;
+    const int cell = iy * nx + ix;
+    if (*P.mcell == cell) return true;
+    const int st = P.mstride;
+    const int nq = (int)s.p[5] / 4;  // float4 groups per quantity
+    const ff* a = ff_ptr(P.pool, s.off);
+    const float4* T = reinterpret_cast<const float4*>(s.tab);
+    const size_t node0 = (size_t)nx * iy + ix;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const size_t node = node0 + (c & 1) + ((c >> 1) ? (size_t)nx : 0);
+        const float4* v = T + node * (size_t)(4 * nq);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            ff acc{0.f, 0.f};
+            for (int k = 0; k < nq; k++) {
+                const float4 w = __ldg(v + q * nq + k);
+                acc = ff_add(acc, ff_mulf(a[4 * k + 0], w.x));
+                acc = ff_add(acc, ff_mulf(a[4 * k + 1], w.y));
+                acc = ff_add(acc, ff_mulf(a[4 * k + 2], w.z));
+                acc = ff_add(acc, ff_mulf(a[4 * k + 3], w.w));
+            }
+            P.mc[(q * 4 + c) * st] = ff_to_double(acc);
+            P.mcf[(q * 4 + c) * st] = acc.hi + acc.lo;
+        }
+    }
+    *P.mcell = cell;
+    return true;
+}
+
+// FP64 sag and slope (ux, uy) = (-dz/dx, -dz/dy) (src/bicubic.cpp:19-40).
+__device__ __forceinline__ void bt_modal_eval(const Prog& P, const bt_surf& s, double x, double y,
+                                              bool want_sag, bool want_slope, double* sag, double* ux,
+                                              double* uy) {
+    double xf, yf;
+    if (P.mc == nullptr || !bt_modal_locate(P, s, x, y, &xf, &yf)) {
+        const double fill = (P.mc == nullptr || s.p[4] != 0.0) ? (double)NAN : 0.0;
+        if (want_sag) *sag = fill;
+        if (want_slope) { *ux = fill; *uy = fill; }
+        return;
+    }
+    const int st = P.mstride;
+    double v[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) v[k] = P.mc[k * st];
+    double val = 0.0, gx = 0.0, gy = 0.0;
+    bt_hermite<double>(xf, yf, s.p[2], s.p[3], v, v + 4, v + 8, v + 12, &val, &gx, &gy, want_sag, want_slope);
+    if (want_sag) *sag = val;
+    if (want_slope) { *ux = -gx; *uy = -gy; }
+}
+
+// FP64 sag with an FP32 slope, for Newton iterations.
+__device__ __forceinline__ void bt_modal_newton_eval(const Prog& P, const bt_surf& s, double x, double y,
+                                                     double* sag, float* ux, float* uy) {
+    double xf, yf;
+    if (P.mc == nullptr || !bt_modal_locate(P, s, x, y, &xf, &yf)) {
+        const double fill = (P.mc == nullptr || s.p[4] != 0.0) ? (double)NAN : 0.0;
+        *sag = fill;
+        *ux = (float)fill;
+        *uy = (float)fill;
+        return;
+    }
+    const int st = P.mstride;
+    double v[16];
+    float w[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        v[k] = P.mc[k * st];
+        w[k] = P.mcf[k * st];
+    }
+    double val;
+    bt_hermite<double>(xf, yf, s.p[2], s.p[3], v, v + 4, v + 8, v + 12, &val, nullptr, nullptr, true, false);
+    float gx, gy;
+    bt_hermite<float>((float)xf, (float)yf, (float)s.p[2], (float)s.p[3], w, w + 4, w + 8, w + 12, nullptr, &gx,
+                      &gy, false, true);
+    *sag = val;
+    *ux = -gx;
+    *uy = -gy;
+}
+
 // Sag and slope of any surface (Sum adds its children: src/sum.cpp:23-45).
 __device__ __forceinline__ void bt_surf_eval(const Prog& P, int si, double x, double y,
                                              bool want_sag, bool want_slope,
                                              double* sag, double* ux, double* uy) {
     const bt_surf& s = P.surfs[si];
+    if (s.kind == BT_S_MODAL) {
+        bt_modal_eval(P, s, x, y, want_sag, want_slope, sag, ux, uy);
+        return;
+    }
     if (s.kind != BT_S_SUM) {
         bt_leaf_eval(s, P.pool, x, y, want_sag, want_slope, sag, ux, uy);
         return;
@@ -245,7 +386,9 @@ __device__ __forceinline__ void bt_surf_eval(const Prog& P, int si, double x, do
     double z = 0.0, gx = 0.0, gy = 0.0;
     for (int c = 0; c < s.n; c++) {
         double cz = 0.0, cx = 0.0, cy = 0.0;
-        bt_leaf_eval(P.surfs[s.m + c], P.pool, x, y, want_sag, want_slope, &cz, &cx, &cy);
+        const bt_surf& cs = P.surfs[s.m + c];
+        if (cs.kind == BT_S_MODAL) bt_modal_eval(P, cs, x, y, want_sag, want_slope, &cz, &cx, &cy);
+        else bt_leaf_eval(cs, P.pool, x, y, want_sag, want_slope, &cz, &cx, &cy);
         z += cz; gx += cx; gy += cy;
     }
     if (want_sag) *sag = z;
@@ -575,7 +718,6 @@ __device__ __forceinline__ bool bt_obsc_run(const Prog& P, int begin, int end, d
 // p[9] = 1/R (0 when R == 0); p[10] = 1 when the conic sag may use
 // (1 - q) * R/(1+k), i.e. |R/(1+k)| <= 100 (absolute error <= 100 ulp(1)).
 // ===========================================================================
-#include "bt_ff.cuh"
 
 // sqrt(w) from w * rsqrt(w), exact for w == 0 and NaN for w < 0.
 __device__ __forceinline__ void bt_sqrt_rsqrt(double w, double* q, double* rs) {
@@ -687,6 +829,10 @@ __device__ __forceinline__ void bt_leaf_newton_eval(const bt_surf& s, const doub
 __device__ __forceinline__ void bt_surf_newton_eval(const Prog& P, int si, double x, double y, double* sag,
                                                     float* ux, float* uy) {
     const bt_surf& s = P.surfs[si];
+    if (s.kind == BT_S_MODAL) {
+        bt_modal_newton_eval(P, s, x, y, sag, ux, uy);
+        return;
+    }
     if (s.kind != BT_S_SUM) {
         bt_leaf_newton_eval(s, P.pool, x, y, sag, ux, uy);
         return;
@@ -696,7 +842,9 @@ __device__ __forceinline__ void bt_surf_newton_eval(const Prog& P, int si, doubl
     for (int c = 0; c < s.n; c++) {
         double cz;
         float cx, cy;
-        bt_leaf_newton_eval(P.surfs[s.m + c], P.pool, x, y, &cz, &cx, &cy);
+        const bt_surf& cs = P.surfs[s.m + c];
+        if (cs.kind == BT_S_MODAL) bt_modal_newton_eval(P, cs, x, y, &cz, &cx, &cy);
+        else bt_leaf_newton_eval(cs, P.pool, x, y, &cz, &cx, &cy);
         z += cz;
         gx += cx;
         gy += cy;
@@ -750,6 +898,11 @@ __device__ __forceinline__ void bt_leaf_slope_precise(const bt_surf& s, const do
 __device__ __forceinline__ void bt_surf_slope_precise(const Prog& P, int si, double x, double y, double* ux,
                                                       double* uy) {
     const bt_surf& s = P.surfs[si];
+    double z;
+    if (s.kind == BT_S_MODAL) {
+        bt_modal_eval(P, s, x, y, false, true, &z, ux, uy);
+        return;
+    }
     if (s.kind != BT_S_SUM) {
         bt_leaf_slope_precise(s, P.pool, x, y, ux, uy);
         return;
@@ -757,7 +910,9 @@ __device__ __forceinline__ void bt_surf_slope_precise(const Prog& P, int si, dou
     double gx = 0.0, gy = 0.0;
     for (int c = 0; c < s.n; c++) {
         double cx, cy;
-        bt_leaf_slope_precise(P.surfs[s.m + c], P.pool, x, y, &cx, &cy);
+        const bt_surf& cs = P.surfs[s.m + c];
+        if (cs.kind == BT_S_MODAL) bt_modal_eval(P, cs, x, y, false, true, &z, &cx, &cy);
+        else bt_leaf_slope_precise(cs, P.pool, x, y, &cx, &cy);
         gx += cx;
         gy += cy;
     }
@@ -870,6 +1025,7 @@ __device__ __forceinline__ bool bt_leaf_tti_fast(const Prog& P, int si, double x
     }
     case BT_S_POLY:
     case BT_S_BICUBIC:
+    case BT_S_MODAL:
         return bt_newton_mixed(P, si, x, y, z, vx, vy, vz, dt, niter);
     default: {
         double ux, uy;
