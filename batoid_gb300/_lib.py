@@ -50,6 +50,38 @@ class BatoidError(RuntimeError):
         self.code = code
 
 
+class BtBatchDesc(ctypes.Structure):
+    """bt_batch_desc of include/batoid_gb300.h."""
+    _fields_ = [
+        ("nstages", c_size_t),
+        ("kinds", c_void_p),
+        ("surfaces", c_void_p),
+        ("dr", c_void_p),
+        ("drot", c_void_p),
+        ("media", c_void_p),
+        ("obscurations", c_void_p),
+        ("nvar", c_int),
+        ("var_stages", c_void_p),
+        ("modal_stage", c_int),
+        ("modal_grid", c_double * 4),
+        ("modal_nx", c_int),
+        ("modal_ny", c_int),
+        ("nmodes", c_int),
+        ("modes", c_void_p),
+        ("modal_use_nan", c_int),
+        ("stop_dr", c_double * 3),
+        ("stop_drot", c_double * 9),
+        ("sphere", c_void_p),
+        ("sphere_radius", c_double),
+        ("pupil_size", c_double),
+        ("r_inner", c_double),
+        ("r_outer", c_double),
+        ("jmax", c_int),
+        ("basis", c_void_p),
+        ("side", c_int),
+    ]
+
+
 # (name, restype, argtypes); handles are void*.
 _P = c_void_p
 _PP = ctypes.POINTER(c_void_p)
@@ -124,6 +156,12 @@ _SIGS = [
     ("bt_huygens_amplitudes_noalloc", c_int, [ctypes.POINTER(BtRayVector), c_double, c_double, c_double,
                                               c_double_p, c_int, c_int, c_double, c_int, _P, _P, _P]),
     ("bt_zernike_normal_equations", c_int, [_P, _P, _P, _P, c_int, _P, c_int, c_int, _P, _P, _P]),
+    ("bt_batch_create", c_int, [ctypes.POINTER(BtBatchDesc), _PP]),
+    ("bt_batch_destroy", None, [_P]),
+    ("bt_batch_prepare", c_int, [_P, c_int, _P, _P]),
+    ("bt_batch_zernike", c_int, [_P, c_int, _P, _P, _P, _P, _P, c_int, _P, _P, _P, _P, c_int, c_int, c_int, _P]),
+    ("bt_batch_zernike_graph", c_int, [_P, c_int, _P, _P, _P, _P, _P, c_int, _P, _P, _P, _P, c_int, c_int, c_int,
+                                       _P]),
     ("bt_measure_fp64_peak", c_int, [c_int, c_double_p, _P]),
     ("bt_check_device_status", c_int, [_P]),
 ]

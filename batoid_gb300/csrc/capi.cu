@@ -9,6 +9,7 @@
 #include <mutex>
 #include "../../include/batoid_gb300.h"
 #include "bt_internal.h"
+#include "bt_batch.h"
 
 // ---------------------------------------------------------------------------
 // errors
@@ -1151,8 +1152,355 @@ extern "C" int bt_measure_fp64_peak(int iters, double* tflops, void* stream) {
 // Test hook: reads and clears the device status word of the trace kernels
 // (BT_ERR_TIMEOUT if a bounded wait expired).  Synchronous.
 extern "C" int bt_check_device_status(void* stream) {
-    int st = 0;
+    int st = 0, sb = 0;
     CUDA_TRY(bt_read_device_status(&st, (cudaStream_t)stream), "device status");
-    if (st != 0) return fail(st, "a kernel's bounded wait expired");
+    CUDA_TRY(bt_read_batch_device_status(&sb, (cudaStream_t)stream), "device status");
+    if (st != 0 || sb != 0) return fail(st != 0 ? st : sb, "a kernel's bounded wait expired");
+    return BT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched wavefronts / Zernike fits
+// ---------------------------------------------------------------------------
+
+struct bt_batch {
+    unsigned char* d_blob = nullptr;
+    int blob_bytes = 0;
+    int ntrace = 0;
+    int nvar = 0;
+    int var_stage[BT_BATCH_MAX_VAR] = {0};
+    int modal_surf = -1;
+    int nmodes = 0;
+    double stop_dr[3] = {0, 0, 0};
+    double stop_drot[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    double sphere_R = 0.0;
+    double pupil = 0.0;
+    double r_in2 = 0.0, r_out2 = 0.0;
+    int jmax = 0;
+    int side = 0;
+    double* d_cart = nullptr;
+    std::vector<long long> off;  // per grid size, -1 where absent
+    long long* d_off = nullptr;
+    double* d_basis = nullptr;
+    double* d_gref = nullptr;
+    int* d_counter = nullptr;
+    std::mutex mu;
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<unsigned char> gkey;
+};
+
+static void batch_free(bt_batch* b) {
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->d_blob) cudaFree(b->d_blob);
+    if (b->d_cart) cudaFree(b->d_cart);
+    if (b->d_off) cudaFree(b->d_off);
+    if (b->d_basis) cudaFree(b->d_basis);
+    if (b->d_gref) cudaFree(b->d_gref);
+    if (b->d_counter) cudaFree(b->d_counter);
+    delete b;
+}
+
+extern "C" void bt_batch_destroy(bt_batch* b) {
+    if (b) batch_free(b);
+}
+
+extern "C" int bt_batch_create(const bt_batch_desc* d, bt_batch** out) {
+    if (!d || !out) return fail(BT_ERR_ARG, "batch: null argument");
+    if (d->nstages < 1 || d->nstages + 1 > BT_MAX_STAGES) return fail(BT_ERR_UNSUPPORTED, "batch: stage count");
+    if (!d->kinds || !d->surfaces || !d->dr || !d->drot) return fail(BT_ERR_ARG, "batch: null stage arrays");
+    if (d->nvar < 0 || d->nvar > BT_BATCH_MAX_VAR || (d->nvar > 0 && !d->var_stages))
+        return fail(BT_ERR_ARG, "batch: at most 8 varying stages");
+    if (d->jmax < 1 || d->jmax > BT_BATCH_MAX_J) return fail(BT_ERR_UNSUPPORTED, "batch: jmax must be 1..32");
+    if (d->side < 1 || !d->basis) return fail(BT_ERR_ARG, "batch: missing fit basis");
+    if (!d->sphere) return fail(BT_ERR_ARG, "batch: missing reference sphere");
+    if (!(d->pupil_size > 0.0) || !(d->r_outer >= d->r_inner)) return fail(BT_ERR_ARG, "batch: pupil / annulus");
+    const bool modal = d->modal_stage >= 0;
+    if (modal) {
+        if ((size_t)d->modal_stage >= d->nstages) return fail(BT_ERR_ARG, "batch: modal stage out of range");
+        if (d->nmodes < 4 || d->nmodes % 4 != 0 || !d->modes || d->modal_nx < 2 || d->modal_ny < 2)
+            return fail(BT_ERR_ARG, "batch: modal tables (nmodes a positive multiple of 4, grid >= 2x2)");
+        if (((uintptr_t)d->modes & 15) != 0) return fail(BT_ERR_ARG, "batch: mode data must be 16-byte aligned");
+    }
+    bt_batch* b = new bt_batch;
+    ProgBuilder pb;
+    for (size_t k = 0; k < d->nstages; k++) {
+        const int kind = d->kinds[k];
+        if (kind != BT_ST_INTERSECT && kind != BT_ST_REFLECT && kind != BT_ST_REFRACT) {
+            batch_free(b);
+            return fail(BT_ERR_ARG, "batch: bad stage kind");
+        }
+        if (!d->surfaces[k]) {
+            batch_free(b);
+            return fail(BT_ERR_ARG, "batch: null surface");
+        }
+        bt_stage st = blank_stage(kind);
+        set_transform(st, d->dr + 3 * k, d->drot + 9 * k);
+        st.surf = pb.add_surface(d->surfaces[k]);
+        if (st.surf < 0) {
+            batch_free(b);
+            return BT_ERR_CUDA;
+        }
+        if (modal && (int)k == d->modal_stage) {
+            bt_surf m;
+            memset(&m, 0, sizeof(m));
+            m.kind = BT_S_MODAL;
+            m.n = d->modal_nx;
+            m.m = d->modal_ny;
+            for (int i = 0; i < 4; i++) m.p[i] = d->modal_grid[i];
+            m.p[4] = d->modal_use_nan ? 1.0 : 0.0;
+            m.p[5] = (double)d->nmodes;
+            m.off = (int32_t)pb.pool.size();
+            m.tab = reinterpret_cast<const double*>(d->modes);
+            pb.pool.insert(pb.pool.end(), (size_t)d->nmodes, 0.0);  // amplitudes, per job
+            const int root = st.surf;
+            const int nrec = (int)pb.surfs.size();
+            if (pb.surfs[root].kind == BT_S_SUM && pb.surfs[root].m + pb.surfs[root].n == nrec &&
+                pb.surfs[root].n < BT_MAX_SUM_CHILDREN) {
+                pb.surfs.push_back(m);
+                pb.surfs[root].n += 1;
+                b->modal_surf = nrec;
+            } else if (pb.surfs[root].kind != BT_S_SUM && root == nrec - 1) {
+                pb.surfs.push_back(m);
+                bt_surf sum;
+                memset(&sum, 0, sizeof(sum));
+                sum.kind = BT_S_SUM;
+                sum.n = 2;
+                sum.m = root;
+                pb.surfs.push_back(sum);
+                st.surf = nrec + 1;
+                b->modal_surf = nrec;
+            } else {
+                batch_free(b);
+                return fail(BT_ERR_UNSUPPORTED, "batch: cannot add the bending term to this surface");
+            }
+        }
+        if (kind == BT_ST_REFRACT) {
+            if (!d->media || !d->media[k]) {
+                batch_free(b);
+                return fail(BT_ERR_ARG, "batch: refracting stage without a medium");
+            }
+            st.medium = pb.add_medium(d->media[k]);
+        }
+        if (d->obscurations && d->obscurations[k]) pb.add_obsc(d->obscurations[k], &st.obsc_begin, &st.obsc_end);
+        pb.stages.push_back(st);
+    }
+    for (int v = 0; v < d->nvar; v++) {
+        const int k = d->var_stages[v];
+        if (k < 0 || (size_t)k >= d->nstages) {
+            batch_free(b);
+            return fail(BT_ERR_ARG, "batch: varying stage out of range");
+        }
+        pb.stages[k].identity = 0;
+        b->var_stage[v] = k;
+    }
+    bt_stage sph = blank_stage(BT_ST_INTERSECT);
+    sph.identity = 0;
+    sph.surf = pb.add_surface(d->sphere);
+    if (sph.surf < 0) {
+        batch_free(b);
+        return BT_ERR_CUDA;
+    }
+    pb.stages.push_back(sph);
+    std::vector<unsigned char> blob = pb.blob();
+    if (blob.size() > kMaxBlobBytes) {
+        batch_free(b);
+        return fail(BT_ERR_UNSUPPORTED, "batch: descriptor too large");
+    }
+    b->blob_bytes = (int)blob.size();
+    b->ntrace = (int)d->nstages;
+    b->nvar = d->nvar;
+    b->nmodes = modal ? d->nmodes : 0;
+    for (int i = 0; i < 3; i++) b->stop_dr[i] = d->stop_dr[i];
+    for (int i = 0; i < 9; i++) b->stop_drot[i] = d->stop_drot[i];
+    b->sphere_R = d->sphere_radius;
+    b->pupil = d->pupil_size;
+    b->r_in2 = d->r_inner * d->r_inner;
+    b->r_out2 = d->r_outer * d->r_outer;
+    b->jmax = d->jmax;
+    b->side = d->side;
+    b->off.assign(BT_BATCH_MAX_NX + 1, -1);
+    const size_t ncart = (size_t)d->jmax * d->side * d->side;
+    const size_t ngref = (size_t)(BT_BATCH_MAX_NX + 1) * d->jmax * d->jmax;
+    cudaError_t e = cudaMalloc((void**)&b->d_blob, blob.size());
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_cart, ncart * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_cart, d->basis, ncart * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_off, b->off.size() * sizeof(long long));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_off, b->off.data(), b->off.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_gref, ngref * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(b->d_gref, 0, ngref * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_counter, sizeof(int));
+    if (e == cudaSuccess) e = bt_batch_set_smem_limit();
+    if (e != cudaSuccess) {
+        batch_free(b);
+        return cuda_fail(e, "batch: set-up");
+    }
+    *out = b;
+    return BT_OK;
+}
+
+extern "C" int bt_batch_prepare(bt_batch* b, int n, const int* nx_values, void* stream) {
+    if (!b || (n > 0 && !nx_values)) return fail(BT_ERR_ARG, "batch prepare: null argument");
+    std::lock_guard<std::mutex> lock(b->mu);
+    std::vector<char> want(BT_BATCH_MAX_NX + 1, 0);
+    bool fresh = false;
+    for (int i = 0; i < n; i++) {
+        const int nx = nx_values[i];
+        if (nx < 2 || nx > BT_BATCH_MAX_NX) return fail(BT_ERR_ARG, "batch prepare: grid size must be 2..512");
+        want[nx] = 1;
+        if (b->off[nx] < 0) fresh = true;
+    }
+    if (!fresh) return BT_OK;
+    for (int nx = 0; nx <= BT_BATCH_MAX_NX; nx++)
+        if (b->off[nx] >= 0) want[nx] = 1;
+    std::vector<long long> off(BT_BATCH_MAX_NX + 1, -1);
+    std::vector<int> list;
+    long long total = 0;
+    for (int nx = 2; nx <= BT_BATCH_MAX_NX; nx++) {
+        if (!want[nx]) continue;
+        off[nx] = total;
+        total += (long long)nx * nx * b->jmax;
+        list.push_back(nx);
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    double* basis = nullptr;
+    int* d_list = nullptr;
+    cudaError_t e = cudaMalloc((void**)&basis, (size_t)total * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_list, list.size() * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_list, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->d_off, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice, s);
+    for (size_t i = 0; e == cudaSuccess && i < list.size(); i++)
+        e = bt_launch_batch_tables(list[i], b->pupil, b->d_cart, b->jmax, b->side, basis + off[list[i]], s);
+    if (e == cudaSuccess)
+        e = bt_launch_batch_gref(d_list, (int)list.size(), b->pupil, b->r_in2, b->r_out2, basis, b->d_off, b->jmax,
+                                 b->d_gref, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (d_list) cudaFree(d_list);
+    if (e != cudaSuccess) {
+        if (basis) cudaFree(basis);
+        // device offsets may already name the new tables: mark all absent
+        std::vector<long long> none(BT_BATCH_MAX_NX + 1, -1);
+        cudaMemcpy(b->d_off, none.data(), none.size() * sizeof(long long), cudaMemcpyHostToDevice);
+        b->off = none;
+        if (b->d_basis) cudaFree(b->d_basis);
+        b->d_basis = nullptr;
+        return cuda_fail(e, "batch prepare");
+    }
+    if (b->d_basis) cudaFree(b->d_basis);
+    b->d_basis = basis;
+    b->off = off;
+    if (b->gexec) {
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+        b->gkey.clear();
+    }
+    return BT_OK;
+}
+
+static int batch_args(bt_batch* b, int nstates, const double* xf, const double* det, const double* amps,
+                      const int* nx, const double* wavelength, int nfields, const double* fields, const int* order,
+                      double* coefs, int* status, int threads, int ctas_per_sm, int niter, BatchArgs* a) {
+    if (!b) return fail(BT_ERR_ARG, "batch: null plan");
+    if (nstates < 0 || nfields < 0) return fail(BT_ERR_ARG, "batch: negative sizes");
+    if ((long long)nstates * nfields > 0x7fffffffLL) return fail(BT_ERR_UNSUPPORTED, "batch: too many jobs");
+    if (threads < 32 || threads > BT_BATCH_MAX_THREADS || threads % 32 != 0)
+        return fail(BT_ERR_ARG, "batch: threads must be 32..256, a multiple of 32");
+    if (ctas_per_sm < 1) return fail(BT_ERR_ARG, "batch: ctas_per_sm must be >= 1");
+    if (niter < 0) return fail(BT_ERR_ARG, "batch: negative niter");
+    if (bt_batch_smem_layout(b->blob_bytes, threads, b->jmax).total > BT_BATCH_MAX_SMEM)
+        return fail(BT_ERR_UNSUPPORTED, "batch: shared memory exceeds the limit for this block size");
+    const int njobs = nstates * nfields;
+    if (njobs > 0 && (!nx || !wavelength || !fields || !order || !coefs || !status || !det ||
+                      (b->nvar > 0 && !xf) || (b->nmodes > 0 && !amps)))
+        return fail(BT_ERR_ARG, "batch: null array");
+    if (!b->d_basis && njobs > 0) return fail(BT_ERR_ARG, "batch: no grid size prepared");
+    memset(a, 0, sizeof(*a));
+    a->xf = xf;
+    a->det = det;
+    a->amps = amps;
+    a->nxs = nx;
+    a->wl = wavelength;
+    a->field = fields;
+    a->basis = b->d_basis;
+    a->basis_off = b->d_off;
+    a->gref = b->d_gref;
+    a->order = order;
+    a->counter = b->d_counter;
+    a->coefs = coefs;
+    a->status = status;
+    a->njobs = njobs;
+    a->nfields = nfields;
+    a->nx_cap = BT_BATCH_MAX_NX;
+    a->nvar = b->nvar;
+    for (int i = 0; i < BT_BATCH_MAX_VAR; i++) a->var_stage[i] = b->var_stage[i];
+    a->ntrace = b->ntrace;
+    a->modal_surf = b->modal_surf;
+    a->nmodes = b->nmodes;
+    for (int i = 0; i < 3; i++) a->stop_dr[i] = b->stop_dr[i];
+    for (int i = 0; i < 9; i++) a->stop_drot[i] = b->stop_drot[i];
+    a->sphere_R = b->sphere_R;
+    a->pupil = b->pupil;
+    a->r_in2 = b->r_in2;
+    a->r_out2 = b->r_out2;
+    a->jmax = b->jmax;
+    a->niter = niter;
+    return BT_OK;
+}
+
+extern "C" int bt_batch_zernike(bt_batch* b, int nstates, const double* xf, const double* det, const double* amps,
+                                const int* nx, const double* wavelength, int nfields, const double* fields,
+                                const int* order, double* coefs, int* status, int threads, int ctas_per_sm,
+                                int niter, void* stream) {
+    BatchArgs a;
+    int rc = batch_args(b, nstates, xf, det, amps, nx, wavelength, nfields, fields, order, coefs, status, threads,
+                        ctas_per_sm, niter, &a);
+    if (rc != BT_OK) return rc;
+    std::lock_guard<std::mutex> lock(b->mu);
+    CUDA_TRY(bt_launch_batch_zernike(b->d_blob, b->blob_bytes, a, threads, ctas_per_sm, (cudaStream_t)stream),
+             "batch zernike");
+    return BT_OK;
+}
+
+extern "C" int bt_batch_zernike_graph(bt_batch* b, int nstates, const double* xf, const double* det,
+                                      const double* amps, const int* nx, const double* wavelength, int nfields,
+                                      const double* fields, const int* order, double* coefs, int* status,
+                                      int threads, int ctas_per_sm, int niter, void* stream) {
+    if (!stream) return fail(BT_ERR_ARG, "batch graph: the legacy default stream cannot be captured");
+    BatchArgs a;
+    int rc = batch_args(b, nstates, xf, det, amps, nx, wavelength, nfields, fields, order, coefs, status, threads,
+                        ctas_per_sm, niter, &a);
+    if (rc != BT_OK) return rc;
+    if (a.njobs == 0) return BT_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<unsigned char> key(sizeof(a) + 3 * sizeof(int) + sizeof(void*));
+    memcpy(key.data(), &a, sizeof(a));
+    const int extra[3] = {threads, ctas_per_sm, niter};
+    memcpy(key.data() + sizeof(a), extra, sizeof(extra));
+    memcpy(key.data() + sizeof(a) + sizeof(extra), &stream, sizeof(void*));
+    std::lock_guard<std::mutex> lock(b->mu);
+    if (!b->gexec || b->gkey != key) {
+        if (b->gexec) {
+            cudaGraphExecDestroy(b->gexec);
+            b->gexec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "batch graph capture");
+        cudaError_t le = bt_launch_batch_zernike(b->d_blob, b->blob_bytes, a, threads, ctas_per_sm, s);
+        cudaError_t ce = cudaStreamEndCapture(s, &g);
+        if (le != cudaSuccess || ce != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_fail(le != cudaSuccess ? le : ce, "batch graph capture");
+        }
+        cudaError_t ie = cudaGraphInstantiate(&b->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+            b->gexec = nullptr;
+            return cuda_fail(ie, "batch graph instantiate");
+        }
+        b->gkey = key;
+    }
+    CUDA_TRY(cudaGraphLaunch(b->gexec, s), "batch graph launch");
     return BT_OK;
 }

@@ -137,7 +137,19 @@ class _Program:
         self.nstages = n
         dr = np.ascontiguousarray(dr)
         drot = np.ascontiguousarray(drot)
-        self._optic = _make_optic(n, kinds, surfs, dr, drot, media, obscs, coats)
+        # the stage arrays, also used to build batched plans of this optic
+        self.arrays = dict(kinds=kinds, surfs=surfs, dr=dr, drot=drot, media=media, obscs=obscs)
+        self._coats = coats
+        self._handle = None
+
+    @property
+    def _optic(self):
+        # the device program is built on first use
+        if self._handle is None:
+            a = self.arrays
+            self._handle = _make_optic(self.nstages, a["kinds"], a["surfs"], a["dr"], a["drot"], a["media"],
+                                       a["obscs"], self._coats)
+        return self._handle
 
     def trace(self, rv):
         from .global_vars import _batoid_niter

@@ -243,6 +243,87 @@ int bt_zernike_normal_equations(const double* x, const double* y, const double* 
                                 int nfits, const double* basis, int jmax, int side, double* G, double* b,
                                 void* stream);
 
+/* ---- Batched wavefronts and Zernike fits of perturbed states --------------
+ * No single counterpart in the reference.  One call computes, for every
+ * (state, field) job of nstates x nfields, what batoid.zernike
+ * (batoid/analysis.py:479-573; reference='chief', include_vignetted=False)
+ * computes for one optic on top of batoid.wavefront (batoid/analysis.py:
+ * 308-388): an nx x nx RayVector.asGrid pupil grid (batoid/rayVector.py:
+ * 220-444) traced through the state's optic, moved to the reference sphere
+ * of radius sphere_radius around the chief ray's image, OPD in waves, and the
+ * least-squares fit of jmax annular Zernike terms to the non-vignetted OPD.
+ * All jobs run in one persistent kernel launch.
+ *
+ * A state differs from the nominal optic in (a) the transforms of the stages
+ * listed in var_stages (rigid-body motions: the per-state table replaces
+ * them) and (b) an optional bending term sum_m a_m * table_m added to the
+ * surface of stage modal_stage, the tables being nmodes bicubic tables on
+ * one grid (FP32 device data, layout [iy][ix][q][mode], q = z, dz/dx,
+ * dz/dy, d2z/dxdy, nmodes a multiple of 4; the caller keeps it alive).     */
+typedef struct bt_batch bt_batch;
+
+typedef struct bt_batch_desc {
+    /* nominal optic: the arrays of bt_optic_create (no coatings) */
+    size_t nstages;
+    const int* kinds;
+    const bt_surface* const* surfaces;
+    const double* dr;
+    const double* drot;
+    const bt_medium_h* const* media;
+    const bt_obscuration* const* obscurations;
+    /* stages whose transform is given per state (at most 8) */
+    int nvar;
+    const int* var_stages;
+    /* bending term (modal_stage = -1: none) */
+    int modal_stage;
+    double modal_grid[4]; /* x0, y0, dx, dy */
+    int modal_nx;
+    int modal_ny;
+    int nmodes;
+    const float* modes;   /* device */
+    int modal_use_nan;
+    /* flat stop surface: transform from its frame to the rays' input frame */
+    double stop_dr[3];
+    double stop_drot[9];
+    /* reference sphere: a Sphere(-sphere_radius) surface */
+    const bt_surface* sphere;
+    double sphere_radius;
+    /* fit: pupil grid side, annulus of the fit, basis (host array of jmax
+     * side x side Cartesian coefficient arrays, as for the normal equations) */
+    double pupil_size;
+    double r_inner;
+    double r_outer;
+    int jmax;             /* <= 32 */
+    const double* basis;
+    int side;
+} bt_batch_desc;
+
+int bt_batch_create(const bt_batch_desc* desc, bt_batch** out);
+void bt_batch_destroy(bt_batch* b);
+/* Builds the fit tables of the given grid sizes (2 <= nx <= 512; host
+ * array).  Synchronous; call before bt_batch_zernike uses those sizes. */
+int bt_batch_prepare(bt_batch* b, int n, const int* nx_values, void* stream);
+/* Device arrays, per state s: xf[s][nvar][12] (dr(3), drot(9) of each varying
+ * stage), det[s][12] (origin(3), rot(9) row-major of the last stage's
+ * frame), amps[s][nmodes], nx[s], wavelength[s]; per field f: fields[f][18]
+ * (back-propagation frame dr(3), rot(9), local velocity(3), velocity(3) as
+ * batoid's finishParallel takes them); order[njobs] = job ids s*nfields+f in
+ * scheduling order.  Outputs coefs[job][jmax+1] (waves, entry 0 = 0) and
+ * status[job] (0, BT_ERR_ARG for a grid size not prepared, BT_ERR_RANK,
+ * -1 if never processed).  threads: 32..256, a multiple of 32; ctas_per_sm
+ * >= 1.  Stream-ordered. */
+int bt_batch_zernike(bt_batch* b, int nstates, const double* xf, const double* det, const double* amps,
+                     const int* nx, const double* wavelength, int nfields, const double* fields,
+                     const int* order, double* coefs, int* status, int threads, int ctas_per_sm, int niter,
+                     void* stream);
+/* Same, replayed from a CUDA graph captured on the first call with these
+ * arguments (recaptured when they change).  stream must not be the legacy
+ * default stream. */
+int bt_batch_zernike_graph(bt_batch* b, int nstates, const double* xf, const double* det, const double* amps,
+                           const int* nx, const double* wavelength, int nfields, const double* fields,
+                           const int* order, double* coefs, int* status, int threads, int ctas_per_sm,
+                           int niter, void* stream);
+
 /* Measures the device's FP64 FMA throughput (TFLOP/s, 2 flops per FMA)
  * with independent DFMA chains; `iters` FMAs per chain (e.g. 1 << 14).
  * The denominator of the tracer's FP64 roofline.  Synchronous. */
