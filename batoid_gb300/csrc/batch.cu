@@ -382,9 +382,25 @@ __global__ void k_batch_gref(const int* __restrict__ nx_list, double pupil, doub
     }
 }
 
+static int g_batch_smem_max = 0;
+
+// Largest dynamic shared memory the kernel can take on this device: the
+// per-block opt-in maximum less the kernel's static shared memory.
 cudaError_t bt_batch_set_smem_limit() {
-    return cudaFuncSetAttribute(k_batch_zernike, cudaFuncAttributeMaxDynamicSharedMemorySize, BT_BATCH_MAX_SMEM);
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_batch_zernike);
+    if (e != cudaSuccess) return e;
+    int lim = optin - (int)fa.sharedSizeBytes;
+    if (lim > BT_BATCH_MAX_SMEM) lim = BT_BATCH_MAX_SMEM;
+    e = cudaFuncSetAttribute(k_batch_zernike, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    if (e == cudaSuccess) g_batch_smem_max = lim;
+    return e;
 }
+
+int bt_batch_smem_max() { return g_batch_smem_max; }
 
 cudaError_t bt_launch_batch_zernike(const unsigned char* d_blob, int blob_bytes, const BatchArgs& a, int threads,
                                     int ctas_per_sm, cudaStream_t stream) {

@@ -81,6 +81,7 @@ __host__ __device__ inline BatchSmem bt_batch_smem_layout(int blob_bytes, int T,
 }
 
 cudaError_t bt_batch_set_smem_limit();
+int bt_batch_smem_max();
 cudaError_t bt_launch_batch_zernike(const unsigned char* d_blob, int blob_bytes, const BatchArgs& a, int threads,
                                     int ctas_per_sm, cudaStream_t stream);
 cudaError_t bt_launch_batch_tables(int nx, double pupil, const double* cart, int jmax, int side, double* out,

@@ -1333,6 +1333,7 @@ extern "C" int bt_batch_create(const bt_batch_desc* d, bt_batch** out) {
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_counter, sizeof(int));
     if (e == cudaSuccess) e = bt_batch_set_smem_limit();
     if (e != cudaSuccess) {
+        cudaGetLastError();  // leave no error behind for the next launch check
         batch_free(b);
         return cuda_fail(e, "batch: set-up");
     }
@@ -1409,7 +1410,7 @@ static int batch_args(bt_batch* b, int nstates, const double* xf, const double* 
         return fail(BT_ERR_ARG, "batch: threads must be 32..256, a multiple of 32");
     if (ctas_per_sm < 1) return fail(BT_ERR_ARG, "batch: ctas_per_sm must be >= 1");
     if (niter < 0) return fail(BT_ERR_ARG, "batch: negative niter");
-    if (bt_batch_smem_layout(b->blob_bytes, threads, b->jmax).total > BT_BATCH_MAX_SMEM)
+    if (bt_batch_smem_layout(b->blob_bytes, threads, b->jmax).total > (size_t)bt_batch_smem_max())
         return fail(BT_ERR_UNSUPPORTED, "batch: shared memory exceeds the limit for this block size");
     const int njobs = nstates * nfields;
     if (njobs > 0 && (!nx || !wavelength || !fields || !order || !coefs || !status || !det ||

@@ -43,6 +43,8 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-huygens", action="store_true")
+    p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--batch-states", type=int, default=4096)
     return p.parse_args()
 
 
@@ -247,6 +249,99 @@ def bench_huygens(bt, opt, nx=256, npix=128, pitch=2e-6, wavelength=620e-9, chec
     return out
 
 
+BATCH_FIELDS = [(fx, fy) for fy in (-1.2, 0.0, 1.2) for fx in (-1.2, 0.0, 1.2)]
+
+
+def batch_states(pt, nstates, seed=31337):
+    """Seeded perturbed states: M2 and camera shifts U(+-1 mm) and tilts
+    U(+-10 arcsec), 20 bending amplitudes N(0, 100 nm); pupil grids
+    U{32..128}; wavelengths from the six 350-1000 nm values."""
+    rng = np.random.default_rng(seed)
+    tilt = np.deg2rad(10.0 / 3600.0)
+    rigid = rng.uniform(-1.0, 1.0, (nstates, 10)) * np.tile([1e-3, 1e-3, 1e-3, tilt, tilt], 2)
+    bend = rng.normal(0.0, 100e-9, (nstates, pt.nmodes))
+    nx = rng.integers(32, 129, nstates)
+    wl = np.linspace(350e-9, 1000e-9, 6)[rng.integers(0, 6, nstates)]
+    return np.concatenate([rigid, bend], axis=1), nx, wl
+
+
+def bench_batched(bt, nstates=4096, reps=3, cpu=True):
+    """Batched wavefronts: 4096 perturbed states x 9 fields, Zernike fit
+    (jmax 28, annular) per (state, field), one persistent graph-captured
+    launch per batch.  Device-timed with the states' tables resident; e2e
+    from host dofs through PerturbedTelescope.zernike."""
+    import torch
+    from batoid_gb300 import _device as D, workloads as W
+    from batoid_gb300.autotune import batch_config
+    from batoid_gb300.batch import PerturbedTelescope
+    from batoid_gb300.modes import ModeSet
+    optic = W.tma_optic(bt)
+    modes = ModeSet(nmodes=20, n=512)
+    pt = PerturbedTelescope(optic, modes=modes, fields=np.deg2rad(BATCH_FIELDS), jmax=28)
+    dofs, nx, wl = batch_states(pt, nstates)
+    pt.prepare(np.arange(32, 129))
+    threads, ctas = batch_config(pt)
+    inp = pt.device_inputs(dofs, nx, wl)
+    F, J = len(BATCH_FIELDS), pt.jmax
+    coefs = torch.empty(nstates * F * (J + 1), dtype=torch.float64, device=D.device())
+    status = torch.empty(nstates * F, dtype=torch.int32, device=D.device())
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        pt.launch(inp, coefs, status, threads, ctas, graph=True)   # capture + first replay
+        stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            pt.launch(inp, coefs, status, threads, ctas, graph=True)
+        e1.record(stream)
+        stream.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    st = D.to_host(status)
+    rays = int(np.sum(nx.astype(np.int64) ** 2)) * F
+    stages = pt.prog.nstages + 1
+    jobs = nstates * F
+    # end to end: host dofs -> tables -> device -> kernel -> coefficients on the host
+    t1 = time.perf_counter()
+    host = pt.zernike(dofs, nx, wl, threads=threads, ctas_per_sm=ctas)
+    e2e_s = time.perf_counter() - t1
+    out = {
+        "workload": f"{nstates} states x {F} fields, pupil grids 32-128 (seeded), jmax 28 annular fit, "
+                    "M2/camera rigid dofs + 20 bending modes (512x512 bicubic), tma_corrector",
+        "wavefronts_per_s": jobs / (ms * 1e-3),
+        "ray_surface_per_s": rays * stages / (ms * 1e-3),
+        "ms_per_batch": ms, "rays_per_batch": rays, "jobs": jobs,
+        "launch": {"threads": threads, "ctas_per_sm": ctas, "graph": True, "kernels_per_batch": 1},
+        "failed_fits": int(np.sum(st != 0)),
+        "e2e": {"wavefronts_per_s": jobs / e2e_s, "s_per_batch": e2e_s,
+                "h2d_bytes": int(sum(t.numel() * t.element_size() for k, t in inp.items() if k != "nstates")),
+                "d2h_bytes": int(coefs.numel() * 8 + status.numel() * 4),
+                "path": "PerturbedTelescope.zernike (host tables, copies, launch, copies back)"},
+    }
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import wavefront as owf
+        from batoid_gb300.utils import fieldToDirCos
+        sample = [(s, s % F) for s in range(0, nstates, max(1, nstates // 6))][:6]
+        srays = 0
+        maxdiff = 0.0
+        t1 = time.perf_counter()
+        for s, f in sample:
+            c = owf.zernike(pt.perturbed(dofs[s]), fieldToDirCos(*np.deg2rad(BATCH_FIELDS[f])), wl[s], int(nx[s]),
+                            J, pt.eps)
+            srays += int(nx[s]) ** 2
+            maxdiff = max(maxdiff, float(np.max(np.abs(c - host[s, f])) * wl[s]))
+        dt = time.perf_counter() - t1
+        import oracle as ora
+        out["cpu_baseline"] = {"s_per_ray": dt / srays, "cores": ora.threads(), "kind": "port",
+                               "extrapolated_s_per_batch": dt / srays * rays,
+                               "sample": f"{len(sample)} (state, field) jobs, oracle trace + numpy lstsq "
+                                         "(reference wavefront/zernike algorithm)"}
+        out["speedup_vs_cpu"] = out["cpu_baseline"]["extrapolated_s_per_batch"] / (ms * 1e-3)
+        out["max_coef_diff_m_vs_oracle"] = maxdiff
+    return out
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -347,6 +442,9 @@ def run_gpu(args):
     if rank == 0 and not args.no_huygens:
         del rv_in, rv_out
         huygens = bench_huygens(bt, opt, cpu=not args.no_cpu_baseline)
+    batched = None
+    if rank == 0 and not args.no_batch:
+        batched = bench_batched(bt, nstates=args.batch_states, cpu=not args.no_cpu_baseline)
 
     if rank == 0:
         line = {
@@ -372,6 +470,7 @@ def run_gpu(args):
             "clocks": clk,
             "gpu_launches": args.steps,
             "huygens_psf": huygens,
+            "batched_wavefronts": batched,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
