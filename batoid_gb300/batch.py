@@ -284,8 +284,8 @@ class PerturbedTelescope:
         the job order (largest grids first)."""
         dofs = np.atleast_2d(np.asarray(dofs, dtype=float))
         S = dofs.shape[0]
-        nx = np.broadcast_to(np.asarray(nx, dtype=np.int32), (S,))
-        wl = np.broadcast_to(np.asarray(wavelength, dtype=float), (S,))
+        nx = np.array(np.broadcast_to(np.asarray(nx, dtype=np.int32), (S,)))
+        wl = np.array(np.broadcast_to(np.asarray(wavelength, dtype=float), (S,)))
         xf, det, amps = self.state_tables(dofs)
         F = len(self.fields)
         jobs = np.arange(S * F, dtype=np.int32)
