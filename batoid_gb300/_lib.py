@@ -159,9 +159,19 @@ _SIGS = [
     ("bt_batch_create", c_int, [ctypes.POINTER(BtBatchDesc), _PP]),
     ("bt_batch_destroy", None, [_P]),
     ("bt_batch_prepare", c_int, [_P, c_int, _P, _P]),
-    ("bt_batch_zernike", c_int, [_P, c_int, _P, _P, _P, _P, _P, c_int, _P, _P, _P, _P, c_int, c_int, c_int, _P]),
-    ("bt_batch_zernike_graph", c_int, [_P, c_int, _P, _P, _P, _P, _P, c_int, _P, _P, _P, _P, c_int, c_int, c_int,
-                                       _P]),
+    ("bt_batch_zernike", c_int, [_P, c_int, _P, _P, _P, _P, _P, c_int, _P, _P, c_int, _P, _P, c_int, c_int, c_int,
+                                 _P]),
+    ("bt_batch_zernike_graph", c_int, [_P, c_int, _P, _P, _P, _P, _P, c_int, _P, _P, c_int, _P, _P, c_int, c_int,
+                                       c_int, _P]),
+    ("bt_mlp_gemm", c_int, [_P, _P, c_int, c_int, c_int, c_int, c_int, c_int, _P, _P, _P, _P, _P, _P]),
+    ("bt_mlp_pack", c_int, [_P, c_int, c_int, c_int, c_int, _P, _P, _P]),
+    ("bt_mlp_loss", c_int, [_P, c_int, _P, _P, c_int, c_int, c_int, c_int, ctypes.c_float, c_int, _P, _P, _P, _P]),
+    ("bt_mlp_colsum", c_int, [_P, c_int, c_int, _P, _P]),
+    ("bt_mlp_adam", c_int, [_P, c_int, _P, ctypes.c_longlong, _P, _P, _P, ctypes.c_float, ctypes.c_float,
+                            ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, c_int, c_int, _P, _P,
+                            _P]),
+    ("bt_surrogate_combine", c_int, [_P, c_int, c_int, _P, _P, _P, c_int, _P, c_double, c_int, c_int, _P, _P, c_int,
+                                     _P]),
     ("bt_measure_fp64_peak", c_int, [c_int, c_double_p, _P]),
     ("bt_check_device_status", c_int, [_P]),
 ]

@@ -19,7 +19,7 @@ from . import _device as D
 from . import _lib
 
 DEFAULT = (128, 3)
-CANDIDATES = [(64, 4), (64, 6), (64, 8), (128, 2), (128, 3), (128, 4), (256, 1), (256, 2)]
+CANDIDATES = [(64, 4), (64, 6), (128, 2), (128, 3), (128, 4)]
 _memo = {}
 
 

@@ -297,14 +297,16 @@ class PerturbedTelescope:
                  order=torch.from_numpy(order).to(D.device()), nstates=S)
         return t
 
-    def launch(self, inp, coefs, status, threads=128, ctas_per_sm=3, niter=None, graph=False):
-        """Stream-ordered launch on device inputs from ``device_inputs``."""
+    def launch(self, inp, coefs, status, threads=128, ctas_per_sm=3, niter=None, graph=False, order=None):
+        """Stream-ordered launch on device inputs from ``device_inputs``;
+        ``order`` (device int32 job ids) runs only those jobs."""
         from .global_vars import _batoid_niter
         plan = self.plan()
         fn = _lib.lib().bt_batch_zernike_graph if graph else _lib.lib().bt_batch_zernike
+        order = inp["order"] if order is None else order
         _lib.check(fn(plan.ptr, inp["nstates"], D.ptr(inp["xf"]), D.ptr(inp["det"]), D.ptr(inp["amps"]),
                       inp["nx"].data_ptr(), D.ptr(inp["wl"]), len(self.fields), D.ptr(self._d_fields),
-                      inp["order"].data_ptr(), coefs.data_ptr(), status.data_ptr(), int(threads),
+                      order.data_ptr(), int(order.numel()), coefs.data_ptr(), status.data_ptr(), int(threads),
                       int(ctas_per_sm), int(_batoid_niter if niter is None else niter), D.stream_ptr()))
 
     def zernike(self, dofs, nx, wavelength, threads=None, ctas_per_sm=None, errors='raise'):

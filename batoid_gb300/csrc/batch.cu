@@ -145,7 +145,7 @@ __device__ __forceinline__ void bt_tri_index(int e, int* a, int* b) {
     *b = bb;
 }
 
-__global__ void __launch_bounds__(BT_BATCH_MAX_THREADS)
+__global__ void __launch_bounds__(BT_BATCH_MAX_THREADS, BT_BATCH_MIN_BLOCKS)
 k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const __grid_constant__ BatchArgs A) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar;
@@ -179,7 +179,7 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
         if (tid == 0) s_q = atomicAdd(A.counter, 1);
         __syncthreads();
         const int q = s_q;
-        if (q >= A.njobs) break;
+        if (q >= A.nqueue) break;
         const int job = A.order[q];
         const int s = job / A.nfields, f = job - s * A.nfields;
         const int nx = A.nxs[s];
@@ -404,14 +404,14 @@ int bt_batch_smem_max() { return g_batch_smem_max; }
 
 cudaError_t bt_launch_batch_zernike(const unsigned char* d_blob, int blob_bytes, const BatchArgs& a, int threads,
                                     int ctas_per_sm, cudaStream_t stream) {
-    if (a.njobs <= 0) return cudaSuccess;
+    if (a.nqueue <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(int), stream);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(a.status, 0xff, sizeof(int) * (size_t)a.njobs, stream);
     if (e != cudaSuccess) return e;
     const size_t smem = bt_batch_smem_layout(blob_bytes, threads, a.jmax).total;
     long long grid = (long long)bt_sm_count() * ctas_per_sm;
-    if (grid > a.njobs) grid = a.njobs;
+    if (grid > a.nqueue) grid = a.nqueue;
     if (grid < 1) grid = 1;
     k_batch_zernike<<<(int)grid, threads, smem, stream>>>(d_blob, blob_bytes, a);
     return cudaGetLastError();

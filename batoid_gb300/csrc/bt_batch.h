@@ -4,7 +4,9 @@
 #include <stdint.h>
 #include <cuda_runtime.h>
 
-#define BT_BATCH_MAX_THREADS 256
+#define BT_BATCH_MAX_THREADS 128
+// resident blocks per SM the register budget is sized for (168 registers)
+#define BT_BATCH_MIN_BLOCKS 3
 #define BT_BATCH_MAX_J 32
 #define BT_BATCH_MAX_VAR 8
 #define BT_BATCH_MAX_NX 512
@@ -34,7 +36,8 @@ struct BatchArgs {
     int* counter;       // queue head, zeroed before each launch
     double* coefs;      // [njobs][jmax + 1]
     int* status;        // [njobs]
-    int njobs;
+    int njobs;          // nstates * nfields (status / coefs extent)
+    int nqueue;         // entries of order to run
     int nfields;
     int nx_cap;
     // plan

@@ -10,6 +10,7 @@
 #include "../../include/batoid_gb300.h"
 #include "bt_internal.h"
 #include "bt_batch.h"
+#include "bt_mlp.h"
 
 // ---------------------------------------------------------------------------
 // errors
@@ -1152,10 +1153,105 @@ extern "C" int bt_measure_fp64_peak(int iters, double* tflops, void* stream) {
 // Test hook: reads and clears the device status word of the trace kernels
 // (BT_ERR_TIMEOUT if a bounded wait expired).  Synchronous.
 extern "C" int bt_check_device_status(void* stream) {
-    int st = 0, sb = 0;
+    int st = 0, sb = 0, sm = 0;
     CUDA_TRY(bt_read_device_status(&st, (cudaStream_t)stream), "device status");
     CUDA_TRY(bt_read_batch_device_status(&sb, (cudaStream_t)stream), "device status");
-    if (st != 0 || sb != 0) return fail(st != 0 ? st : sb, "a kernel's bounded wait expired");
+    CUDA_TRY(bt_read_mlp_device_status(&sm, (cudaStream_t)stream), "device status");
+    const int any = st ? st : (sb ? sb : sm);
+    if (any != 0) return fail(any, "a kernel's bounded wait expired");
+    return BT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Surrogate MLP building blocks
+// ---------------------------------------------------------------------------
+
+extern "C" int bt_mlp_gemm(const void* A, const void* B, int M, int N, int K, int bn, int splitk, int mode,
+                           const float* bias, float* out32, float* zs, void* h16, void* h16t, void* stream) {
+    if (!A || !B) return fail(BT_ERR_ARG, "mlp gemm: null operand");
+    if (M <= 0 || N <= 0 || K <= 0 || M % 128 || (bn != 128 && bn != 256) || N % bn || splitk < 1 ||
+        K % (64 * splitk))
+        return fail(BT_ERR_ARG, "mlp gemm: M % 128, N % bn (128 or 256) and K % (64 * splitk) must be 0");
+    if (((uintptr_t)A & 15) || ((uintptr_t)B & 15)) return fail(BT_ERR_ARG, "mlp gemm: operands must be 16-byte aligned");
+    switch (mode) {
+    case MLP_EPI_F32:
+        if (!out32) return fail(BT_ERR_ARG, "mlp gemm: mode 0 needs out32");
+        break;
+    case MLP_EPI_BIAS:
+        if (!out32 || !bias || splitk != 1) return fail(BT_ERR_ARG, "mlp gemm: mode 1 needs out32, bias, splitk 1");
+        break;
+    case MLP_EPI_GELU:
+        if (!h16 || !bias || splitk != 1) return fail(BT_ERR_ARG, "mlp gemm: mode 2 needs h16, bias, splitk 1");
+        break;
+    case MLP_EPI_DGELU:
+        if (!h16 || !zs || splitk != 1) return fail(BT_ERR_ARG, "mlp gemm: mode 3 needs h16, zs, splitk 1");
+        break;
+    default:
+        return fail(BT_ERR_ARG, "mlp gemm: bad mode");
+    }
+    MlpGemmArgs a;
+    memset(&a, 0, sizeof(a));
+    a.M = M;
+    a.N = N;
+    a.K = K;
+    a.bn = bn;
+    a.mode = mode;
+    a.bias = bias;
+    a.out32 = out32;
+    a.zs = zs;
+    a.h16 = (__nv_bfloat16*)h16;
+    a.h16t = (__nv_bfloat16*)h16t;
+    CUDA_TRY(bt_launch_mlp_gemm((const __nv_bfloat16*)A, (const __nv_bfloat16*)B, a, splitk, (cudaStream_t)stream),
+             "mlp gemm");
+    return BT_OK;
+}
+
+extern "C" int bt_mlp_pack(const float* x, int rows, int cols, int ld_out, int rows_out, void* out, void* out_t,
+                           void* stream) {
+    if (!x || !out || rows < 0 || cols < 0 || rows_out < rows || ld_out < cols)
+        return fail(BT_ERR_ARG, "mlp pack: bad arguments");
+    if (rows_out == 0) return BT_OK;
+    CUDA_TRY(bt_launch_mlp_pack(x, rows, cols, ld_out, rows_out, (__nv_bfloat16*)out, (__nv_bfloat16*)out_t,
+                                (cudaStream_t)stream), "mlp pack");
+    return BT_OK;
+}
+
+extern "C" int bt_mlp_loss(const float* y, int ldy, const float* t, const float* wt, int rows, int rows_valid,
+                           int ncols, int err_col, float err_weight, int ld_out, void* dz, void* dzt, float* loss,
+                           void* stream) {
+    if (!y || !t || !dz || !dzt || rows_valid < 1 || rows_valid > rows || ncols > ld_out || ncols > ldy ||
+        err_col >= ld_out || err_col >= ldy)
+        return fail(BT_ERR_ARG, "mlp loss: bad arguments");
+    CUDA_TRY(bt_launch_mlp_loss(y, ldy, t, wt, rows, rows_valid, ncols, err_col, err_weight, ld_out,
+                                (__nv_bfloat16*)dz, (__nv_bfloat16*)dzt, loss, (cudaStream_t)stream), "mlp loss");
+    return BT_OK;
+}
+
+extern "C" int bt_mlp_colsum(const void* xt, int rows, int cols, float* out, void* stream) {
+    if (!xt || !out || rows < 1 || cols < 1) return fail(BT_ERR_ARG, "mlp colsum: bad arguments");
+    CUDA_TRY(bt_launch_mlp_colsum((const __nv_bfloat16*)xt, rows, cols, out, (cudaStream_t)stream), "mlp colsum");
+    return BT_OK;
+}
+
+extern "C" int bt_surrogate_combine(const float* feat, int nfeat, int nlin, const int* grp, const double* theta,
+                                    const float* y, int ldy, const double* wl, double scale, int J, int err_col,
+                                    double* out, float* err_nm, int n, void* stream) {
+    if (n < 0 || (n > 0 && (!feat || !grp || !theta || !y || !wl || !out)) || nlin > nfeat || J < 1 || J > ldy ||
+        err_col >= ldy)
+        return fail(BT_ERR_ARG, "surrogate combine: bad arguments");
+    CUDA_TRY(bt_launch_surrogate_combine(feat, nfeat, nlin, grp, theta, y, ldy, wl, scale, J, err_col, out, err_nm, n,
+                                         (cudaStream_t)stream), "surrogate combine");
+    return BT_OK;
+}
+
+extern "C" int bt_mlp_adam(const float* partials, int nsplit, const float* grad, long long n, float* w, float* m,
+                           float* v, float lr, float b1, float b2, float eps, float bc1, float bc2, int rows, int cols,
+                           void* w16, void* w16t, void* stream) {
+    if (!w || !m || !v || n < 1 || (nsplit > 0 && !partials) || (long long)rows * cols != n || !(bc1 > 0.f) ||
+        !(bc2 > 0.f))
+        return fail(BT_ERR_ARG, "mlp adam: bad arguments");
+    CUDA_TRY(bt_launch_mlp_adam(partials, nsplit, grad, n, w, m, v, lr, b1, b2, eps, bc1, bc2, rows, cols,
+                                (__nv_bfloat16*)w16, (__nv_bfloat16*)w16t, (cudaStream_t)stream), "mlp adam");
     return BT_OK;
 }
 
@@ -1402,12 +1498,13 @@ extern "C" int bt_batch_prepare(bt_batch* b, int n, const int* nx_values, void* 
 
 static int batch_args(bt_batch* b, int nstates, const double* xf, const double* det, const double* amps,
                       const int* nx, const double* wavelength, int nfields, const double* fields, const int* order,
-                      double* coefs, int* status, int threads, int ctas_per_sm, int niter, BatchArgs* a) {
+                      int nqueue, double* coefs, int* status, int threads, int ctas_per_sm, int niter,
+                      BatchArgs* a) {
     if (!b) return fail(BT_ERR_ARG, "batch: null plan");
     if (nstates < 0 || nfields < 0) return fail(BT_ERR_ARG, "batch: negative sizes");
     if ((long long)nstates * nfields > 0x7fffffffLL) return fail(BT_ERR_UNSUPPORTED, "batch: too many jobs");
     if (threads < 32 || threads > BT_BATCH_MAX_THREADS || threads % 32 != 0)
-        return fail(BT_ERR_ARG, "batch: threads must be 32..256, a multiple of 32");
+        return fail(BT_ERR_ARG, "batch: threads must be 32..128, a multiple of 32");
     if (ctas_per_sm < 1) return fail(BT_ERR_ARG, "batch: ctas_per_sm must be >= 1");
     if (niter < 0) return fail(BT_ERR_ARG, "batch: negative niter");
     if (bt_batch_smem_layout(b->blob_bytes, threads, b->jmax).total > (size_t)bt_batch_smem_max())
@@ -1432,6 +1529,7 @@ static int batch_args(bt_batch* b, int nstates, const double* xf, const double* 
     a->coefs = coefs;
     a->status = status;
     a->njobs = njobs;
+    a->nqueue = (nqueue <= 0 || nqueue > njobs) ? njobs : nqueue;
     a->nfields = nfields;
     a->nx_cap = BT_BATCH_MAX_NX;
     a->nvar = b->nvar;
@@ -1452,11 +1550,11 @@ static int batch_args(bt_batch* b, int nstates, const double* xf, const double* 
 
 extern "C" int bt_batch_zernike(bt_batch* b, int nstates, const double* xf, const double* det, const double* amps,
                                 const int* nx, const double* wavelength, int nfields, const double* fields,
-                                const int* order, double* coefs, int* status, int threads, int ctas_per_sm,
-                                int niter, void* stream) {
+                                const int* order, int nqueue, double* coefs, int* status, int threads,
+                                int ctas_per_sm, int niter, void* stream) {
     BatchArgs a;
-    int rc = batch_args(b, nstates, xf, det, amps, nx, wavelength, nfields, fields, order, coefs, status, threads,
-                        ctas_per_sm, niter, &a);
+    int rc = batch_args(b, nstates, xf, det, amps, nx, wavelength, nfields, fields, order, nqueue, coefs, status,
+                        threads, ctas_per_sm, niter, &a);
     if (rc != BT_OK) return rc;
     std::lock_guard<std::mutex> lock(b->mu);
     CUDA_TRY(bt_launch_batch_zernike(b->d_blob, b->blob_bytes, a, threads, ctas_per_sm, (cudaStream_t)stream),
@@ -1466,12 +1564,12 @@ extern "C" int bt_batch_zernike(bt_batch* b, int nstates, const double* xf, cons
 
 extern "C" int bt_batch_zernike_graph(bt_batch* b, int nstates, const double* xf, const double* det,
                                       const double* amps, const int* nx, const double* wavelength, int nfields,
-                                      const double* fields, const int* order, double* coefs, int* status,
-                                      int threads, int ctas_per_sm, int niter, void* stream) {
+                                      const double* fields, const int* order, int nqueue, double* coefs,
+                                      int* status, int threads, int ctas_per_sm, int niter, void* stream) {
     if (!stream) return fail(BT_ERR_ARG, "batch graph: the legacy default stream cannot be captured");
     BatchArgs a;
-    int rc = batch_args(b, nstates, xf, det, amps, nx, wavelength, nfields, fields, order, coefs, status, threads,
-                        ctas_per_sm, niter, &a);
+    int rc = batch_args(b, nstates, xf, det, amps, nx, wavelength, nfields, fields, order, nqueue, coefs, status,
+                        threads, ctas_per_sm, niter, &a);
     if (rc != BT_OK) return rc;
     if (a.njobs == 0) return BT_OK;
     cudaStream_t s = (cudaStream_t)stream;

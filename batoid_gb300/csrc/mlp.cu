@@ -1,0 +1,524 @@
+// BF16 GEMMs of the wavefront surrogate MLP on the 5th-generation tensor
+// cores (tcgen05), FP32 accumulation in tensor memory, with fused epilogues.
+//
+//   C[M x N] = A[M x K] . B[N x K]^T      (both operands K-major, bf16)
+//
+// One CTA computes a 128 x BN tile (BN = 128 or 256) over a K range:
+//   * warp 0 / lane 0 streams 128 x 64 and BN x 64 operand tiles from global
+//     memory with TMA (cp.async.bulk.tensor, 128-byte swizzle) into a
+//     4-stage shared-memory ring (full / empty mbarriers);
+//   * warp 1 / lane 0 issues tcgen05.mma (M 128, N BN, K 16) from shared
+//     memory descriptors into a TMEM accumulator of BN columns and releases
+//     each stage with tcgen05.commit;
+//   * all four warps read the accumulator back with tcgen05.ld (warp w owns
+//     TMEM lanes 32w..32w+31 = tile rows) and run the epilogue.
+// Every wait is bounded: on expiry the CTA records BT_ERR_TIMEOUT in the
+// device status word, stops issuing, waits (bounded) for the copies and
+// MMAs it started, frees its TMEM and returns.
+//
+// Epilogues (per element (m, n) of the tile):
+//   F32      out32[kz][m][n] = acc                       (split-K partials)
+//   BIAS     out32[m][n]     = acc + bias[n]             (output layer)
+//   GELU     z = acc + bias[n]; zs[m][n] = z;  h = gelu(z);
+//            h16[m][n] = h16T[n][m] = bf16(h)             (hidden layers)
+//   DGELU    g = acc * gelu'(zs[m][n]);
+//            h16[m][n] = h16T[n][m] = bf16(g)             (backward)
+#include <cuda_runtime.h>
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include "bt_internal.h"
+#include "bt_stage_smem.cuh"
+#include "bt_mlp.h"
+
+#define MLP_BM 128
+#define MLP_BK 64
+#define MLP_STAGES 4
+#define MLP_THREADS 128
+
+cudaError_t bt_read_mlp_device_status(int* status, cudaStream_t stream) {
+    int zero = 0;
+    cudaError_t e = cudaMemcpyFromSymbolAsync(status, bt_dev_status, sizeof(int), 0, cudaMemcpyDeviceToHost, stream);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return e;
+    if (*status != 0) {
+        e = cudaMemcpyToSymbolAsync(bt_dev_status, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
+        if (e != cudaSuccess) return e;
+        e = cudaStreamSynchronize(stream);
+    }
+    return e;
+}
+
+// ---------------------------------------------------------------------------
+// PTX wrappers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bt_smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bt_smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Bounded parity wait; false when the limit expired or another role aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort) {
+    for (uint32_t i = 0; i < BT_WAIT_LIMIT; i++) {
+        if (bt_mbar_try_wait(bar, parity)) return true;
+        if ((i & 1023u) == 1023u && *abort) return false;
+    }
+    *abort = 1;
+    atomicExch(&bt_dev_status, 5 /* BT_ERR_TIMEOUT */);
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(bt_smem_addr(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(bt_smem_addr(bar))
+        : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows of
+// 128 bytes in 8-row (1024-byte) atoms.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);   // start address
+    d |= (uint64_t)1 << 16;                      // leading byte offset (unused here)
+    d |= (uint64_t)(1024 >> 4) << 32;            // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                      // descriptor version
+    d |= (uint64_t)2 << 61;                      // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor of kind::f16: D f32, A and B bf16, both K-major.
+__device__ __forceinline__ uint32_t mma_idesc(int bn) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(MLP_BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(tmem), "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 ::"r"(bt_smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// GELU (erf form) and its derivative.
+__device__ __forceinline__ float gelu_f(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float dgelu_f(float z) {
+    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * __expf(-0.5f * z * z);
+}
+
+// ---------------------------------------------------------------------------
+// The GEMM kernel
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(MLP_THREADS, 1)
+k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, MlpGemmArgs g) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full[MLP_STAGES];
+    __shared__ __align__(8) uint64_t empty[MLP_STAGES];
+    __shared__ __align__(8) uint64_t done;
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_abort;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int BN = g.bn;
+    // operand ring, 1024-byte aligned for the swizzle atoms
+    const uint32_t raw = bt_smem_addr(smem_raw);
+    unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+    const uint32_t a_bytes = MLP_BM * MLP_BK * 2, b_bytes = (uint32_t)BN * MLP_BK * 2;
+    unsigned char* sA = base;
+    unsigned char* sB = base + MLP_STAGES * a_bytes;
+    const int m0 = blockIdx.x * MLP_BM, n0 = blockIdx.y * BN;
+    const int kz = blockIdx.z;
+    const int kbeg = kz * g.kchunk;
+    const int nk = g.kchunk / MLP_BK;
+    volatile int* abort = &s_abort;
+
+    if (tid == 0) {
+        for (int s = 0; s < MLP_STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(&done, 1);
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(bt_smem_addr(&s_tmem)), "r"((uint32_t)BN) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s_tmem;
+
+    if (warp == 0 && lane == 0) {
+        // producer
+        int issued = 0;
+        for (int kb = 0; kb < nk; kb++) {
+            const int s = kb % MLP_STAGES;
+            if (kb >= MLP_STAGES && !mbar_wait(&empty[s], ((kb / MLP_STAGES) - 1) & 1, abort)) break;
+            if (*abort) break;
+            mbar_expect_tx(&full[s], a_bytes + b_bytes);
+            tma_load_2d(sA + s * a_bytes, &tmA, kbeg + kb * MLP_BK, m0, &full[s]);
+            tma_load_2d(sB + s * b_bytes, &tmB, kbeg + kb * MLP_BK, n0, &full[s]);
+            issued = kb + 1;
+        }
+        // copies still in flight complete before the CTA may exit
+        for (int kb = (issued > MLP_STAGES ? issued - MLP_STAGES : 0); kb < issued; kb++) {
+            for (uint32_t i = 0; i < BT_WAIT_LIMIT; i++)
+                if (bt_mbar_try_wait(&full[kb % MLP_STAGES], (kb / MLP_STAGES) & 1)) break;
+        }
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        const uint32_t idesc = mma_idesc(BN);
+        for (int kb = 0; kb < nk; kb++) {
+            const int s = kb % MLP_STAGES;
+            if (!mbar_wait(&full[s], (kb / MLP_STAGES) & 1, abort)) break;
+            tc_fence_after();
+            const uint32_t a0 = bt_smem_addr(sA + s * a_bytes), b0 = bt_smem_addr(sB + s * b_bytes);
+#pragma unroll
+            for (int k = 0; k < MLP_BK / 16; k++)
+                mma_bf16(tmem, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), idesc, (kb > 0 || k > 0) ? 1u : 0u);
+            mma_commit(&empty[s]);
+        }
+        // completes once every MMA issued above has finished
+        mma_commit(&done);
+    }
+    __syncwarp();
+    // epilogue: all threads; the decision to store is uniform over the CTA
+    mbar_wait(&done, 0, abort);
+    __syncthreads();
+    const bool ok = !*abort;
+    tc_fence_after();
+    if (ok) {
+        const int row = warp * 32 + lane;
+        const int m = m0 + row;
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int c = 0; c < BN; c += 32) {
+            float v[32];
+            tmem_ld32(trow + (uint32_t)c, v);
+            const int nb = n0 + c;
+            if (g.mode == MLP_EPI_F32) {
+                float* o = g.out32 + (size_t)kz * g.M * g.N + (size_t)m * g.N + nb;
+#pragma unroll
+                for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(o + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+            } else if (g.mode == MLP_EPI_BIAS) {
+                float* o = g.out32 + (size_t)m * g.N + nb;
+#pragma unroll
+                for (int i = 0; i < 32; i += 4)
+                    *reinterpret_cast<float4*>(o + i) = make_float4(v[i] + g.bias[nb + i], v[i + 1] + g.bias[nb + i + 1],
+                                                                    v[i + 2] + g.bias[nb + i + 2], v[i + 3] + g.bias[nb + i + 3]);
+            } else {
+                float h[32];
+                if (g.mode == MLP_EPI_GELU) {
+                    float* zs = g.zs + (size_t)m * g.N + nb;
+#pragma unroll
+                    for (int i = 0; i < 32; i++) {
+                        const float z = v[i] + g.bias[nb + i];
+                        v[i] = z;
+                        h[i] = gelu_f(z);
+                    }
+                    if (zs) {
+#pragma unroll
+                        for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(zs + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                    }
+                } else {  // MLP_EPI_DGELU
+                    const float* zs = g.zs + (size_t)m * g.N + nb;
+#pragma unroll
+                    for (int i = 0; i < 32; i++) h[i] = v[i] * dgelu_f(zs[i]);
+                }
+                __nv_bfloat16* o = g.h16 + (size_t)m * g.N + nb;
+#pragma unroll
+                for (int i = 0; i < 32; i += 8) {
+                    __align__(16) __nv_bfloat162 p[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) p[q] = __floats2bfloat162_rn(h[i + 2 * q], h[i + 2 * q + 1]);
+                    *reinterpret_cast<uint4*>(o + i) = *reinterpret_cast<uint4*>(p);
+                }
+                if (g.h16t) {
+#pragma unroll
+                    for (int i = 0; i < 32; i++) g.h16t[(size_t)(nb + i) * g.M + m] = __float2bfloat16_rn(h[i]);
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN) : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side: tensor maps and launch
+// ---------------------------------------------------------------------------
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+// Row-major bf16 matrix [rows][cols] viewed as (cols, rows) with a box of
+// 64 x box_rows elements and 128-byte swizzle.
+static bool make_map(CUtensorMap* map, const void* ptr, int rows, int cols, int box_rows) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+    cuuint32_t box[2] = {MLP_BK, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+size_t bt_mlp_gemm_smem(int bn) {
+    return 1024 + (size_t)MLP_STAGES * (MLP_BM * MLP_BK * 2 + (size_t)bn * MLP_BK * 2);
+}
+
+cudaError_t bt_launch_mlp_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, const MlpGemmArgs& a, int splitk,
+                               cudaStream_t stream) {
+    if (a.M % MLP_BM || (a.bn != 128 && a.bn != 256) || a.N % a.bn || splitk < 1 || a.K % (splitk * MLP_BK))
+        return cudaErrorInvalidValue;
+    if (((uintptr_t)A & 15) || ((uintptr_t)B & 15)) return cudaErrorInvalidValue;
+    CUtensorMap ta, tb;
+    if (!make_map(&ta, A, a.M, a.K, MLP_BM) || !make_map(&tb, B, a.N, a.K, a.bn)) return cudaErrorInvalidValue;
+    MlpGemmArgs g = a;
+    g.kchunk = a.K / splitk;
+    const size_t smem = bt_mlp_gemm_smem(a.bn);
+    static int attr_set = 0;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_mlp_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)bt_mlp_gemm_smem(256));
+        if (e != cudaSuccess) return e;
+        attr_set = 1;
+    }
+    dim3 grid(a.M / MLP_BM, a.N / a.bn, splitk);
+    k_mlp_gemm<<<grid, MLP_THREADS, smem, stream>>>(ta, tb, g);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Training and inference helpers
+// ---------------------------------------------------------------------------
+
+// FP32 features [rows][cols] -> bf16 [rows_out][ld_out] and its transpose,
+// zero-padded.
+__global__ void k_mlp_pack(const float* __restrict__ x, int rows, int cols, int ld_out, int rows_out,
+                           __nv_bfloat16* __restrict__ out, __nv_bfloat16* __restrict__ out_t) {
+    const long long n = (long long)rows_out * ld_out;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(e / ld_out), c = (int)(e - (long long)r * ld_out);
+        const float v = (r < rows && c < cols) ? x[(size_t)r * cols + c] : 0.f;
+        const __nv_bfloat16 b = __float2bfloat16_rn(v);
+        out[e] = b;
+        if (out_t) out_t[(size_t)c * rows_out + r] = b;
+    }
+}
+
+// Gradient of the weighted mean-squared error of columns [0, ncols) and of
+// the error head (column err_col, which predicts the log of the row's
+// residual norm sqrt(sum_j r_j^2), a detached target).  One thread per row.
+__global__ void k_mlp_loss(const float* __restrict__ y, int ldy, const float* __restrict__ t,
+                           const float* __restrict__ wt, int rows, int rows_valid, int ncols, int err_col,
+                           float err_weight, int ld_out, __nv_bfloat16* __restrict__ dz,
+                           __nv_bfloat16* __restrict__ dzt, float* loss) {
+    __shared__ float s_main[256], s_err[256];
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    float lm = 0.f, le = 0.f;
+    if (m < rows) {
+        const bool valid = m < rows_valid;
+        const float scale = 2.0f / (float)rows_valid;
+        float ss = 0.f;
+        for (int j = 0; j < ld_out; j++) {
+            float g = 0.f;
+            if (valid && j < ncols) {
+                const float r = y[(size_t)m * ldy + j] - t[(size_t)m * ncols + j];
+                const float w = wt ? wt[j] : 1.0f;
+                ss += r * r;
+                lm += w * r * r;
+                g = scale * w * r;
+            }
+            if (j != err_col || !valid) {
+                dz[(size_t)m * ld_out + j] = __float2bfloat16_rn(g);
+                dzt[(size_t)j * rows + m] = __float2bfloat16_rn(g);
+            }
+        }
+        if (err_col >= 0) {
+            float g = 0.f;
+            if (valid) {
+                const float target = 0.5f * __logf(ss + 1e-12f);
+                const float r = y[(size_t)m * ldy + err_col] - target;
+                le = r * r;
+                g = scale * err_weight * r;
+            }
+            dz[(size_t)m * ld_out + err_col] = __float2bfloat16_rn(g);
+            dzt[(size_t)err_col * rows + m] = __float2bfloat16_rn(g);
+        }
+    }
+    s_main[threadIdx.x] = lm;
+    s_err[threadIdx.x] = le;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            s_main[threadIdx.x] += s_main[threadIdx.x + o];
+            s_err[threadIdx.x] += s_err[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && loss) {
+        atomicAdd(loss, s_main[0] / (float)rows_valid);
+        atomicAdd(loss + 1, s_err[0] / (float)rows_valid);
+    }
+}
+
+// out[r] = sum_c xt[r][c]: one block per row.
+__global__ void k_mlp_colsum(const __nv_bfloat16* __restrict__ xt, int cols, float* __restrict__ out) {
+    __shared__ float s[256];
+    const __nv_bfloat16* row = xt + (size_t)blockIdx.x * cols;
+    float acc = 0.f;
+    for (int c = threadIdx.x; c < cols; c += blockDim.x) acc += __bfloat162float(row[c]);
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = s[0];
+}
+
+// Adam step on FP32 master weights from the sum of split-K partial gradients
+// (or a direct gradient), then the bf16 copies used by the GEMMs:
+// w16 [rows][cols] and, if given, w16t [cols][rows].
+__global__ void k_mlp_adam(const float* __restrict__ partials, int nsplit, const float* __restrict__ gdir,
+                           long long n, float* __restrict__ w, float* __restrict__ m, float* __restrict__ v, float lr,
+                           float b1, float b2, float eps, float bc1, float bc2, int rows, int cols,
+                           __nv_bfloat16* __restrict__ w16, __nv_bfloat16* __restrict__ w16t) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float g = gdir ? gdir[i] : 0.f;
+        for (int s = 0; s < nsplit; s++) g += partials[(size_t)s * n + i];
+        const float mi = b1 * m[i] + (1.f - b1) * g;
+        const float vi = b2 * v[i] + (1.f - b2) * g * g;
+        m[i] = mi;
+        v[i] = vi;
+        const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+        w[i] = wi;
+        if (w16) {
+            const __nv_bfloat16 b = __float2bfloat16_rn(wi);
+            w16[i] = b;
+            if (w16t) {
+                const int r = (int)(i / cols), c = (int)(i - (long long)r * cols);
+                w16t[(size_t)c * rows + r] = b;
+            }
+        }
+    }
+}
+
+static int mlp_grid(long long n) {
+    long long b = (n + 255) / 256;
+    long long cap = (long long)bt_sm_count() * 8;
+    return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+cudaError_t bt_launch_mlp_pack(const float* x, int rows, int cols, int ld_out, int rows_out, __nv_bfloat16* out,
+                               __nv_bfloat16* out_t, cudaStream_t stream) {
+    k_mlp_pack<<<mlp_grid((long long)rows_out * ld_out), 256, 0, stream>>>(x, rows, cols, ld_out, rows_out, out, out_t);
+    return cudaGetLastError();
+}
+
+cudaError_t bt_launch_mlp_loss(const float* y, int ldy, const float* t, const float* wt, int rows, int rows_valid,
+                               int ncols, int err_col, float err_weight, int ld_out, __nv_bfloat16* dz,
+                               __nv_bfloat16* dzt, float* loss, cudaStream_t stream) {
+    k_mlp_loss<<<(rows + 255) / 256, 256, 0, stream>>>(y, ldy, t, wt, rows, rows_valid, ncols, err_col, err_weight,
+                                                       ld_out, dz, dzt, loss);
+    return cudaGetLastError();
+}
+
+cudaError_t bt_launch_mlp_colsum(const __nv_bfloat16* xt, int rows, int cols, float* out, cudaStream_t stream) {
+    k_mlp_colsum<<<rows, 256, 0, stream>>>(xt, cols, out);
+    return cudaGetLastError();
+}
+
+cudaError_t bt_launch_mlp_adam(const float* partials, int nsplit, const float* grad_direct, long long n, float* w,
+                               float* m, float* v, float lr, float b1, float b2, float eps, float bc1, float bc2,
+                               int rows, int cols, __nv_bfloat16* w16, __nv_bfloat16* w16t, cudaStream_t stream) {
+    k_mlp_adam<<<mlp_grid(n), 256, 0, stream>>>(partials, nsplit, grad_direct, n, w, m, v, lr, b1, b2, eps, bc1, bc2,
+                                                rows, cols, w16, w16t);
+    return cudaGetLastError();
+}
+
+// Surrogate output: per sample n (group g = grp[n]),
+//   lin_j = theta[g][0][j] + sum_k theta[g][1 + k][j] * feat[n][k]   (k < nlin)
+//   out[n][0] = 0, out[n][1 + j] = lin_j + y[n][j] * scale / (wl[n] * 1e9)   (waves)
+//   err_nm[n] = scale * exp(y[n][err_col])
+// FP64 for the linear part, which carries most of the signal.
+__global__ void k_surrogate_combine(const float* __restrict__ feat, int nfeat, int nlin, const int* __restrict__ grp,
+                                    const double* __restrict__ theta, const float* __restrict__ y, int ldy,
+                                    const double* __restrict__ wl, double scale, int J, int err_col,
+                                    double* __restrict__ out, float* __restrict__ err_nm, int n) {
+    const long long total = (long long)n * J;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int s = (int)(e / J), j = (int)(e - (long long)s * J);
+        const double* th = theta + (size_t)grp[s] * (nlin + 1) * J;
+        double acc = th[j];
+        const float* f = feat + (size_t)s * nfeat;
+        for (int k = 0; k < nlin; k++) acc += th[(size_t)(k + 1) * J + j] * (double)f[k];
+        out[(size_t)s * (J + 1) + 1 + j] = acc + (double)y[(size_t)s * ldy + j] * scale / (wl[s] * 1e9);
+        if (j == 0) {
+            out[(size_t)s * (J + 1)] = 0.0;
+            if (err_nm) err_nm[s] = (float)(scale * exp((double)y[(size_t)s * ldy + err_col]));
+        }
+    }
+}
+
+cudaError_t bt_launch_surrogate_combine(const float* feat, int nfeat, int nlin, const int* grp, const double* theta,
+                                        const float* y, int ldy, const double* wl, double scale, int J, int err_col,
+                                        double* out, float* err_nm, int n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    k_surrogate_combine<<<mlp_grid((long long)n * J), 256, 0, stream>>>(feat, nfeat, nlin, grp, theta, y, ldy, wl,
+                                                                         scale, J, err_col, out, err_nm, n);
+    return cudaGetLastError();
+}

@@ -4,6 +4,7 @@
 // (batoid/optic.py:1013-1083): instead of reading and writing all 74 bytes
 // per ray once per surface, each ray is loaded once and stored once.
 #include <cuda_runtime.h>
+#include <stdlib.h>
 #include "bt_internal.h"
 #include "bt_device.cuh"
 #include "bt_stage_smem.cuh"
@@ -25,8 +26,13 @@ cudaError_t bt_read_device_status(int* status, cudaStream_t stream) {
 }
 
 #define TRACE_THREADS 128
+#define BT_TRACE_MINB_DEFAULT 4
 
-__global__ void __launch_bounds__(TRACE_THREADS)
+// MINB = resident blocks per SM the register budget is sized for: 4 gives
+// 128 registers (16 warps per SM, a few spills), 1 gives the compiler's
+// choice (154 registers, no spills, 12 warps per SM).
+template <int MINB>
+__global__ void __launch_bounds__(TRACE_THREADS, MINB)
 k_trace(const unsigned char* __restrict__ gblob, int blob_bytes, RV in, RV out,
         const __grid_constant__ SnapSet snaps, int nsnaps, int niter) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -82,14 +88,21 @@ cudaError_t bt_launch_trace(const unsigned char* d_blob, int blob_bytes, const R
     if (in.n <= 0) return cudaSuccess;
     static SnapSet empty;
     const SnapSet& ss = snaps ? *snaps : empty;
+    // register budget variant; BATOID_GB300_TRACE_MINB=1 or 4 overrides
+    static int minb = 0;
+    if (minb == 0) {
+        const char* env = getenv("BATOID_GB300_TRACE_MINB");
+        minb = (env && atoi(env) == 1) ? 1 : (env && atoi(env) == 4) ? 4 : BT_TRACE_MINB_DEFAULT;
+    }
+    auto kern = (minb == 1) ? k_trace<1> : k_trace<4>;
     if (blob_bytes > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_trace, cudaFuncAttributeMaxDynamicSharedMemorySize, blob_bytes);
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, blob_bytes);
         if (e != cudaSuccess) return e;
     }
     // Persistent grid: the blob is staged once per block and amortised over
     // the grid-stride loop.
     const int grid = grid_for(in.n, TRACE_THREADS, 16);
-    k_trace<<<grid, TRACE_THREADS, blob_bytes, stream>>>(d_blob, blob_bytes, in, out, ss, nsnaps, niter);
+    kern<<<grid, TRACE_THREADS, blob_bytes, stream>>>(d_blob, blob_bytes, in, out, ss, nsnaps, niter);
     return cudaGetLastError();
 }
 

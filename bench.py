@@ -45,6 +45,9 @@ def parse():
     p.add_argument("--no-huygens", action="store_true")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--batch-states", type=int, default=4096)
+    p.add_argument("--no-surrogate", action="store_true")
+    p.add_argument("--surrogate-samples", type=int, default=2_000_000)
+    p.add_argument("--surrogate-epochs", type=int, default=24)
     return p.parse_args()
 
 
@@ -342,6 +345,128 @@ def bench_batched(bt, nstates=4096, reps=3, cpu=True):
     return out
 
 
+def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24, threshold_nm=2.0, cpu=True):
+    """Learned surrogate: MLP 33 -> 4 x 512 GELU -> 28 (+ error head), BF16
+    tensor-core kernels with FP32 accumulation, trained on batched-trace
+    data (nx 32 pupil grids, 9 fields, 6 wavelengths); evaluated on held-out
+    states against the batched trace, with fallback to the trace above
+    threshold_nm of calibrated predicted RMS wavefront error."""
+    import torch
+    from batoid_gb300 import _device as D, workloads as W
+    from batoid_gb300.autotune import batch_config
+    from batoid_gb300.batch import PerturbedTelescope
+    from batoid_gb300.modes import ModeSet
+    from batoid_gb300.surrogate import WavefrontSurrogate, rms_nm
+    optic = W.tma_optic(bt)
+    pt = PerturbedTelescope(optic, modes=ModeSet(nmodes=20, n=512), fields=np.deg2rad(BATCH_FIELDS), jmax=28)
+    sur = WavefrontSurrogate(pt, W.WAVELENGTHS, nx=32)
+    pt.prepare([32])
+    threads, ctas = batch_config(pt)
+    F = len(BATCH_FIELDS)
+    t1 = time.perf_counter()
+    dofs, widx = sur.sample_states((train_samples + F - 1) // F, seed=101)
+    coefs = sur.trace(dofs, widx, threads=threads, ctas_per_sm=ctas)
+    datagen_s = time.perf_counter() - t1
+    feat, grp, w = sur.features(dofs, widx)
+    t1 = time.perf_counter()
+    sur.train(feat, grp, w, coefs, epochs=epochs, batch=8192, lr=1e-3)
+    train_s = time.perf_counter() - t1
+    steps = epochs * (len(feat) // 8192)
+    vd, vw = sur.sample_states(4096, seed=202)
+    vc = sur.trace(vd, vw, threads=threads, ctas_per_sm=ctas)
+    vf, vg, vwl = sur.features(vd, vw)
+    kappa = sur.calibrate(vf, vg, vwl, vc)
+    # held-out: the batched trace (device-resident inputs, graph replay) is the judge and the baseline
+    hd, hw = sur.sample_states(heldout_states, seed=303)
+    inp = pt.device_inputs(hd, 32, W.WAVELENGTHS[hw])
+    N = heldout_states * F
+    tc = torch.empty(N * 29, dtype=torch.float64, device=D.device())
+    ts = torch.empty(N, dtype=torch.int32, device=D.device())
+    stream = torch.cuda.Stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        pt.launch(inp, tc, ts, threads, ctas, graph=True)
+        stream.synchronize()
+        e0.record(stream)
+        for _ in range(3):
+            pt.launch(inp, tc, ts, threads, ctas, graph=True)
+        e1.record(stream)
+        stream.synchronize()
+    trace_ms = e0.elapsed_time(e1) / 3
+    truth = D.to_host(tc).reshape(N, 29)
+    hf, hg, hwl = sur.features(hd, hw)
+    feat_d = torch.from_numpy(hf).to(D.device())
+    grp_d = torch.from_numpy(hg).to(D.device())
+    w_d = D.to_device(hwl)
+    out = torch.empty((N, 29), dtype=torch.float64, device=D.device())
+    err = torch.empty(N, dtype=torch.float32, device=D.device())
+    with torch.cuda.stream(stream):
+        sur.predict_device(feat_d, grp_d, w_d, out, err)
+        stream.synchronize()
+        e0.record(stream)
+        for _ in range(10):
+            sur.predict_device(feat_d, grp_d, w_d, out, err)
+        e1.record(stream)
+        stream.synchronize()
+    infer_ms = e0.elapsed_time(e1) / 10
+    pred = D.to_host(out)
+    perr = D.to_host(err) * kappa
+    fb = perr > threshold_nm
+    jobs = np.flatnonzero(fb)
+    fb_ms = 0.0
+    if len(jobs):
+        order = torch.from_numpy(jobs.astype(np.int32)).to(D.device())
+        fc = torch.empty(N * 29, dtype=torch.float64, device=D.device())
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            pt.launch(inp, fc, ts, threads, ctas, order=order)
+            e1.record(stream)
+            stream.synchronize()
+        fb_ms = e0.elapsed_time(e1)
+        pred[fb] = D.to_host(fc).reshape(N, 29)[fb]
+    lin = np.concatenate([np.zeros((N, 1)), sur.linear(hf, hg)], axis=1)
+    e_lin = rms_nm(lin, truth, hwl)
+    raw, _ = sur.predict(hf, hg, hwl)
+    e_raw = rms_nm(raw, truth, hwl)
+    e_fin = rms_nm(pred, truth, hwl)
+
+    def stats(e):
+        return {"mean_nm": float(np.mean(e)), "p50_nm": float(np.median(e)), "p99_nm": float(np.quantile(e, 0.99)),
+                "max_nm": float(np.max(e)), "frac_above_threshold": float(np.mean(e > threshold_nm))}
+
+    flops_fwd = 2.0 * (33 * 512 + 3 * 512 * 512 + 512 * 28)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        pass
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    infer_tflops = flops_fwd * N / (infer_ms * 1e-3) / 1e12
+    out_d = {
+        "workload": f"MLP 33 -> 4x512 GELU -> 28 + error head, bf16/fp32-accumulate tcgen05 kernels; trained on "
+                    f"{len(feat)} (state, field) samples of the 4096-state generator (nx 32), evaluated on "
+                    f"{N} held-out samples vs the batched trace",
+        "wavefronts_per_s_with_fallback": N / ((infer_ms + fb_ms) * 1e-3),
+        "wavefronts_per_s_surrogate_only": N / (infer_ms * 1e-3),
+        "wavefronts_per_s_batched_trace": N / (trace_ms * 1e-3),
+        "speedup_vs_batched_trace": trace_ms / (infer_ms + fb_ms),
+        "fallback_fraction": float(np.mean(fb)), "threshold_nm": threshold_nm, "error_calibration_kappa": kappa,
+        "rms_error_with_fallback": stats(e_fin), "rms_error_surrogate_only": stats(e_raw),
+        "rms_error_linear_model_only": stats(e_lin),
+        "ms": {"inference": infer_ms, "fallback_trace": fb_ms, "batched_trace": trace_ms, "datagen_s": datagen_s,
+               "train_s": train_s},
+        "training": {"steps": steps, "batch": 8192, "epochs": epochs,
+                     "samples_per_s": steps * 8192 / train_s},
+        "roofline_inference": {"bound": "tensor", "achieved": infer_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
+                               "frac": infer_tflops / bf16_peak, "flops_per_sample": flops_fwd,
+                               "note": "whole inference pipeline (pack, 5 GEMMs, combine) over its event time"},
+        "gpu_launches_per_inference": 7,
+    }
+    return out_d
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -445,6 +570,9 @@ def run_gpu(args):
     batched = None
     if rank == 0 and not args.no_batch:
         batched = bench_batched(bt, nstates=args.batch_states, cpu=not args.no_cpu_baseline)
+    surrogate = None
+    if rank == 0 and not args.no_surrogate:
+        surrogate = bench_surrogate(bt, train_samples=args.surrogate_samples, epochs=args.surrogate_epochs)
 
     if rank == 0:
         line = {
@@ -471,6 +599,7 @@ def run_gpu(args):
             "gpu_launches": args.steps,
             "huygens_psf": huygens,
             "batched_wavefronts": batched,
+            "surrogate": surrogate,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -307,22 +307,70 @@ int bt_batch_prepare(bt_batch* b, int n, const int* nx_values, void* stream);
  * stage), det[s][12] (origin(3), rot(9) row-major of the last stage's
  * frame), amps[s][nmodes], nx[s], wavelength[s]; per field f: fields[f][18]
  * (back-propagation frame dr(3), rot(9), local velocity(3), velocity(3) as
- * batoid's finishParallel takes them); order[njobs] = job ids s*nfields+f in
- * scheduling order.  Outputs coefs[job][jmax+1] (waves, entry 0 = 0) and
- * status[job] (0, BT_ERR_ARG for a grid size not prepared, BT_ERR_RANK,
- * -1 if never processed).  threads: 32..256, a multiple of 32; ctas_per_sm
- * >= 1.  Stream-ordered. */
+ * batoid's finishParallel takes them); order[nqueue] = the job ids
+ * s*nfields+f to run, in scheduling order (nqueue <= 0: all nstates*nfields
+ * jobs, order holding each once).  Outputs coefs[job][jmax+1] (waves, entry
+ * 0 = 0) and status[job] (0, BT_ERR_ARG for a grid size not prepared,
+ * BT_ERR_RANK, -1 if not run).  threads: 32..128, a multiple of 32;
+ * ctas_per_sm >= 1.  Stream-ordered. */
 int bt_batch_zernike(bt_batch* b, int nstates, const double* xf, const double* det, const double* amps,
                      const int* nx, const double* wavelength, int nfields, const double* fields,
-                     const int* order, double* coefs, int* status, int threads, int ctas_per_sm, int niter,
-                     void* stream);
+                     const int* order, int nqueue, double* coefs, int* status, int threads, int ctas_per_sm,
+                     int niter, void* stream);
 /* Same, replayed from a CUDA graph captured on the first call with these
  * arguments (recaptured when they change).  stream must not be the legacy
  * default stream. */
 int bt_batch_zernike_graph(bt_batch* b, int nstates, const double* xf, const double* det, const double* amps,
                            const int* nx, const double* wavelength, int nfields, const double* fields,
-                           const int* order, double* coefs, int* status, int threads, int ctas_per_sm,
-                           int niter, void* stream);
+                           const int* order, int nqueue, double* coefs, int* status, int threads,
+                           int ctas_per_sm, int niter, void* stream);
+
+/* ---- Wavefront surrogate MLP (BF16 tensor cores) -------------------------
+ * No counterpart in the reference.  Building blocks of the training and
+ * inference of the surrogate network that maps perturbation dofs, field
+ * and wavelength to Zernike coefficients; all pointers are device pointers,
+ * bf16 arrays are 16-byte aligned row-major, all calls stream-ordered.
+ *
+ * C[M x N] = A[M x K] . B[N x K]^T with A, B bf16 (K contiguous), FP32
+ * accumulation in tensor memory (tcgen05.mma), fused epilogue `mode`:
+ *   0: out32[kz][m][n] = partial sum of K-split kz (splitk splits)
+ *   1: out32[m][n] = acc + bias[n]
+ *   2: zs[m][n] = acc + bias[n] (zs may be null); h16[m][n] = h16t[n][m] =
+ *      bf16(gelu(zs)) (h16t may be null)
+ *   3: h16[m][n] = h16t[n][m] = bf16(acc * gelu'(zs[m][n]))
+ * M a multiple of 128; bn 128 or 256 dividing N; K a multiple of 64*splitk. */
+int bt_mlp_gemm(const void* A, const void* B, int M, int N, int K, int bn, int splitk, int mode, const float* bias,
+                float* out32, float* zs, void* h16, void* h16t, void* stream);
+/* FP32 features x[rows][cols] -> bf16 out[rows_out][ld_out] (zero padded)
+ * and its transpose out_t[ld_out][rows_out] (may be null). */
+int bt_mlp_pack(const float* x, int rows, int cols, int ld_out, int rows_out, void* out, void* out_t, void* stream);
+/* Gradient of the mean (over rows_valid rows) of sum_j wt[j] (y - t)^2 over
+ * columns j < ncols, and of the squared error of column err_col (if >= 0)
+ * against the detached target log sqrt(sum_j (y - t)^2), weighted by
+ * err_weight; written as bf16 dz[rows][ld_out] and dzt[ld_out][rows].
+ * loss[0], loss[1] (may be null) accumulate the two terms. */
+int bt_mlp_loss(const float* y, int ldy, const float* t, const float* wt, int rows, int rows_valid, int ncols,
+                int err_col, float err_weight, int ld_out, void* dz, void* dzt, float* loss, void* stream);
+/* out[r] = sum_c xt[r][c] of a bf16 [rows][cols] array (bias gradients). */
+int bt_mlp_colsum(const void* xt, int rows, int cols, float* out, void* stream);
+/* One Adam step of n FP32 parameters w (moments m, v; bias corrections
+ * bc1 = 1 - b1^t, bc2 = 1 - b2^t) with gradient grad (may be null) plus the
+ * sum of nsplit partial gradients (partials, [nsplit][n], may be null);
+ * refreshes the bf16 copies w16 [rows][cols] and w16t [cols][rows] (either
+ * may be null). */
+int bt_mlp_adam(const float* partials, int nsplit, const float* grad, long long n, float* w, float* m, float* v,
+                float lr, float b1, float b2, float eps, float bc1, float bc2, int rows, int cols, void* w16,
+                void* w16t, void* stream);
+
+/* Surrogate output assembly: for sample s in group grp[s], Zernike
+ * coefficients out[s][0..J] (waves; entry 0 = 0) = linear model
+ * theta[grp][0][j] + sum_k theta[grp][1+k][j] feat[s][k] (k < nlin; theta
+ * is [groups][nlin+1][J] FP64) plus the network's residual y[s][j] (nm
+ * divided by `scale`) converted to waves at wl[s]; err_nm[s] (may be null)
+ * = scale * exp(y[s][err_col]), the predicted residual norm in nm. */
+int bt_surrogate_combine(const float* feat, int nfeat, int nlin, const int* grp, const double* theta, const float* y,
+                         int ldy, const double* wl, double scale, int J, int err_col, double* out, float* err_nm,
+                         int n, void* stream);
 
 /* Measures the device's FP64 FMA throughput (TFLOP/s, 2 flops per FMA)
  * with independent DFMA chains; `iters` FMAs per chain (e.g. 1 << 14).

@@ -63,7 +63,7 @@ def test_batch_matches_oracle(pt):
 def test_batch_large_grid_and_vignetting_edge(pt):
     dofs = _dofs(pt, 1, 5)
     nx, wl = np.array([128]), np.array([700e-9])
-    got = pt.zernike(dofs, nx, wl, threads=256, ctas_per_sm=1)
+    got = pt.zernike(dofs, nx, wl, threads=128, ctas_per_sm=3)
     want = _oracle(pt, dofs, nx, wl)
     assert (np.abs(got - want) * wl[:, None, None]).max() <= TOL_M
 
@@ -97,7 +97,7 @@ def test_launch_shapes_agree_and_graph_replay_is_exact(pt):
 
     a = run(128, 3, False)
     b = run(64, 6, False)
-    c = run(256, 1, False)
+    c = run(64, 4, False)
     np.testing.assert_allclose(b, a, rtol=0, atol=1e-9)
     np.testing.assert_allclose(c, a, rtol=0, atol=1e-9)
     s = torch.cuda.Stream()

@@ -1,0 +1,66 @@
+"""Learned wavefront surrogate, end to end on a small problem: data from the
+batched tracer, linear sensitivity model, MLP trained by the tensor-core
+kernels, error-head calibration and the trace fallback."""
+import numpy as np
+import pytest
+
+import batoid_gb300 as bt
+from batoid_gb300 import workloads
+from batoid_gb300.batch import PerturbedTelescope
+from batoid_gb300.modes import ModeSet
+from batoid_gb300.surrogate import WavefrontSurrogate, rms_nm
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def trained():
+    modes = ModeSet(nmodes=8, n=128, seed=5)
+    optic = workloads.tma_optic(bt)
+    fields = np.deg2rad([[0.0, 0.0], [0.8, -0.5], [-1.0, 0.9]])
+    pt = PerturbedTelescope(optic, modes=modes, fields=fields)
+    sur = WavefrontSurrogate(pt, wavelengths=[500e-9, 800e-9], nx=24, hidden=256, layers=2, seed=1)
+    dofs, widx = sur.sample_states(6000, seed=1)
+    coefs = sur.trace(dofs, widx, threads=128, ctas_per_sm=3)
+    feat, grp, w = sur.features(dofs, widx)
+    losses = []
+    sur.train(feat, grp, w, coefs, epochs=40, batch=2048, lr=2e-3, log=lambda e, a, b: losses.append(a))
+    vd, vw = sur.sample_states(600, seed=2)
+    vc = sur.trace(vd, vw, threads=128, ctas_per_sm=3)
+    vf, vg, vwl = sur.features(vd, vw)
+    sur.calibrate(vf, vg, vwl, vc)
+    return sur, losses
+
+
+def test_training_converges(trained):
+    sur, losses = trained
+    assert losses[-1] < 0.2 * losses[0]
+
+
+def test_network_improves_on_linear_model(trained):
+    sur, _ = trained
+    d, wi = sur.sample_states(600, seed=3)
+    truth = sur.trace(d, wi, threads=128, ctas_per_sm=3).reshape(-1, sur.J + 1)
+    feat, grp, w = sur.features(d, wi)
+    lin = np.concatenate([np.zeros((len(feat), 1)), sur.linear(feat, grp)], axis=1)
+    pred, _ = sur.predict(feat, grp, w)
+    e_lin = rms_nm(lin, truth, w)
+    e_net = rms_nm(pred, truth, w)
+    print(f"held-out RMS wavefront error: linear {np.mean(e_lin):.3f} nm, linear + MLP {np.mean(e_net):.3f} nm")
+    assert np.mean(e_net) < 0.7 * np.mean(e_lin)
+
+
+def test_fallback_rows_are_the_trace(trained):
+    sur, _ = trained
+    d, wi = sur.sample_states(200, seed=4)
+    truth = sur.trace(d, wi, threads=128, ctas_per_sm=3)
+    feat, grp, w = sur.features(d, wi)
+    _, err = sur.predict(feat, grp, w)
+    thr = float(np.median(sur.kappa * err))  # about half the samples fall back
+    out, fb = sur.with_fallback(d, wi, threshold_nm=thr, threads=128, ctas_per_sm=3)
+    assert 0 < fb.sum() < fb.size
+    np.testing.assert_array_equal(out[fb], truth[fb])
+    acc = ~fb.ravel()
+    e = rms_nm(out.reshape(-1, sur.J + 1)[acc], truth.reshape(-1, sur.J + 1)[acc], w[acc])
+    # the calibrated estimate bounds most accepted errors
+    assert np.mean(e <= thr) > 0.9
