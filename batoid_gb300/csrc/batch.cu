@@ -145,6 +145,71 @@ __device__ __forceinline__ void bt_tri_index(int e, int* a, int* b) {
     *b = bb;
 }
 
+// gw += sign * z z^T on the packed lower triangle, lanes striding over the
+// entries (one vignetting mismatch; out of line, it is rare).
+__device__ __noinline__ void bt_gram_update(double* gw, const double* zv, double sign, int lane, int NT) {
+    int a, b;
+    bt_tri_index(lane, &a, &b);
+    for (int e = lane; e < NT; e += 32) {
+        gw[e] += sign * (zv[a] * zv[b]);
+        b += 32;
+        while (b > a) {
+            b -= a + 1;
+            a++;
+        }
+    }
+}
+
+// Cholesky G = L L^T in place (lower triangle; lanes = rows) and the two
+// triangular solves of G c = bv by one warp.  Writes out[0] = 0 and
+// out[1..J], or NaN and the rank status when a pivot falls below
+// BT_BATCH_PIVOT_TOL of the largest diagonal entry.
+__device__ __noinline__ void bt_chol_solve(double* G, const double* bv, int J, int lane, double* out, int* status) {
+    double maxd = 0.0;
+    for (int j = 0; j < J; j++) maxd = fmax(maxd, G[j * J + j]);
+    const double tol = maxd * BT_BATCH_PIVOT_TOL;
+    bool ok = true;
+    for (int k = 0; k < J; k++) {
+        __syncwarp();
+        const double dkk = G[k * J + k];
+        if (!(dkk > tol)) {
+            ok = false;
+            break;
+        }
+        const double l = sqrt(dkk);
+        __syncwarp();
+        if (lane > k && lane < J) G[lane * J + k] /= l;
+        __syncwarp();
+        if (lane == k) G[k * J + k] = l;
+        if (lane > k && lane < J) {
+            const double lik = G[lane * J + k];
+            for (int j = k + 1; j <= lane; j++) G[lane * J + j] -= lik * G[j * J + k];
+        }
+    }
+    __syncwarp();
+    if (ok) {
+        double x = (lane < J) ? bv[lane] : 0.0;
+        for (int k = 0; k < J; k++) {
+            const double yk = __shfl_sync(0xffffffffu, x, k) / G[k * J + k];
+            if (lane == k) x = yk;
+            else if (lane > k && lane < J) x -= G[lane * J + k] * yk;
+        }
+        for (int k = J - 1; k >= 0; k--) {
+            const double ck = __shfl_sync(0xffffffffu, x, k) / G[k * J + k];
+            if (lane == k) x = ck;
+            else if (lane < k) x -= G[k * J + lane] * ck;
+        }
+        if (lane < J) out[1 + lane] = x;
+        if (lane == 0) {
+            out[0] = 0.0;
+            *status = 0;
+        }
+    } else {
+        for (int j = lane; j <= J; j += 32) out[j] = NAN;
+        if (lane == 0) *status = BT_BATCH_RANK;
+    }
+}
+
 __global__ void __launch_bounds__(BT_BATCH_MAX_THREADS, BT_BATCH_MIN_BLOCKS)
 k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const __grid_constant__ BatchArgs A) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -159,7 +224,7 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
     double* pool = reinterpret_cast<double*>(smem + hdr->off_pool);
     BatchSmem L = bt_batch_smem_layout(blob_bytes, T, J);
     double* mc = reinterpret_cast<double*>(smem + L.mc);
-    double* bacc = reinterpret_cast<double*>(smem + L.bacc);
+    double* bsum = reinterpret_cast<double*>(smem + L.bacc);  // [nwarps][32]
     double* gcorr = reinterpret_cast<double*>(smem + L.gcorr);
     double* zv = reinterpret_cast<double*>(smem + L.zv) + warp * 32;
     double* G = reinterpret_cast<double*>(smem + L.G);
@@ -209,7 +274,7 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
             }
         }
         mcell[tid] = -1;
-        for (int j = 0; j < J; j++) bacc[j * T + tid] = 0.0;
+        double bj = 0.0;  // lane j < J: this warp's share of (B^T v)_j
         for (int e = lane; e < NT; e += 32) gw[e] = 0.0;
         __syncthreads();
 
@@ -241,12 +306,20 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
                 continue;
             }
             bool valid = false, inref = false;
+            double opd = 0.0;
             if (active) {
                 valid = !r.vig;
                 inref = bt_in_annulus(gx, gy, A.r_in2, A.r_out2);
-                if (valid) {
-                    const double opd = (s_t0 - r.t) / wl;
-                    for (int j = 0; j < J; j++) bacc[j * T + tid] += __ldg(Z + (size_t)j * nray + i) * opd;
+                if (valid) opd = (s_t0 - r.t) / wl;
+            }
+            // B^T v: lane j accumulates sum_k Z_j(ray k) opd_k over the warp's
+            // 32 rays (a row of the basis table per lane, contiguous in k)
+            {
+                const int wbase = base + warp * 32;
+                const double* zrow = Z + (size_t)(lane < J ? lane : 0) * nray;
+                for (int k = 0; k < 32; k++) {
+                    const double ok = __shfl_sync(0xffffffffu, opd, k);
+                    if (lane < J && ok != 0.0) bj += __ldg(zrow + wbase + k) * ok;
                 }
             }
             unsigned mm = __ballot_sync(0xffffffffu, valid != inref);
@@ -258,25 +331,16 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
                 __syncwarp();
                 if (lane < J) zv[lane] = __ldg(Z + (size_t)lane * nray + pi);
                 __syncwarp();
-                int a, b;
-                bt_tri_index(lane, &a, &b);
-                for (int e = lane; e < NT; e += 32) {
-                    gw[e] += sign * (zv[a] * zv[b]);
-                    b += 32;
-                    while (b > a) {
-                        b -= a + 1;
-                        a++;
-                    }
-                }
+                bt_gram_update(gw, zv, sign, lane, NT);
             }
         }
+        bsum[warp * 32 + lane] = bj;
         __syncthreads();
         // B^T v
-        for (int j = warp; j < J; j += nwarps) {
+        for (int j = tid; j < J; j += T) {
             double acc = 0.0;
-            for (int t = lane; t < T; t += 32) acc += bacc[j * T + t];
-            acc = bt_warp_sum(acc);
-            if (lane == 0) bv[j] = acc;
+            for (int w = 0; w < nwarps; w++) acc += bsum[w * 32 + j];
+            bv[j] = acc;
         }
         // B^T B
         const double* GR = A.gref + (size_t)nx * J * J;
@@ -289,53 +353,7 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
             G[b * J + a] = v;
         }
         __syncthreads();
-        if (warp == 0) {
-            // Cholesky G = L L^T in place (lower triangle), lanes = rows
-            double maxd = 0.0;
-            for (int j = 0; j < J; j++) maxd = fmax(maxd, G[j * J + j]);
-            const double tol = maxd * BT_BATCH_PIVOT_TOL;
-            bool ok = true;
-            for (int k = 0; k < J; k++) {
-                __syncwarp();
-                const double dkk = G[k * J + k];
-                if (!(dkk > tol)) {
-                    ok = false;
-                    break;
-                }
-                const double l = sqrt(dkk);
-                __syncwarp();
-                if (lane > k && lane < J) G[lane * J + k] /= l;
-                __syncwarp();
-                if (lane == k) G[k * J + k] = l;
-                if (lane > k && lane < J) {
-                    const double lik = G[lane * J + k];
-                    for (int j = k + 1; j <= lane; j++) G[lane * J + j] -= lik * G[j * J + k];
-                }
-            }
-            __syncwarp();
-            double* out = A.coefs + (size_t)job * (J + 1);
-            if (ok) {
-                double x = (lane < J) ? bv[lane] : 0.0;
-                for (int k = 0; k < J; k++) {
-                    const double yk = __shfl_sync(0xffffffffu, x, k) / G[k * J + k];
-                    if (lane == k) x = yk;
-                    else if (lane > k && lane < J) x -= G[lane * J + k] * yk;
-                }
-                for (int k = J - 1; k >= 0; k--) {
-                    const double ck = __shfl_sync(0xffffffffu, x, k) / G[k * J + k];
-                    if (lane == k) x = ck;
-                    else if (lane < k) x -= G[k * J + lane] * ck;
-                }
-                if (lane < J) out[1 + lane] = x;
-                if (lane == 0) {
-                    out[0] = 0.0;
-                    A.status[job] = 0;
-                }
-            } else {
-                for (int j = lane; j <= J; j += 32) out[j] = NAN;
-                if (lane == 0) A.status[job] = BT_BATCH_RANK;
-            }
-        }
+        if (warp == 0) bt_chol_solve(G, bv, J, lane, A.coefs + (size_t)job * (J + 1), A.status + job);
     }
 }
 

@@ -5,8 +5,8 @@
 #include <cuda_runtime.h>
 
 #define BT_BATCH_MAX_THREADS 128
-// resident blocks per SM the register budget is sized for (168 registers)
-#define BT_BATCH_MIN_BLOCKS 3
+// resident blocks per SM the register budget is sized for (128 registers)
+#define BT_BATCH_MIN_BLOCKS 4
 #define BT_BATCH_MAX_J 32
 #define BT_BATCH_MAX_VAR 8
 #define BT_BATCH_MAX_NX 512
@@ -65,8 +65,8 @@ __host__ __device__ inline BatchSmem bt_batch_smem_layout(int blob_bytes, int T,
     size_t off = ((size_t)blob_bytes + 127) & ~(size_t)127;
     L.mc = off;
     off += (size_t)16 * T * sizeof(double);
-    L.bacc = off;
-    off += (size_t)J * T * sizeof(double);
+    L.bacc = off;  // per-warp partial sums of B^T v
+    off += (size_t)(T / 32) * 32 * sizeof(double);
     L.gcorr = off;
     off += (size_t)(T / 32) * (J * (J + 1) / 2) * sizeof(double);
     L.zv = off;

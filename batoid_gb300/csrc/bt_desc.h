@@ -46,7 +46,8 @@ enum bt_surf_kind {
 //  SUM:        n=#children m=index of first child (children are contiguous)
 //  MODAL:      sum_m a_m * table_m of nmodes bicubic tables on one grid, the
 //              amplitudes a_m supplied per job by the batched kernel:
-//              p0=x0 p1=y0 p2=dx p3=dy p4=use_nan p5=nmodes (multiple of 4);
+//              p0=x0 p1=y0 p2=dx p3=dy p4=use_nan p5=nmodes (multiple of 4)
+//              p6=1/dx p7=1/dy;
 //              n=nx m=ny; off = pool index of the nmodes amplitudes, stored
 //              as float-float pairs; tab = FP32 mode data laid out
 //              [iy][ix][q][mode] with q = z, dz/dx, dz/dy, d2z/dxdy.

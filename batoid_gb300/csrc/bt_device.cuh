@@ -286,23 +286,37 @@ __device__ __forceinline__ ff ff_mulf(ff a, float b) {
     return ff{p, e};
 }
 
-__device__ __forceinline__ bool bt_modal_locate(const Prog& P, const bt_surf& s, double x, double y,
-                                                double* xfrac, double* yfrac) {
-    int ix, iy;
-    if (!bt_table_cell(s, x, y, &ix, &iy, xfrac, yfrac)) return false;
+// Cell lookup with the reciprocal grid steps p[6] = 1/dx, p[7] = 1/dy
+// (no division).  Where rounding moves a point across a cell edge the
+// neighbouring patch gives the same value and slope to rounding: Hermite
+// patches are C1 across edges.
+__device__ __forceinline__ bool bt_modal_cell(const bt_surf& s, double x, double y, int* ix, int* iy,
+                                              double* xfrac, double* yfrac) {
+    const double x0 = s.p[0], y0 = s.p[1], dx = s.p[2], dy = s.p[3];
+    const double fx = floor((x - x0) * s.p[6]);
+    const double fy = floor((y - y0) * s.p[7]);
+    if (!(fx >= 0.0) || !(fy >= 0.0) || fx >= (double)(s.n - 1) || fy >= (double)(s.m - 1)) return false;
+    *ix = (int)fx;
+    *iy = (int)fy;
+    *xfrac = (x - (x0 + *ix * dx)) * s.p[6];
+    *yfrac = (y - (y0 + *iy * dy)) * s.p[7];
+    return true;
+}
+
+// Weighted corner values of cell (ix, iy) into the per-thread cache; out of
+// line: it runs once per ray and cell, the Newton iterations that use the
+// cache are the hot path.
+static __device__ __noinline__ void bt_modal_fill(const double* pool, const bt_surf* sp, int ix, int iy, double* mc,
+                                           float* mcf, int st) {
+    const bt_surf& s = *sp;
     const int nx = s.n;
-    const int cell = iy * nx + ix;
-    if (*P.mcell == cell) return true;
-    const int st = P.mstride;
     const int nq = (int)s.p[5] / 4;  // float4 groups per quantity
-    const ff* a = ff_ptr(P.pool, s.off);
+    const ff* a = ff_ptr(pool, s.off);
     const float4* T = reinterpret_cast<const float4*>(s.tab);
     const size_t node0 = (size_t)nx * iy + ix;
-#pragma unroll
     for (int c = 0; c < 4; c++) {
         const size_t node = node0 + (c & 1) + ((c >> 1) ? (size_t)nx : 0);
         const float4* v = T + node * (size_t)(4 * nq);
-#pragma unroll
         for (int q = 0; q < 4; q++) {
             ff acc{0.f, 0.f};
             for (int k = 0; k < nq; k++) {
@@ -312,10 +326,19 @@ __device__ __forceinline__ bool bt_modal_locate(const Prog& P, const bt_surf& s,
                 acc = ff_add(acc, ff_mulf(a[4 * k + 2], w.z));
                 acc = ff_add(acc, ff_mulf(a[4 * k + 3], w.w));
             }
-            P.mc[(q * 4 + c) * st] = ff_to_double(acc);
-            P.mcf[(q * 4 + c) * st] = acc.hi + acc.lo;
+            mc[(q * 4 + c) * st] = ff_to_double(acc);
+            mcf[(q * 4 + c) * st] = acc.hi + acc.lo;
         }
     }
+}
+
+__device__ __forceinline__ bool bt_modal_locate(const Prog& P, const bt_surf& s, double x, double y,
+                                                double* xfrac, double* yfrac) {
+    int ix, iy;
+    if (!bt_modal_cell(s, x, y, &ix, &iy, xfrac, yfrac)) return false;
+    const int cell = iy * s.n + ix;
+    if (*P.mcell == cell) return true;
+    bt_modal_fill(P.pool, &s, ix, iy, P.mc, P.mcf, P.mstride);
     *P.mcell = cell;
     return true;
 }

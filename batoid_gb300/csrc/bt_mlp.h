@@ -16,6 +16,7 @@ struct MlpGemmArgs {
     int M, N, K;        // C[M x N] = A[M x K] . B[N x K]^T
     int bn;             // tile width, 128 or 256
     int kchunk;         // K per split (set by the launcher)
+    int stages;         // operand ring depth (set by the launcher)
     int mode;
     const float* bias;  // [N]
     float* out32;       // F32: [splitk][M][N]; BIAS: [M][N]

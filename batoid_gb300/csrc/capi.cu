@@ -1313,7 +1313,8 @@ extern "C" int bt_batch_create(const bt_batch_desc* d, bt_batch** out) {
     const bool modal = d->modal_stage >= 0;
     if (modal) {
         if ((size_t)d->modal_stage >= d->nstages) return fail(BT_ERR_ARG, "batch: modal stage out of range");
-        if (d->nmodes < 4 || d->nmodes % 4 != 0 || !d->modes || d->modal_nx < 2 || d->modal_ny < 2)
+        if (d->nmodes < 4 || d->nmodes % 4 != 0 || !d->modes || d->modal_nx < 2 || d->modal_ny < 2 ||
+            !(d->modal_grid[2] > 0.0) || !(d->modal_grid[3] > 0.0))
             return fail(BT_ERR_ARG, "batch: modal tables (nmodes a positive multiple of 4, grid >= 2x2)");
         if (((uintptr_t)d->modes & 15) != 0) return fail(BT_ERR_ARG, "batch: mode data must be 16-byte aligned");
     }
@@ -1345,6 +1346,8 @@ extern "C" int bt_batch_create(const bt_batch_desc* d, bt_batch** out) {
             for (int i = 0; i < 4; i++) m.p[i] = d->modal_grid[i];
             m.p[4] = d->modal_use_nan ? 1.0 : 0.0;
             m.p[5] = (double)d->nmodes;
+            m.p[6] = 1.0 / d->modal_grid[2];
+            m.p[7] = 1.0 / d->modal_grid[3];
             m.off = (int32_t)pb.pool.size();
             m.tab = reinterpret_cast<const double*>(d->modes);
             pb.pool.insert(pb.pool.end(), (size_t)d->nmodes, 0.0);  // amplitudes, per job

@@ -10,8 +10,11 @@
 //   * warp 1 / lane 0 issues tcgen05.mma (M 128, N BN, K 16) from shared
 //     memory descriptors into a TMEM accumulator of BN columns and releases
 //     each stage with tcgen05.commit;
-//   * all four warps read the accumulator back with tcgen05.ld (warp w owns
-//     TMEM lanes 32w..32w+31 = tile rows) and run the epilogue.
+//   * all eight warps read the accumulator back with tcgen05.ld (warp w
+//     owns TMEM lanes 32(w%4)..32(w%4)+31 = tile rows, and half w/4 of the
+//     columns) and run the epilogue.
+// The ring has 2 stages at BN 256 and 3 at BN 128 (97 KB), so two CTAs share
+// an SM and one's epilogue overlaps the other's MMAs.
 // Every wait is bounded: on expiry the CTA records BT_ERR_TIMEOUT in the
 // device status word, stops issuing, waits (bounded) for the copies and
 // MMAs it started, frees its TMEM and returns.
@@ -34,7 +37,7 @@
 #define MLP_BM 128
 #define MLP_BK 64
 #define MLP_STAGES 4
-#define MLP_THREADS 128
+#define MLP_THREADS 256
 
 cudaError_t bt_read_mlp_device_status(int* status, cudaStream_t stream) {
     int zero = 0;
@@ -140,7 +143,7 @@ __device__ __forceinline__ float dgelu_f(float z) {
 // The GEMM kernel
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(MLP_THREADS, 1)
+__global__ void __launch_bounds__(MLP_THREADS, 2)
 k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, MlpGemmArgs g) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t full[MLP_STAGES];
@@ -150,12 +153,13 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     __shared__ int s_abort;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int BN = g.bn;
+    const int NS = g.stages;
     // operand ring, 1024-byte aligned for the swizzle atoms
     const uint32_t raw = bt_smem_addr(smem_raw);
     unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
     const uint32_t a_bytes = MLP_BM * MLP_BK * 2, b_bytes = (uint32_t)BN * MLP_BK * 2;
     unsigned char* sA = base;
-    unsigned char* sB = base + MLP_STAGES * a_bytes;
+    unsigned char* sB = base + NS * a_bytes;
     const int m0 = blockIdx.x * MLP_BM, n0 = blockIdx.y * BN;
     const int kz = blockIdx.z;
     const int kbeg = kz * g.kchunk;
@@ -163,7 +167,7 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     volatile int* abort = &s_abort;
 
     if (tid == 0) {
-        for (int s = 0; s < MLP_STAGES; s++) {
+        for (int s = 0; s < NS; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
@@ -185,8 +189,8 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
         // producer
         int issued = 0;
         for (int kb = 0; kb < nk; kb++) {
-            const int s = kb % MLP_STAGES;
-            if (kb >= MLP_STAGES && !mbar_wait(&empty[s], ((kb / MLP_STAGES) - 1) & 1, abort)) break;
+            const int s = kb % NS;
+            if (kb >= NS && !mbar_wait(&empty[s], ((kb / NS) - 1) & 1, abort)) break;
             if (*abort) break;
             mbar_expect_tx(&full[s], a_bytes + b_bytes);
             tma_load_2d(sA + s * a_bytes, &tmA, kbeg + kb * MLP_BK, m0, &full[s]);
@@ -194,16 +198,16 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
             issued = kb + 1;
         }
         // copies still in flight complete before the CTA may exit
-        for (int kb = (issued > MLP_STAGES ? issued - MLP_STAGES : 0); kb < issued; kb++) {
+        for (int kb = (issued > NS ? issued - NS : 0); kb < issued; kb++) {
             for (uint32_t i = 0; i < BT_WAIT_LIMIT; i++)
-                if (bt_mbar_try_wait(&full[kb % MLP_STAGES], (kb / MLP_STAGES) & 1)) break;
+                if (bt_mbar_try_wait(&full[kb % NS], (kb / NS) & 1)) break;
         }
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
         const uint32_t idesc = mma_idesc(BN);
         for (int kb = 0; kb < nk; kb++) {
-            const int s = kb % MLP_STAGES;
-            if (!mbar_wait(&full[s], (kb / MLP_STAGES) & 1, abort)) break;
+            const int s = kb % NS;
+            if (!mbar_wait(&full[s], (kb / NS) & 1, abort)) break;
             tc_fence_after();
             const uint32_t a0 = bt_smem_addr(sA + s * a_bytes), b0 = bt_smem_addr(sB + s * b_bytes);
 #pragma unroll
@@ -221,10 +225,12 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     const bool ok = !*abort;
     tc_fence_after();
     if (ok) {
-        const int row = warp * 32 + lane;
+        const int wq = warp & 3;
+        const int row = wq * 32 + lane;
         const int m = m0 + row;
-        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-        for (int c = 0; c < BN; c += 32) {
+        const uint32_t trow = tmem + ((uint32_t)(wq * 32) << 16);
+        const int c0 = (warp >> 2) * (BN / 2);
+        for (int c = c0; c < c0 + BN / 2; c += 32) {
             float v[32];
             tmem_ld32(trow + (uint32_t)c, v);
             const int nb = n0 + c;
@@ -314,8 +320,10 @@ static bool make_map(CUtensorMap* map, const void* ptr, int rows, int cols, int 
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+static int mlp_stages(int bn) { return bn == 256 ? 2 : 3; }
+
 size_t bt_mlp_gemm_smem(int bn) {
-    return 1024 + (size_t)MLP_STAGES * (MLP_BM * MLP_BK * 2 + (size_t)bn * MLP_BK * 2);
+    return 1024 + (size_t)mlp_stages(bn) * (MLP_BM * MLP_BK * 2 + (size_t)bn * MLP_BK * 2);
 }
 
 cudaError_t bt_launch_mlp_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, const MlpGemmArgs& a, int splitk,
@@ -327,11 +335,13 @@ cudaError_t bt_launch_mlp_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, c
     if (!make_map(&ta, A, a.M, a.K, MLP_BM) || !make_map(&tb, B, a.N, a.K, a.bn)) return cudaErrorInvalidValue;
     MlpGemmArgs g = a;
     g.kchunk = a.K / splitk;
+    g.stages = mlp_stages(a.bn);
     const size_t smem = bt_mlp_gemm_smem(a.bn);
     static int attr_set = 0;
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(k_mlp_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)bt_mlp_gemm_smem(256));
+                                             (int)(bt_mlp_gemm_smem(256) > bt_mlp_gemm_smem(128)
+                                                       ? bt_mlp_gemm_smem(256) : bt_mlp_gemm_smem(128)));
         if (e != cudaSuccess) return e;
         attr_set = 1;
     }
