@@ -131,6 +131,8 @@ _SIGS = [
     ("bt_apply_reverse_transform_arrays", c_int, [_D3, _D3, _P, _P, _P, c_size_t, c_int, _P]),
     ("bt_finish_parallel", c_int, [_D3, _D3, _D3, _P, _P, _P, c_size_t, _P]),
     ("bt_obscure", c_int, [_P, ctypes.POINTER(BtRayVector), c_int, _P]),
+    ("bt_rsplit", c_int, [_P, _D3, _D3, _P, _P, _P, ctypes.POINTER(BtRayVector), ctypes.POINTER(BtRayVector), c_int,
+                          c_int, _P]),
     ("bt_intersect", c_int, [_P, _D3, _D3, ctypes.POINTER(BtRayVector), _P, c_int, c_int, _P]),
     ("bt_reflect", c_int, [_P, _D3, _D3, ctypes.POINTER(BtRayVector), _P, c_int, c_int, _P]),
     ("bt_refract", c_int, [_P, _D3, _D3, _P, _P, ctypes.POINTER(BtRayVector), _P, c_int, c_int, _P]),

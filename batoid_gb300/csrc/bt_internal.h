@@ -40,6 +40,8 @@ cudaError_t bt_launch_surface_eval(const unsigned char* d_blob, int blob_bytes, 
                                    cudaStream_t stream);
 cudaError_t bt_launch_getN(const unsigned char* d_blob, int blob_bytes, const double* w, double* out,
                            long long n, cudaStream_t stream);
+cudaError_t bt_launch_rsplit(const unsigned char* d_blob, int blob_bytes, const RV& rv, const RV& sp, int niter,
+                             cudaStream_t stream);
 cudaError_t bt_launch_obsc(const unsigned char* d_blob, int blob_bytes, const double* x, const double* y,
                            uint8_t* out, const RV* rv, long long n, cudaStream_t stream);
 

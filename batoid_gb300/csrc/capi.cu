@@ -674,6 +674,38 @@ extern "C" int bt_refract(const bt_surface* s, const double dr[3], const double 
     return surface_op(BT_ST_REFRACT, s, dr, drot, m2, rv, coating, niter, stream, "refract");
 }
 
+extern "C" int bt_rsplit(const bt_surface* s, const double dr[3], const double drot[9], const bt_medium_h* m1,
+                         const bt_medium_h* m2, const bt_coating* coating, const bt_rayvector* rv,
+                         const bt_rayvector* rv_split, int max_threads, int niter, void* stream) {
+    (void)max_threads;
+    (void)m1;  // n1 comes from |v| (src/batoid.cpp:599-603)
+    if (!s || !m2 || !coating) return fail(BT_ERR_ARG, "rsplit: null surface, medium or coating");
+    int rc = check_rv(rv);
+    if (rc != BT_OK) return rc;
+    rc = check_rv(rv_split);
+    if (rc != BT_OK) return rc;
+    if (rv_split->size != rv->size) return fail(BT_ERR_ARG, "rsplit: ray vectors differ in size");
+    if (!dr || !drot) return fail(BT_ERR_ARG, "rsplit: null transform");
+    if (niter < 0) return fail(BT_ERR_ARG, "rsplit: negative niter");
+    if (rv->size == 0) return BT_OK;
+    ProgBuilder pb;
+    bt_stage st = blank_stage(BT_ST_REFRACT);
+    set_transform(st, dr, drot);
+    st.surf = pb.add_surface(s);
+    if (st.surf < 0) return BT_ERR_CUDA;
+    st.medium = pb.add_medium(m2);
+    st.coated = 1;
+    st.coat_r = coating->R;
+    st.coat_t = coating->T;
+    pb.stages.push_back(st);
+    std::vector<unsigned char> b = pb.blob();
+    TempBlob tb;
+    CUDA_TRY(tb.upload(b, (cudaStream_t)stream), "rsplit");
+    RV v = to_rv(rv), w = to_rv(rv_split);
+    CUDA_TRY(bt_launch_rsplit(tb.d, tb.bytes, v, w, niter, (cudaStream_t)stream), "rsplit");
+    return BT_OK;
+}
+
 extern "C" int bt_obscure(const bt_obscuration* o, const bt_rayvector* rv, int max_threads, void* stream) {
     (void)max_threads;
     if (!o) return fail(BT_ERR_ARG, "obscure: null obscuration");

@@ -234,6 +234,33 @@ class Interface(Optic):
             result[self.name] = {'name': self.name, 'in': rv, 'out': self.trace(rv.copy(), reverse=reverse)}
         return result
 
+    def traceSplit(self, rv, minFlux=1e-3, reverse=False, _verbose=False):
+        """(forward, reverse) lists of rays after splitting at this surface
+        (batoid/optic.py:466-536): obscuration applied to both, ``path``
+        extended by this interface's name."""
+        if _verbose:
+            s = "forward" if not reverse else "reverse"
+            print("traceSplit {}       {:30s} flux = {:18.8f}   nphot = {:10d}".format(
+                s, self.name, float(np.sum(rv.flux)), len(rv)))
+        if self.skip:
+            return ([], [rv]) if reverse else ([rv], [])
+        refracted, reflected = self.rSplit(rv, reverse=reverse)
+        if self.obscuration is not None:
+            if refracted is not None:
+                self.obscuration.obscure(refracted)
+            if reflected is not None:
+                self.obscuration.obscure(reflected)
+        path = list(getattr(rv, 'path', []))
+        for r in (refracted, reflected):
+            if r is not None:
+                r.path = path + [self.name]
+        rForward, rReverse = [refracted], [reflected]
+        if reverse:
+            rForward, rReverse = rReverse, rForward
+        if isinstance(self, Mirror):
+            rForward, rReverse = rReverse, rForward
+        return rForward, rReverse
+
     def clearObscuration(self, unless=()):
         if self.name not in unless:
             self.obscuration = None
@@ -345,6 +372,16 @@ class RefractiveInterface(Interface):
     def refract(self, rv, reverse=False):
         return self.interact(rv, reverse=reverse)
 
+    def rSplit(self, rv, reverse=False):
+        """(refracted, reflected); as the reference, the forward pass uses
+        reverseCoating and the reverse pass forwardCoating
+        (batoid/optic.py:786-797)."""
+        if reverse:
+            m1, m2, coating = self.outMedium, self.inMedium, self.forwardCoating
+        else:
+            m1, m2, coating = self.inMedium, self.outMedium, self.reverseCoating
+        return self.surface.rSplit(rv, m1, m2, coating, coordSys=self.coordSys)
+
 
 class Mirror(Interface):
     def __init__(self, *args, **kwargs):
@@ -358,6 +395,10 @@ class Mirror(Interface):
     def reflect(self, rv, reverse=False):
         return self.interact(rv, reverse=reverse)
 
+    def rSplit(self, rv, reverse=False):
+        # reflection only (batoid/optic.py:821-823)
+        return None, self.surface.reflect(rv, coordSys=self.coordSys)
+
 
 class Detector(Interface):
     def __init__(self, *args, **kwargs):
@@ -365,12 +406,21 @@ class Detector(Interface):
         self.forwardCoating = SimpleCoating(reflectivity=0.0, transmissivity=1.0)
         self.reverseCoating = None
 
+    def rSplit(self, rv, reverse=False):
+        # batoid/optic.py:840-845
+        assert reverse is False
+        return self.surface.rSplit(rv, self.inMedium, self.outMedium, self.forwardCoating, coordSys=self.coordSys)
+
 
 class Baffle(Interface):
     def __init__(self, *args, **kwargs):
         Interface.__init__(self, *args, **kwargs)
         self.forwardCoating = SimpleCoating(reflectivity=0.0, transmissivity=1.0)
         self.reverseCoating = SimpleCoating(reflectivity=0.0, transmissivity=1.0)
+
+    def rSplit(self, rv, reverse=False):
+        # straight through (batoid/optic.py:864-865)
+        return self.surface.intersect(rv, self.coordSys), None
 
 
 class OPDScreen(Interface):
@@ -474,6 +524,46 @@ class CompoundOptic(Optic):
         if self.skip and path is None:
             return OrderedDict()
         return self._traceFull_fused(rv, reverse, path)
+
+    def traceSplit(self, rv, minFlux=1e-3, reverse=False, _verbose=False):
+        """Recursive split trace with a work queue (batoid/optic.py:1184-1280):
+        (forward, reverse) lists of RayVectors, one per distinct path, each
+        with its ``path``; vignetted rays and rays below minFlux are dropped
+        between items (stream compaction on the device)."""
+        if _verbose:
+            s = "reverse" if reverse else "forward"
+            print("traceSplit {}       {:30s} flux = {:18.8f}   nphot = {:10d}".format(
+                s, self.name, float(np.sum(rv.flux)), len(rv)))
+        if self.skip:
+            return ([], [rv]) if reverse else ([rv], [])
+        workQueue = [(rv, "forward", 0)] if not reverse else [(rv, "reverse", len(self.items) - 1)]
+        outF, outR = [], []
+        while workQueue:
+            rays, direction, idx = workQueue.pop()
+            optic = self.items[idx]
+            rF, rR = optic.traceSplit(rays, minFlux=minFlux, reverse=(direction == "reverse"), _verbose=_verbose)
+            rF = [r for r in rF if r is not None]
+            rR = [r for r in rR if r is not None]
+            for lst in (rF, rR):
+                for k, rr in enumerate(lst):
+                    keep = (rr._b[0] == 0) & (rr._d[8] >= minFlux)
+                    nr = RayVector._fromBuffers(rr._d[:, keep].contiguous(), rr._b[:, keep].contiguous(),
+                                                rr.coordSys)
+                    nr.path = rr.path
+                    lst[k] = nr
+            for rr in rF:
+                if len(rr) > 0:
+                    if idx == len(self.items) - 1:
+                        outF.append(rr)
+                    else:
+                        workQueue.append((rr, "forward", idx + 1))
+            for rr in rR:
+                if len(rr) > 0:
+                    if idx == 0:
+                        outR.append(rr)
+                    else:
+                        workQueue.append((rr, "reverse", idx - 1))
+        return outF, outR
 
     def clearObscuration(self, unless=()):
         for item in self.items:

@@ -62,6 +62,11 @@ class Surface(ABC):
     def refract(self, rv, inMedium, outMedium, coordSys=None, coating=None):
         return refract(self, rv, inMedium, outMedium, coordSys, coating)
 
+    def rSplit(self, rv, inMedium, outMedium, coating, coordSys=None):
+        """(refracted, reflected) rays (batoid/surface.py:107-133)."""
+        from .trace import rSplit
+        return rSplit(self, rv, inMedium, outMedium, coating, coordSys)
+
     def __ne__(self, rhs):
         return not (self == rhs)
 

@@ -308,7 +308,7 @@ class WavefrontSurrogate:
         out, err = self.predict_device(feat_d, grp_d, w_d)
         return D.to_host(out), D.to_host(err)
 
-    def calibrate(self, feat, grp, w, coefs, quantile=0.999):
+    def calibrate(self, feat, grp, w, coefs, quantile=0.99):
         """Safety factor on the predicted error: the given quantile of
         actual / predicted over a validation set."""
         pred, err = self.predict(feat, grp, w)

@@ -89,3 +89,17 @@ def refract(surface, rv, m1, m2, coordSys=None, coating=None):
                                      D.stream_ptr()))
     rv.coordSys = coordSys
     return rv
+
+
+def rSplit(surface, rv, inMedium, outMedium, coating, coordSys=None):
+    """(refracted, reflected): ``rv`` becomes the refracted rays, a copy the
+    reflected ones (batoid/trace.py:119-136; src/batoid.cpp:509-674)."""
+    if coordSys is None:
+        coordSys = rv.coordSys
+    keep, pdr, prot = _ct_args(CoordTransform(rv.coordSys, coordSys))
+    rvSplit = rv.copy()
+    _lib.check(_lib.lib().bt_rsplit(surface._surface.ptr, pdr, prot, inMedium._medium.ptr, outMedium._medium.ptr,
+                                    coating._coating.ptr, rv._rv, rvSplit._rv, 1, _niter(), D.stream_ptr()))
+    rv.coordSys = coordSys
+    rvSplit.coordSys = coordSys
+    return rv, rvSplit

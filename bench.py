@@ -435,6 +435,22 @@ def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24,
         return {"mean_nm": float(np.mean(e)), "p50_nm": float(np.median(e)), "p99_nm": float(np.quantile(e, 0.99)),
                 "max_nm": float(np.max(e)), "frac_above_threshold": float(np.mean(e > threshold_nm))}
 
+    # the largest surrogate errors: is the batched truth right there?  Recompute
+    # those samples with the CPU oracle of batoid.zernike
+    worst = np.argsort(-e_raw)[:4]
+    outliers = []
+    try:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import wavefront as owf
+        from batoid_gb300.utils import fieldToDirCos
+        for n in worst:
+            s_, f_ = divmod(int(n), F)
+            c = owf.zernike(pt.perturbed(hd[s_]), fieldToDirCos(*np.deg2rad(BATCH_FIELDS[f_])), hwl[n], 32, 28, pt.eps)
+            outliers.append({"sample": int(n), "surrogate_err_nm": float(e_raw[n]), "linear_err_nm": float(e_lin[n]),
+                             "batched_vs_oracle_m": float(np.max(np.abs(c - truth[n])) * hwl[n]),
+                             "dofs_max_abs_normalised": float(np.max(np.abs(hd[s_] / sur.dof_scale)))})
+    except Exception as exc:  # diagnostic only
+        outliers.append({"error": repr(exc)})
     flops_fwd = 2.0 * (33 * 512 + 3 * 512 * 512 + 512 * 28)
     peaks = {}
     try:
@@ -463,6 +479,7 @@ def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24,
                                "frac": infer_tflops / bf16_peak, "flops_per_sample": flops_fwd,
                                "note": "whole inference pipeline (pack, 5 GEMMs, combine) over its event time"},
         "gpu_launches_per_inference": 7,
+        "largest_errors": outliers,
     }
     return out_d
 

@@ -150,6 +150,14 @@ int bt_apply_reverse_transform_arrays(const double dr[3], const double drot[9],
                                       int max_threads, void* stream);    /* src/batoid.cpp:24-38 */
 int bt_finish_parallel(const double dr[3], const double drot[9], const double vv[3],
                        double* x, double* y, double* z, size_t n, void* stream); /* src/batoid.cpp:40-69 */
+/* rSplit(surface, dr, drot, m1, m2, coating, rv, rvSplit, max_threads, niter)
+ * (src/batoid.cpp:509-674; pysrc/batoid.cpp): intersect, then the refracted
+ * ray replaces rv's ray and the reflected ray is written to rv_split, which
+ * must hold a copy of rv on entry (batoid/trace.py:125); fluxes are scaled
+ * by the coating's transmissivity / reflectivity. */
+int bt_rsplit(const bt_surface* s, const double dr[3], const double drot[9], const bt_medium_h* m1,
+              const bt_medium_h* m2, const bt_coating* coating, const bt_rayvector* rv, const bt_rayvector* rv_split,
+              int max_threads, int niter, void* stream);
 int bt_obscure(const bt_obscuration* o, const bt_rayvector* rv, int max_threads, void* stream); /* src/batoid.cpp:151-172 */
 int bt_intersect(const bt_surface* s, const double dr[3], const double drot[9], const bt_rayvector* rv,
                  const bt_coating* coating, int max_threads, int niter, void* stream); /* src/batoid.cpp:175-270 */

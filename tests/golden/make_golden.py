@@ -291,16 +291,42 @@ def zemax_fixture(batoid, ref_root):
     return out
 
 
+def split_fixture(batoid):
+    """rSplit on single surfaces (incl. TIR, misses, failed inputs) and
+    traceSplit through a two-singlet system with 2 % reflecting coatings."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _split_optic as S
+    out = {}
+    for c, (surf, m1, m2, coat, cs, speed) in enumerate(S.rsplit_cases(batoid)):
+        rv = make_rv(batoid, S.rsplit_rays(speed=speed))
+        a, b = batoid.trace.rSplit(surf, rv, m1, m2, coat, coordSys=cs)
+        out.update(rv_to_dict(a, f"rs{c}_refr"))
+        out.update(rv_to_dict(b, f"rs{c}_refl"))
+    optic = S.split_optic(batoid)
+    fwd, rev = optic.traceSplit(make_rv(batoid, S.split_rays()), minFlux=1e-4)
+    for tag, lst in (("F", fwd), ("R", rev)):
+        out[f"{tag}_n"] = np.array(len(lst))
+        out[f"{tag}_paths"] = np.array(["|".join(r.path) for r in lst])
+        for k, r in enumerate(lst):
+            out.update(rv_to_dict(r, f"{tag}{k}"))
+    return out
+
+
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    ref_root = args[0] if args else "/root/reference"
     os.environ["BATOID_REF"] = ref_root
     batoid = import_reference(ref_root)
     batoid.global_vars._batoid_max_threads = 1
+    if "--only-split" in sys.argv:
+        np.savez_compressed(os.path.join(HERE, "split.npz"), **split_fixture(batoid))
+        return
     np.savez_compressed(os.path.join(HERE, "workloads.npz"), **workload_fixtures(batoid))
     np.savez_compressed(os.path.join(HERE, "primitives.npz"), **primitive_fixtures(batoid))
     np.savez_compressed(os.path.join(HERE, "huygens.npz"), **huygens_fixture(batoid))
     np.savez_compressed(os.path.join(HERE, "sellmeier_csv.npz"), **sellmeier_csv_fixture(ref_root))
     np.savez_compressed(os.path.join(HERE, "zemax.npz"), **zemax_fixture(batoid, ref_root))
+    np.savez_compressed(os.path.join(HERE, "split.npz"), **split_fixture(batoid))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
