@@ -165,3 +165,267 @@ def normal_equations(x, y, values, basis):
     """(B^T B, B^T v) for the Cartesian-polynomial basis over the points."""
     from . import _fit
     return _fit.normal_equations(x, y, values, basis)
+
+
+# ---------------------------------------------------------------------------
+# Further analyses (batoid/analysis.py:59-180, 391-476, 576-1090): the rays
+# are traced on the device; the small reductions that follow run on the host
+# as in the reference.
+# ---------------------------------------------------------------------------
+
+def zernikeBasis(jmax, x, y, R_outer=1.0, R_inner=0.0):
+    """Annular Zernike basis values, shape (jmax+1, npoints), row 0 zero
+    (the layout of galsim.zernike.zernikeBasis the reference calls)."""
+    x = np.asarray(x, dtype=float)
+    y = np.asarray(y, dtype=float)
+    cart = _zk.basis_xy(jmax, R_outer, R_inner)
+    out = np.zeros((jmax + 1,) + x.shape)
+    for j in range(jmax):
+        out[j + 1] = _zk.horner2d_host(x, y, cart[j])
+    return out
+
+
+def _dZernikeBasis(jmax, x, y, R_outer=1.0, R_inner=0.0):
+    """Gradients of the basis: array (2, jmax+1, npoints) (batoid/analysis.py:715-730)."""
+    x = np.asarray(x, dtype=float)
+    y = np.asarray(y, dtype=float)
+    cart = _zk.basis_xy(jmax, R_outer, R_inner)
+    xout = np.zeros((jmax + 1,) + x.shape)
+    yout = np.zeros_like(xout)
+    for j in range(jmax):
+        gx, gy = _zk.grad_xy(cart[j])
+        xout[j + 1] = _zk.horner2d_host(x, y, gx)
+        yout[j + 1] = _zk.horner2d_host(x, y, gy)
+    return np.array([xout, yout])
+
+
+def drdth(optic, theta_x, theta_y, wavelength, nrad=6, naz=36, projection='postel'):
+    """Focal-plane Jacobian d(x, y)/d(theta_x, theta_y) by finite differences
+    (batoid/analysis.py:59-136)."""
+    from .rayVector import concatenateRayVectors
+    dth = 1e-5
+    nominalCos = fieldToDirCos(theta_x, theta_y, projection=projection)
+    dthxCos = fieldToDirCos(theta_x + dth, theta_y, projection=projection)
+    dthyCos = fieldToDirCos(theta_x, theta_y + dth, projection=projection)
+    rays = RayVector.asPolar(optic=optic, wavelength=wavelength, dirCos=nominalCos, nrad=nrad, naz=naz)
+    rays_x = RayVector.asPolar(optic=optic, wavelength=wavelength, dirCos=dthxCos, nrad=nrad, naz=naz)
+    rays_y = RayVector.asPolar(optic=optic, wavelength=wavelength, dirCos=dthyCos, nrad=nrad, naz=naz)
+    rays_c = concatenateRayVectors([rays, rays_x, rays_y])
+    optic.trace(rays_c)
+    n = len(rays)
+    rays, rays_x, rays_y = rays_c[:n], rays_c[n:2 * n], rays_c[2 * n:3 * n]
+    w = ~rays.vignetted
+    mx = np.mean(rays.x[w])
+    my = np.mean(rays.y[w])
+    drx_dthx = (np.mean(rays_x.x[w]) - mx) / dth
+    drx_dthy = (np.mean(rays_y.x[w]) - mx) / dth
+    dry_dthx = (np.mean(rays_x.y[w]) - my) / dth
+    dry_dthy = (np.mean(rays_y.y[w]) - my) / dth
+    return np.array([[drx_dthx, drx_dthy], [dry_dthx, dry_dthy]])
+
+
+def dthdr(optic, theta_x, theta_y, wavelength, nrad=6, naz=36, projection='postel'):
+    """Inverse of drdth (batoid/analysis.py:139-178)."""
+    return np.linalg.inv(drdth(optic, theta_x, theta_y, wavelength, nrad=nrad, naz=naz, projection=projection))
+
+
+def spot(optic, theta_x, theta_y, wavelength, projection='postel', nx=32, reference='chief'):
+    """Spot diagram: focal-plane x, y of non-vignetted grid rays relative to
+    the reference point (batoid/analysis.py:391-413)."""
+    dirCos = fieldToDirCos(theta_x, theta_y, projection=projection)
+    rays = RayVector.asGrid(optic=optic, wavelength=wavelength, nx=nx, dirCos=dirCos)
+    optic.trace(rays)
+    if reference == 'mean':
+        w = np.where(1 - rays.vignetted)[0]
+        point = np.mean(rays.r[w], axis=0)
+    elif reference == 'chief':
+        point = rays[_chief_index(nx)].r[0]
+    else:
+        point = [0, 0, 0]
+    targetCoordSys = rays.coordSys.shiftLocal(point)
+    rays.toCoordSys(targetCoordSys)
+    w = ~rays.vignetted
+    return rays.x[w], rays.y[w]
+
+
+def fftPSF(optic, theta_x, theta_y, wavelength, projection='postel', nx=32, pad_factor=2, sphereRadius=None,
+           reference='chief'):
+    """PSF as |FFT(pupil function)|^2 of the wavefront (batoid/analysis.py:416-476)."""
+    wf = wavefront(optic, theta_x, theta_y, wavelength, nx=nx, projection=projection, sphereRadius=sphereRadius,
+                   reference=reference)
+    wfarr = wf.array
+    pad_size = nx * pad_factor
+    expwf = np.zeros((pad_size, pad_size), dtype=np.complex128)
+    start = pad_size // 2 - nx // 2
+    stop = pad_size // 2 + nx // 2
+    expwf[start:stop, start:stop][~wfarr.mask] = np.exp(2j * np.pi * wfarr[~wfarr.mask])
+    psf = np.abs(np.fft.fftshift(np.fft.fft2(expwf))) ** 2
+    primitiveU = wf.primitiveVectors
+    primitiveK = dkdu(optic, theta_x, theta_y, wavelength, projection=projection).dot(primitiveU)
+    primitiveX = np.vstack(_reciprocalLatticeVectors(primitiveK[0], primitiveK[1], pad_size))
+    return Lattice(psf, primitiveX)
+
+
+def _chief_ray(optic, wavelength, dirCos):
+    return RayVector.fromStop(0.0, 0.0, backDist=optic.backDist, wavelength=wavelength, dirCos=dirCos,
+                              medium=optic.inMedium, stopSurface=optic.stopSurface)
+
+
+def zernikeGQ(optic, theta_x, theta_y, wavelength, projection='postel', rings=6, spokes=None, sphereRadius=None,
+              reference='chief', jmax=22, eps=0.0):
+    """Zernike coefficients (waves) by Gaussian quadrature over the annulus
+    (batoid/analysis.py:576-712)."""
+    from .surface import Sphere
+    dirCos = fieldToDirCos(theta_x, theta_y, projection=projection)
+    inner = eps * optic.pupilSize / 2
+    rays = RayVector.asSpokes(optic=optic, wavelength=wavelength, inner=inner, dirCos=dirCos, rings=rings,
+                              spokes=spokes, spacing='GQ')
+    epRays = rays.copy().toCoordSys(optic.stopSurface.coordSys)
+    optic.stopSurface.surface.intersect(epRays)
+    basis = zernikeBasis(jmax, epRays.x, epRays.y, R_outer=optic.pupilSize / 2, R_inner=inner)
+    if sphereRadius is None:
+        sphereRadius = optic.sphereRadius
+    optic.trace(rays)
+    if np.any(rays.failed):
+        raise ValueError("Cannot compute zernike with Gaussian Quadrature with failed rays.")
+    if reference == 'mean':
+        w = np.where(1 - rays.vignetted)[0]
+        point = np.mean(rays.r[w], axis=0)
+    elif reference == 'chief':
+        chiefRay = _chief_ray(optic, wavelength, dirCos)
+        optic.trace(chiefRay)
+        point = chiefRay.r[0]
+    targetCoordSys = rays.coordSys.shiftLocal(point + np.array([0, 0, sphereRadius]))
+    rays.toCoordSys(targetCoordSys)
+    sphere = Sphere(-sphereRadius)
+    sphere.intersect(rays)
+    if reference == 'mean':
+        w = np.where(1 - rays.vignetted)[0]
+        t0 = np.mean(rays.t[w])
+    elif reference == 'chief':
+        chiefRay.toCoordSys(targetCoordSys)
+        sphere.intersect(chiefRay)
+        t0 = chiefRay.t
+    area = np.pi * (1. - eps ** 2)
+    return np.dot(basis, (t0 - rays.t) / wavelength * rays.flux) / area
+
+
+def zernikeTA(optic, theta_x, theta_y, wavelength, projection='postel', nrad=6, naz=36, reference='chief', jmax=22,
+              eps=0.0, focal_length=None, include_vignetted=False):
+    """Zernike coefficients (waves) whose wavefront gradient matches the
+    transverse ray aberrations (batoid/analysis.py:732-833)."""
+    dirCos = fieldToDirCos(theta_x, theta_y, projection=projection)
+    rays = RayVector.asPolar(optic=optic, wavelength=wavelength, dirCos=dirCos, nrad=nrad, naz=naz)
+    epRays = rays.copy().toCoordSys(optic.stopSurface.coordSys)
+    optic.stopSurface.surface.intersect(epRays)
+    u = np.array(epRays.x)
+    v = np.array(epRays.y)
+    rays = optic.trace(rays)
+    w = slice(None) if include_vignetted else ~rays.vignetted
+    if reference == 'mean':
+        point = np.mean(rays.r[w], axis=0)
+    elif reference == 'chief':
+        chief = RayVector.fromStop(0, 0, optic, wavelength=wavelength, dirCos=dirCos)
+        optic.trace(chief)
+        point = chief.r[0]
+    x = rays.x - point[0]
+    y = rays.y - point[1]
+    if focal_length is None:
+        focal_length = np.sqrt(np.linalg.det(drdth(optic, theta_x, theta_y, wavelength, projection=projection)))
+    dzb = _dZernikeBasis(jmax, u[w], v[w], optic.pupilSize / 2, eps * optic.pupilSize / 2)
+    a = np.hstack(dzb).T
+    b = np.hstack([x[w], y[w]])
+    r, _, rank, _ = np.linalg.lstsq(a, b, rcond=None)
+    if rank < jmax - 1:
+        raise RuntimeError(f"Rank {rank} matrix found when fitting {jmax} Zernike coefficients.  ")
+    r[0] = 0.0
+    return -r / focal_length / wavelength
+
+
+def zernikeXYAberrations(optic, theta_x, theta_y, wavelength, projection='postel', nrad=6, naz=36,
+                         reference='chief', jmax=22, eps=0.0, include_vignetted=False):
+    """Zernike fits (meters) of the x and y transverse aberrations
+    (batoid/analysis.py:836-925)."""
+    dirCos = fieldToDirCos(theta_x, theta_y, projection=projection)
+    rays = RayVector.asPolar(optic=optic, wavelength=wavelength, dirCos=dirCos, nrad=nrad, naz=naz)
+    epRays = rays.copy().toCoordSys(optic.stopSurface.coordSys)
+    optic.stopSurface.surface.intersect(epRays)
+    u = np.array(epRays.x)
+    v = np.array(epRays.y)
+    rays = optic.trace(rays)
+    if reference == 'mean':
+        w = ~rays.vignetted
+        point = np.mean(rays.r[w], axis=0)
+    elif reference == 'chief':
+        chief = RayVector.fromStop(0, 0, optic, wavelength=wavelength, dirCos=dirCos)
+        optic.trace(chief)
+        point = chief.r[0]
+    x = rays.x - point[0]
+    y = rays.y - point[1]
+    if not include_vignetted:
+        w = ~rays.vignetted
+        u, v, x, y = u[w], v[w], x[w], y[w]
+    basis = zernikeBasis(jmax, u, v, R_outer=optic.pupilSize / 2, R_inner=optic.pupilSize / 2 * eps)
+    x_coefs, _, x_rank, _ = np.linalg.lstsq(basis.T, x, rcond=None)
+    y_coefs, _, y_rank, _ = np.linalg.lstsq(basis.T, y, rcond=None)
+    rank = min(x_rank, y_rank)
+    if rank < jmax:
+        raise RuntimeError(f"Rank {rank} matrix found when fitting {jmax} Zernike coefficients.  ")
+    x_coefs[0] = 0.0
+    y_coefs[0] = 0.0
+    return x_coefs, y_coefs
+
+
+def doubleZernike(optic, field, wavelength, rings=6, spokes=None, kmax=22, **kwargs):
+    """Double Zernike coefficients (waves) over pupil and field by Gaussian
+    quadrature in both (batoid/analysis.py:928-993)."""
+    if spokes is None:
+        spokes = 2 * rings + 1
+    Li, w = np.polynomial.legendre.leggauss(rings)
+    radii = np.sqrt((1 + Li) / 2) * field
+    w *= np.pi / (2 * spokes)
+    azs = np.linspace(0, 2 * np.pi, spokes, endpoint=False)
+    radii, azs = np.meshgrid(radii, azs)
+    w = np.broadcast_to(w, radii.shape)
+    radii = radii.ravel()
+    azs = azs.ravel()
+    w = w.ravel()
+    thx = radii * np.cos(azs)
+    thy = radii * np.sin(azs)
+    coefs = np.array([zernikeGQ(optic, thx_, thy_, wavelength, rings=rings, spokes=spokes, **kwargs)
+                      for thx_, thy_ in zip(thx, thy)])
+    basis = zernikeBasis(kmax, thx, thy, R_outer=field)
+    return np.dot(basis, coefs * w[:, None]) / np.pi
+
+
+def _closestApproach(P, u, Q, v):
+    """Point on P + u t closest to the line Q + v t."""
+    a = np.dot(u, u)
+    b = np.dot(u, v)
+    c = np.dot(v, v)
+    w0 = P - Q
+    d = np.dot(u, w0)
+    e = np.dot(v, w0)
+    den = a * c - b * b
+    if den == 0:
+        raise ValueError("Lines are parallel")
+    sc = (b * e - c * d) / den
+    return P + sc * u
+
+
+def exitPupilPos(optic, wavelength, smallAngle=np.deg2rad(1. / 3600), **kwargs):
+    """Exit-pupil position from small-angle chief rays' closest approach to
+    the optic axis (batoid/analysis.py:1025-1065)."""
+    from .constants import globalCoordSys
+    thx = np.array([0, 0, smallAngle, -smallAngle])
+    thy = np.array([smallAngle, -smallAngle, 0, 0])
+    rays = RayVector.fromFieldAngles(thx, thy, optic=optic, wavelength=wavelength, **kwargs)
+    optic.trace(rays)
+    rays.toCoordSys(globalCoordSys)
+    ps = [_closestApproach(ray.r[0], ray.v[0], np.array([0., 0., 0.]), np.array([0., 0., 1.0])) for ray in rays]
+    return np.mean(ps, axis=0)
+
+
+def focalLength(*args, **kwargs):
+    """sqrt(det(drdth)) (batoid/analysis.py:1068-1090)."""
+    return np.sqrt(np.linalg.det(drdth(*args, **kwargs)))

@@ -312,6 +312,23 @@ def split_fixture(batoid):
     return out
 
 
+def analysis_fixture(batoid):
+    """drdth, dthdr, spot, fftPSF, exitPupilPos and focalLength of the
+    12-surface system at one off-axis field (the reference's own analysis
+    functions; the GalSim-based ones cannot run here)."""
+    opt = W.tma_optic(batoid, zernike_factory=ref_zernike_factory(batoid))
+    thx, thy, wl = np.deg2rad(0.6), np.deg2rad(-0.4), 620e-9
+    A = batoid.analysis
+    out = {"drdth": A.drdth(opt, thx, thy, wl), "dthdr": A.dthdr(opt, thx, thy, wl)}
+    sx, sy = A.spot(opt, thx, thy, wl, nx=32)
+    out["spot_x"], out["spot_y"] = np.asarray(sx), np.asarray(sy)
+    psf = A.fftPSF(opt, thx, thy, wl, nx=32, pad_factor=2)
+    out["fft_array"], out["fft_prim"] = np.asarray(psf.array), np.asarray(psf.primitiveVectors)
+    out["epp"] = A.exitPupilPos(opt, wl)
+    out["focal_length"] = np.array(A.focalLength(opt, thx, thy, wl))
+    return out
+
+
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     ref_root = args[0] if args else "/root/reference"
@@ -321,12 +338,16 @@ def main():
     if "--only-split" in sys.argv:
         np.savez_compressed(os.path.join(HERE, "split.npz"), **split_fixture(batoid))
         return
+    if "--only-analysis" in sys.argv:
+        np.savez_compressed(os.path.join(HERE, "analysis.npz"), **analysis_fixture(batoid))
+        return
     np.savez_compressed(os.path.join(HERE, "workloads.npz"), **workload_fixtures(batoid))
     np.savez_compressed(os.path.join(HERE, "primitives.npz"), **primitive_fixtures(batoid))
     np.savez_compressed(os.path.join(HERE, "huygens.npz"), **huygens_fixture(batoid))
     np.savez_compressed(os.path.join(HERE, "sellmeier_csv.npz"), **sellmeier_csv_fixture(ref_root))
     np.savez_compressed(os.path.join(HERE, "zemax.npz"), **zemax_fixture(batoid, ref_root))
     np.savez_compressed(os.path.join(HERE, "split.npz"), **split_fixture(batoid))
+    np.savez_compressed(os.path.join(HERE, "analysis.npz"), **analysis_fixture(batoid))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -1,0 +1,71 @@
+"""Analysis functions on the GPU trace: drdth, dthdr, spot, fftPSF,
+exitPupilPos, focalLength against the reference's own outputs
+(tests/golden/analysis.npz); zernikeGQ / zernikeTA / zernikeXYAberrations /
+doubleZernike (GalSim-based in the reference, so unpinned) against the
+least-squares zernike fit and each other."""
+import numpy as np
+import pytest
+
+import batoid_gb300 as bt
+from batoid_gb300 import workloads as W
+from _helpers import golden
+
+pytestmark = pytest.mark.gpu
+
+TH = (np.deg2rad(0.6), np.deg2rad(-0.4))
+WL = 620e-9
+
+
+@pytest.fixture(scope="module")
+def optic():
+    return W.tma_optic(bt)
+
+
+def test_reference_analyses(optic):
+    g = golden("analysis")
+    np.testing.assert_allclose(bt.drdth(optic, *TH, WL), g["drdth"], rtol=0, atol=1e-6)
+    np.testing.assert_allclose(bt.dthdr(optic, *TH, WL), g["dthdr"], rtol=0, atol=1e-8)
+    sx, sy = bt.spot(optic, *TH, WL, nx=32)
+    np.testing.assert_allclose(sx, g["spot_x"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(sy, g["spot_y"], rtol=0, atol=1e-12)
+    psf = bt.fftPSF(optic, *TH, WL, nx=32, pad_factor=2)
+    np.testing.assert_allclose(psf.array, g["fft_array"], rtol=0, atol=1e-6 * g["fft_array"].max())
+    np.testing.assert_allclose(psf.primitiveVectors, g["fft_prim"], rtol=1e-6, atol=0)
+    np.testing.assert_allclose(bt.exitPupilPos(optic, WL), g["epp"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(bt.focalLength(optic, *TH, WL), g["focal_length"], rtol=1e-9)
+
+
+def test_zernikeGQ_agrees_with_least_squares(optic):
+    eps = optic.pupilObscuration
+    gq = bt.zernikeGQ(optic, 0.0, 0.0, WL, rings=12, jmax=22, eps=eps)
+    ls = bt.zernike(optic, 0.0, 0.0, WL, nx=160, jmax=22, eps=eps)
+    assert gq.shape == (23,)
+    # on axis the support of both is the full annulus
+    np.testing.assert_allclose(gq[4:], ls[4:], rtol=0, atol=2e-3)
+
+
+def test_zernikeTA_and_xy_aberrations(optic):
+    eps = optic.pupilObscuration
+    ta = bt.zernikeTA(optic, *TH, WL, nrad=10, naz=60, jmax=22, eps=eps)
+    ls = bt.zernike(optic, *TH, WL, nx=128, jmax=22, eps=eps)
+    assert ta[0] == 0.0 and np.all(np.isfinite(ta))
+    # transverse-aberration and wavefront fits describe the same aberrations
+    a, b = ta[4:], ls[4:]
+    assert np.dot(a, b) / np.linalg.norm(a) / np.linalg.norm(b) > 0.9
+    xz, yz = bt.zernikeXYAberrations(optic, *TH, WL, nrad=10, naz=60, jmax=22, eps=eps)
+    assert xz[0] == 0.0 and yz[0] == 0.0 and np.all(np.isfinite(xz)) and np.all(np.isfinite(yz))
+
+
+def test_doubleZernike_reproduces_field_dependence(optic):
+    eps = optic.pupilObscuration
+    field = np.deg2rad(1.2)
+    dz = bt.doubleZernike(optic, field, WL, rings=4, kmax=10, jmax=11, eps=eps)
+    assert dz.shape == (11, 12)
+    # the field-average term of each pupil Zernike is the mean over field of zernikeGQ
+    Li, w = np.polynomial.legendre.leggauss(4)
+    r = np.sqrt((1 + Li) / 2) * field
+    mean = np.zeros(12)
+    for rr, ww in zip(r, w):
+        for az in np.linspace(0, 2 * np.pi, 9, endpoint=False):
+            mean += ww * bt.zernikeGQ(optic, rr * np.cos(az), rr * np.sin(az), WL, rings=4, jmax=11, eps=eps) / 18
+    np.testing.assert_allclose(dz[1], mean, rtol=0, atol=1e-9)
