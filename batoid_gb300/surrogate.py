@@ -199,14 +199,16 @@ class WavefrontSurrogate:
         self.kappa = 1.0
 
     # -- data ----------------------------------------------------------------------
-    def sample_states(self, nstates, seed):
+    def sample_states(self, nstates, seed, widen=1.0):
         """Seeded states: rigid dofs uniform within +-1 mm / +-10 arcsec,
-        bending amplitudes N(0, 100 nm), wavelength index uniform."""
+        bending amplitudes N(0, 100 nm), wavelength index uniform.  `widen`
+        scales both ranges (training on a wider distribution than the one
+        evaluated keeps its tails inside the training support)."""
         rng = np.random.default_rng(seed)
         nr = 5 * len(self.pt.rigid)
         dofs = np.empty((nstates, self.pt.ndof))
-        dofs[:, :nr] = rng.uniform(-1, 1, (nstates, nr)) * self.dof_scale[:nr]
-        dofs[:, nr:] = rng.normal(0.0, 100e-9, (nstates, self.pt.nmodes))
+        dofs[:, :nr] = rng.uniform(-widen, widen, (nstates, nr)) * self.dof_scale[:nr]
+        dofs[:, nr:] = rng.normal(0.0, 100e-9 * widen, (nstates, self.pt.nmodes))
         widx = rng.integers(0, len(self.wavelengths), nstates)
         return dofs, widx
 
