@@ -128,6 +128,40 @@ __device__ __noinline__ void bt_batch_target(const BatchArgs& A, int s, const Ra
     sph.identity = 0;
 }
 
+// The reference-sphere stage: transform into the sphere's frame, intersect
+// the Sphere(-R) surface (src/sphere.cpp root choice), propagate; a miss
+// fails and vignettes the ray (src/batoid.cpp:175-270 with a sphere).
+__device__ __forceinline__ void bt_sphere_stage(const Prog& P, const bt_stage& st, RayState& r) {
+    if (r.fail) return;
+    const double dx = r.x - st.dr[0], dy = r.y - st.dr[1], dz = r.z - st.dr[2];
+    double x = dx * st.drot[0] + dy * st.drot[3] + dz * st.drot[6];
+    double y = dx * st.drot[1] + dy * st.drot[4] + dz * st.drot[7];
+    double z = dx * st.drot[2] + dy * st.drot[5] + dz * st.drot[8];
+    const double vx = r.vx * st.drot[0] + r.vy * st.drot[3] + r.vz * st.drot[6];
+    const double vy = r.vx * st.drot[1] + r.vy * st.drot[4] + r.vz * st.drot[7];
+    const double vz = r.vx * st.drot[2] + r.vy * st.drot[5] + r.vz * st.drot[8];
+    const bt_surf& sp = P.surfs[st.surf];
+    const double R = sp.p[0];
+    const double z0 = z - R;
+    const double a = vz * vz + (vx * vx + vy * vy);
+    const double b = 2 * vz * z0 + 2 * (vx * x + vy * y);
+    const double c = z0 * z0 - sp.p[1] + (x * x + y * y);
+    const bool want_max = (vz * R < 0);
+    double dt;
+    if (!bt_one_root(a, b, c, want_max == (a > 0), &dt)) {
+        r.fail = true;
+        r.vig = true;
+        return;
+    }
+    r.x = x + vx * dt;
+    r.y = y + vy * dt;
+    r.z = z + vz * dt;
+    r.vx = vx;
+    r.vy = vy;
+    r.vz = vz;
+    r.t += dt;
+}
+
 __device__ __forceinline__ double bt_warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -294,11 +328,9 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
                 bt_batch_ray(A, F, nx, i, wl, r, &gx, &gy);
                 int cm = -1;
                 double cn = 0.0, cin = 0.0;
-                for (int k = 0; k <= A.ntrace; k++) {
-                    if (chief && k == A.ntrace) bt_batch_target(A, s, r, sph);
-                    // stage ntrace: the reference sphere
-                    run_stage(P, stages[k], r, A.niter, cm, cn, cin);
-                }
+                for (int k = 0; k < A.ntrace; k++) run_stage(P, stages[k], r, A.niter, cm, cn, cin);
+                if (chief) bt_batch_target(A, s, r, sph);
+                bt_sphere_stage(P, sph, r);
             }
             if (chief) {
                 if (tid == 0) s_t0 = r.t;

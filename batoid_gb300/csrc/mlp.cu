@@ -3,18 +3,18 @@
 //
 //   C[M x N] = A[M x K] . B[N x K]^T      (both operands K-major, bf16)
 //
-// One CTA computes a 128 x BN tile (BN = 128 or 256) over a K range:
+// Tiles of 128 x BN (BN = 128 or 256) over a K range; one persistent CTA
+// per SM (384 threads) walks the tile list:
 //   * warp 0 / lane 0 streams 128 x 64 and BN x 64 operand tiles from global
 //     memory with TMA (cp.async.bulk.tensor, 128-byte swizzle) into a
 //     4-stage shared-memory ring (full / empty mbarriers);
 //   * warp 1 / lane 0 issues tcgen05.mma (M 128, N BN, K 16) from shared
-//     memory descriptors into a TMEM accumulator of BN columns and releases
-//     each stage with tcgen05.commit;
-//   * all eight warps read the accumulator back with tcgen05.ld (warp w
-//     owns TMEM lanes 32(w%4)..32(w%4)+31 = tile rows, and half w/4 of the
-//     columns) and run the epilogue.
-// The ring has 2 stages at BN 256 and 3 at BN 128 (97 KB), so two CTAs share
-// an SM and one's epilogue overlaps the other's MMAs.
+//     memory descriptors into one of two TMEM accumulators of BN columns,
+//     releases each stage with tcgen05.commit and hands the finished
+//     accumulator to the epilogue;
+//   * warps 4..11 read it back with tcgen05.ld (warp w owns TMEM lanes
+//     32(w%4)..32(w%4)+31 = tile rows, and half (w-4)/4 of the columns) and
+//     run the epilogue while the next tile accumulates in the other buffer.
 // Every wait is bounded: on expiry the CTA records BT_ERR_TIMEOUT in the
 // device status word, stops issuing, waits (bounded) for the copies and
 // MMAs it started, frees its TMEM and returns.
@@ -37,7 +37,9 @@
 #define MLP_BM 128
 #define MLP_BK 64
 #define MLP_STAGES 4
-#define MLP_THREADS 256
+#define MLP_THREADS 384
+#define MLP_EPI_WARP0 4
+#define MLP_NEPI 8
 
 cudaError_t bt_read_mlp_device_status(int* status, cudaStream_t stream) {
     int zero = 0;
@@ -143,26 +145,37 @@ __device__ __forceinline__ float dgelu_f(float z) {
 // The GEMM kernel
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(MLP_THREADS, 2)
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bt_smem_addr(bar)) : "memory");
+}
+
+// Persistent: one CTA per SM walks the tile list (M fastest, so CTAs running
+// together share the weight tile in L2).  Warp 0 lane 0 streams operands
+// into the ring; warp 1 lane 0 issues the MMAs of tile i into TMEM
+// accumulator buffer i % 2; warps 4..11 drain the other buffer (epilogue)
+// meanwhile.  Barriers: full/empty per ring stage, acc_full/acc_empty per
+// accumulator buffer; the first use of each "empty" barrier waits on the
+// phase before the barrier's first, which counts as completed.
+__global__ void __launch_bounds__(MLP_THREADS, 1)
 k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, MlpGemmArgs g) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t full[MLP_STAGES];
     __shared__ __align__(8) uint64_t empty[MLP_STAGES];
+    __shared__ __align__(8) uint64_t acc_full[2];
+    __shared__ __align__(8) uint64_t acc_empty[2];
     __shared__ __align__(8) uint64_t done;
     __shared__ uint32_t s_tmem;
     __shared__ int s_abort;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int BN = g.bn;
     const int NS = g.stages;
-    // operand ring, 1024-byte aligned for the swizzle atoms
     const uint32_t raw = bt_smem_addr(smem_raw);
     unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
     const uint32_t a_bytes = MLP_BM * MLP_BK * 2, b_bytes = (uint32_t)BN * MLP_BK * 2;
     unsigned char* sA = base;
     unsigned char* sB = base + NS * a_bytes;
-    const int m0 = blockIdx.x * MLP_BM, n0 = blockIdx.y * BN;
-    const int kz = blockIdx.z;
-    const int kbeg = kz * g.kchunk;
+    const int tiles_m = g.M / MLP_BM, tiles_n = g.N / BN;
+    const int ntiles = tiles_m * tiles_n * (g.K / g.kchunk);
     const int nk = g.kchunk / MLP_BK;
     volatile int* abort = &s_abort;
 
@@ -171,13 +184,17 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], MLP_NEPI);
+        }
         mbar_init(&done, 1);
         s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     ::"r"(bt_smem_addr(&s_tmem)), "r"((uint32_t)BN) : "memory");
+                     ::"r"(bt_smem_addr(&s_tmem)), "r"((uint32_t)(2 * BN)) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     tc_fence_before();
@@ -187,102 +204,124 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
 
     if (warp == 0 && lane == 0) {
         // producer
-        int issued = 0;
-        for (int kb = 0; kb < nk; kb++) {
-            const int s = kb % NS;
-            if (kb >= NS && !mbar_wait(&empty[s], ((kb / NS) - 1) & 1, abort)) break;
-            if (*abort) break;
-            mbar_expect_tx(&full[s], a_bytes + b_bytes);
-            tma_load_2d(sA + s * a_bytes, &tmA, kbeg + kb * MLP_BK, m0, &full[s]);
-            tma_load_2d(sB + s * b_bytes, &tmB, kbeg + kb * MLP_BK, n0, &full[s]);
-            issued = kb + 1;
+        int gk = 0;
+        for (int t = blockIdx.x; t < ntiles && !*abort; t += gridDim.x) {
+            const int kz = t / (tiles_m * tiles_n), r = t - kz * tiles_m * tiles_n;
+            const int m0 = (r % tiles_m) * MLP_BM, n0 = (r / tiles_m) * BN;
+            const int kbeg = kz * g.kchunk;
+            for (int kb = 0; kb < nk; kb++, gk++) {
+                const int s = gk % NS;
+                if (!mbar_wait(&empty[s], ((gk / NS) & 1) ^ 1, abort)) break;
+                mbar_expect_tx(&full[s], a_bytes + b_bytes);
+                tma_load_2d(sA + s * a_bytes, &tmA, kbeg + kb * MLP_BK, m0, &full[s]);
+                tma_load_2d(sB + s * b_bytes, &tmB, kbeg + kb * MLP_BK, n0, &full[s]);
+            }
         }
         // copies still in flight complete before the CTA may exit
-        for (int kb = (issued > NS ? issued - NS : 0); kb < issued; kb++) {
+        for (int k = (gk > NS ? gk - NS : 0); k < gk; k++) {
             for (uint32_t i = 0; i < BT_WAIT_LIMIT; i++)
-                if (bt_mbar_try_wait(&full[kb % NS], (kb / NS) & 1)) break;
+                if (bt_mbar_try_wait(&full[k % NS], (k / NS) & 1)) break;
         }
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
         const uint32_t idesc = mma_idesc(BN);
-        for (int kb = 0; kb < nk; kb++) {
-            const int s = kb % NS;
-            if (!mbar_wait(&full[s], (kb / NS) & 1, abort)) break;
+        int gk = 0, it = 0;
+        for (int t = blockIdx.x; t < ntiles && !*abort; t += gridDim.x, it++) {
+            const int b = it & 1;
+            if (!mbar_wait(&acc_empty[b], ((it >> 1) & 1) ^ 1, abort)) break;
             tc_fence_after();
-            const uint32_t a0 = bt_smem_addr(sA + s * a_bytes), b0 = bt_smem_addr(sB + s * b_bytes);
+            const uint32_t d = tmem + (uint32_t)(b * BN);
+            bool ok = true;
+            for (int kb = 0; kb < nk; kb++, gk++) {
+                const int s = gk % NS;
+                if (!mbar_wait(&full[s], (gk / NS) & 1, abort)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t a0 = bt_smem_addr(sA + s * a_bytes), b0 = bt_smem_addr(sB + s * b_bytes);
 #pragma unroll
-            for (int k = 0; k < MLP_BK / 16; k++)
-                mma_bf16(tmem, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), idesc, (kb > 0 || k > 0) ? 1u : 0u);
-            mma_commit(&empty[s]);
+                for (int k = 0; k < MLP_BK / 16; k++)
+                    mma_bf16(d, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), idesc, (kb > 0 || k > 0) ? 1u : 0u);
+                mma_commit(&empty[s]);
+            }
+            if (!ok) break;
+            mma_commit(&acc_full[b]);
         }
         // completes once every MMA issued above has finished
         mma_commit(&done);
-    }
-    __syncwarp();
-    // epilogue: all threads; the decision to store is uniform over the CTA
-    mbar_wait(&done, 0, abort);
-    __syncthreads();
-    const bool ok = !*abort;
-    tc_fence_after();
-    if (ok) {
-        const int wq = warp & 3;
-        const int row = wq * 32 + lane;
-        const int m = m0 + row;
-        const uint32_t trow = tmem + ((uint32_t)(wq * 32) << 16);
-        const int c0 = (warp >> 2) * (BN / 2);
-        for (int c = c0; c < c0 + BN / 2; c += 32) {
-            float v[32];
-            tmem_ld32(trow + (uint32_t)c, v);
-            const int nb = n0 + c;
-            if (g.mode == MLP_EPI_F32) {
-                float* o = g.out32 + (size_t)kz * g.M * g.N + (size_t)m * g.N + nb;
+    } else if (warp >= MLP_EPI_WARP0) {
+        // epilogue: warp w reads TMEM lanes 32 (w % 4).. and half (w - 4) / 4 of the columns
+        const int q = warp & 3, half = (warp - MLP_EPI_WARP0) >> 2;
+        int it = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
+            const int b = it & 1;
+            if (!mbar_wait(&acc_full[b], (it >> 1) & 1, abort)) break;
+            tc_fence_after();
+            const int kz = t / (tiles_m * tiles_n), r = t - kz * tiles_m * tiles_n;
+            const int m0 = (r % tiles_m) * MLP_BM, n0 = (r / tiles_m) * BN;
+            const int m = m0 + q * 32 + lane;
+            const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
+            const int c0 = half * (BN / 2);
+            for (int c = c0; c < c0 + BN / 2; c += 32) {
+                float v[32];
+                tmem_ld32(trow + (uint32_t)c, v);
+                const int nb = n0 + c;
+                if (g.mode == MLP_EPI_F32) {
+                    float* o = g.out32 + (size_t)kz * g.M * g.N + (size_t)m * g.N + nb;
 #pragma unroll
-                for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(o + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
-            } else if (g.mode == MLP_EPI_BIAS) {
-                float* o = g.out32 + (size_t)m * g.N + nb;
+                    for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(o + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                } else if (g.mode == MLP_EPI_BIAS) {
+                    float* o = g.out32 + (size_t)m * g.N + nb;
 #pragma unroll
-                for (int i = 0; i < 32; i += 4)
-                    *reinterpret_cast<float4*>(o + i) = make_float4(v[i] + g.bias[nb + i], v[i + 1] + g.bias[nb + i + 1],
-                                                                    v[i + 2] + g.bias[nb + i + 2], v[i + 3] + g.bias[nb + i + 3]);
-            } else {
-                float h[32];
-                if (g.mode == MLP_EPI_GELU) {
-                    float* zs = g.zs + (size_t)m * g.N + nb;
+                    for (int i = 0; i < 32; i += 4)
+                        *reinterpret_cast<float4*>(o + i) = make_float4(v[i] + g.bias[nb + i], v[i + 1] + g.bias[nb + i + 1],
+                                                                        v[i + 2] + g.bias[nb + i + 2], v[i + 3] + g.bias[nb + i + 3]);
+                } else {
+                    float h[32];
+                    if (g.mode == MLP_EPI_GELU) {
 #pragma unroll
-                    for (int i = 0; i < 32; i++) {
-                        const float z = v[i] + g.bias[nb + i];
-                        v[i] = z;
-                        h[i] = gelu_f(z);
+                        for (int i = 0; i < 32; i++) {
+                            const float z = v[i] + g.bias[nb + i];
+                            v[i] = z;
+                            h[i] = gelu_f(z);
+                        }
+                        if (g.zs) {
+                            float* zs = g.zs + (size_t)m * g.N + nb;
+#pragma unroll
+                            for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(zs + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                        }
+                    } else {  // MLP_EPI_DGELU
+                        const float* zs = g.zs + (size_t)m * g.N + nb;
+#pragma unroll
+                        for (int i = 0; i < 32; i++) h[i] = v[i] * dgelu_f(zs[i]);
                     }
-                    if (zs) {
+                    __nv_bfloat16* o = g.h16 + (size_t)m * g.N + nb;
 #pragma unroll
-                        for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(zs + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                    for (int i = 0; i < 32; i += 8) {
+                        __align__(16) __nv_bfloat162 p[4];
+#pragma unroll
+                        for (int k = 0; k < 4; k++) p[k] = __floats2bfloat162_rn(h[i + 2 * k], h[i + 2 * k + 1]);
+                        *reinterpret_cast<uint4*>(o + i) = *reinterpret_cast<uint4*>(p);
                     }
-                } else {  // MLP_EPI_DGELU
-                    const float* zs = g.zs + (size_t)m * g.N + nb;
+                    if (g.h16t) {
 #pragma unroll
-                    for (int i = 0; i < 32; i++) h[i] = v[i] * dgelu_f(zs[i]);
-                }
-                __nv_bfloat16* o = g.h16 + (size_t)m * g.N + nb;
-#pragma unroll
-                for (int i = 0; i < 32; i += 8) {
-                    __align__(16) __nv_bfloat162 p[4];
-#pragma unroll
-                    for (int q = 0; q < 4; q++) p[q] = __floats2bfloat162_rn(h[i + 2 * q], h[i + 2 * q + 1]);
-                    *reinterpret_cast<uint4*>(o + i) = *reinterpret_cast<uint4*>(p);
-                }
-                if (g.h16t) {
-#pragma unroll
-                    for (int i = 0; i < 32; i++) g.h16t[(size_t)(nb + i) * g.M + m] = __float2bfloat16_rn(h[i]);
+                        for (int i = 0; i < 32; i++) g.h16t[(size_t)(nb + i) * g.M + m] = __float2bfloat16_rn(h[i]);
+                    }
                 }
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[b]);
         }
     }
+    __syncwarp();
+    mbar_wait(&done, 0, abort);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(2 * BN)) : "memory");
     }
 }
 
@@ -320,7 +359,7 @@ static bool make_map(CUtensorMap* map, const void* ptr, int rows, int cols, int 
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-static int mlp_stages(int bn) { return bn == 256 ? 2 : 3; }
+static int mlp_stages(int bn) { return 4; }
 
 size_t bt_mlp_gemm_smem(int bn) {
     return 1024 + (size_t)mlp_stages(bn) * (MLP_BM * MLP_BK * 2 + (size_t)bn * MLP_BK * 2);
@@ -345,7 +384,8 @@ cudaError_t bt_launch_mlp_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, c
         if (e != cudaSuccess) return e;
         attr_set = 1;
     }
-    dim3 grid(a.M / MLP_BM, a.N / a.bn, splitk);
+    const long long ntiles = (long long)(a.M / MLP_BM) * (a.N / a.bn) * splitk;
+    const int grid = (int)(ntiles < bt_sm_count() ? ntiles : bt_sm_count());
     k_mlp_gemm<<<grid, MLP_THREADS, smem, stream>>>(ta, tb, g);
     return cudaGetLastError();
 }
