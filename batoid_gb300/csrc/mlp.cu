@@ -22,7 +22,7 @@
 // Epilogues (per element (m, n) of the tile):
 //   F32      out32[kz][m][n] = acc                       (split-K partials)
 //   BIAS     out32[m][n]     = acc + bias[n]             (output layer)
-//   GELU     z = acc + bias[n]; zs[m][n] = z;  h = gelu(z);
+//   GELU     z = acc + bias[n]; zs[m][n] = z;  h = gelu(z) (tanh form);
 //            h16[m][n] = h16T[n][m] = bf16(h)             (hidden layers)
 //   DGELU    g = acc * gelu'(zs[m][n]);
 //            h16[m][n] = h16T[n][m] = bf16(g)             (backward)
@@ -135,10 +135,21 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// GELU (erf form) and its derivative.
-__device__ __forceinline__ float gelu_f(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+// GELU, tanh form: 0.5 z (1 + tanh(s (z + 0.044715 z^3))), s = sqrt(2/pi),
+// with the hardware tanh approximation (one MUFU op); and its derivative.
+__device__ __forceinline__ float tanh_fast(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float gelu_f(float z) {
+    const float u = 0.7978845608028654f * fmaf(0.044715f * z, z * z, z);
+    return 0.5f * z * (1.0f + tanh_fast(u));
+}
 __device__ __forceinline__ float dgelu_f(float z) {
-    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * __expf(-0.5f * z * z);
+    const float z2 = z * z;
+    const float t = tanh_fast(0.7978845608028654f * fmaf(0.044715f * z, z2, z));
+    return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * 0.7978845608028654f * fmaf(0.134145f, z2, 1.0f);
 }
 
 // ---------------------------------------------------------------------------

@@ -364,7 +364,7 @@ def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24,
     threads, ctas = batch_config(pt)
     F = len(BATCH_FIELDS)
     t1 = time.perf_counter()
-    dofs, widx = sur.sample_states((train_samples + F - 1) // F, seed=101, widen=1.5)
+    dofs, widx = sur.sample_states((train_samples + F - 1) // F, seed=101)
     coefs = sur.trace(dofs, widx, threads=threads, ctas_per_sm=ctas)
     datagen_s = time.perf_counter() - t1
     feat, grp, w = sur.features(dofs, widx)
@@ -438,6 +438,14 @@ def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24,
     # the largest surrogate errors: is the batched truth right there?  Recompute
     # those samples with the CPU oracle of batoid.zernike
     worst = np.argsort(-e_raw)[:4]
+    above = np.flatnonzero(e_fin > threshold_nm)
+    zmax = np.max(np.abs(hd / sur.dof_scale), axis=1)
+    tail_profile = {"count": int(len(above)),
+                    "fields": np.bincount(above % F, minlength=F).tolist(),
+                    "wavelength_nm": np.bincount(hw[above // F], minlength=len(W.WAVELENGTHS)).tolist(),
+                    "median_max_abs_dof_z": float(np.median(zmax[above // F])) if len(above) else None,
+                    "median_max_abs_dof_z_all": float(np.median(zmax)),
+                    "distinct_states": int(len(np.unique(above // F)))}
     outliers = []
     try:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -462,8 +470,7 @@ def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24,
     infer_tflops = flops_fwd * N / (infer_ms * 1e-3) / 1e12
     out_d = {
         "workload": f"MLP 33 -> 4x512 GELU -> 28 + error head, bf16/fp32-accumulate tcgen05 kernels; trained on "
-                    f"{len(feat)} (state, field) samples of the 4096-state generator (nx 32; dof ranges widened "
-                    f"1.5x for training), evaluated on "
+                    f"{len(feat)} (state, field) samples of the 4096-state generator (nx 32), evaluated on "
                     f"{N} held-out samples vs the batched trace",
         "wavefronts_per_s_with_fallback": N / ((infer_ms + fb_ms) * 1e-3),
         "wavefronts_per_s_surrogate_only": N / (infer_ms * 1e-3),
@@ -481,6 +488,7 @@ def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24,
                                "note": "whole inference pipeline (pack, 5 GEMMs, combine) over its event time"},
         "gpu_launches_per_inference": 7,
         "largest_errors": outliers,
+        "above_threshold_profile": tail_profile,
     }
     return out_d
 

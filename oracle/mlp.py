@@ -12,7 +12,6 @@ sum_j w_j (y_j - t_j)^2 over the target columns, plus err_weight times the
 squared error of the error column against log ||y - t|| (detached).
 """
 import numpy as np
-from scipy.special import erf
 
 
 def bf16(a):
@@ -23,12 +22,17 @@ def bf16(a):
     return r.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
+S2PI = np.sqrt(2.0 / np.pi)
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + erf(z / np.sqrt(2.0)))
+    """GELU, tanh form: 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3)))."""
+    return 0.5 * z * (1.0 + np.tanh(S2PI * (z + 0.044715 * z ** 3)))
 
 
 def dgelu(z):
-    return 0.5 * (1.0 + erf(z / np.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / np.sqrt(2.0 * np.pi)
+    t = np.tanh(S2PI * (z + 0.044715 * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * S2PI * (1.0 + 3 * 0.044715 * z * z)
 
 
 def forward(x16, Ws, bs):

@@ -20,12 +20,16 @@ def _gemm(A, B, M, N, K, bn, mode, splitk=1, bias=None, out32=None, zs=None, h16
     torch.cuda.synchronize()
 
 
+S2PI = np.sqrt(2.0 / np.pi)
+
+
 def _gelu(z):
-    return 0.5 * z * (1 + torch.erf(z / np.sqrt(2.0)))
+    return 0.5 * z * (1 + torch.tanh(S2PI * (z + 0.044715 * z ** 3)))
 
 
 def _dgelu(z):
-    return 0.5 * (1 + torch.erf(z / np.sqrt(2.0))) + z * torch.exp(-0.5 * z * z) / np.sqrt(2 * np.pi)
+    t = torch.tanh(S2PI * (z + 0.044715 * z ** 3))
+    return 0.5 * (1 + t) + 0.5 * z * (1 - t * t) * S2PI * (1 + 3 * 0.044715 * z * z)
 
 
 @pytest.mark.parametrize("N,bn", [(256, 128), (512, 256)])
