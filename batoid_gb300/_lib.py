@@ -30,6 +30,7 @@ BT_ERR_ALLOC = 6
 STAGE_INTERSECT = 0
 STAGE_REFLECT = 1
 STAGE_REFRACT = 2
+STAGE_SCREEN = 4
 
 
 class BtRayVector(ctypes.Structure):
@@ -131,6 +132,7 @@ _SIGS = [
     ("bt_apply_reverse_transform_arrays", c_int, [_D3, _D3, _P, _P, _P, c_size_t, c_int, _P]),
     ("bt_finish_parallel", c_int, [_D3, _D3, _D3, _P, _P, _P, c_size_t, _P]),
     ("bt_obscure", c_int, [_P, ctypes.POINTER(BtRayVector), c_int, _P]),
+    ("bt_refract_screen", c_int, [_P, _D3, _D3, _P, ctypes.POINTER(BtRayVector), c_int, c_int, _P]),
     ("bt_rsplit", c_int, [_P, _D3, _D3, _P, _P, _P, ctypes.POINTER(BtRayVector), ctypes.POINTER(BtRayVector), c_int,
                           c_int, _P]),
     ("bt_intersect", c_int, [_P, _D3, _D3, ctypes.POINTER(BtRayVector), _P, c_int, c_int, _P]),
@@ -147,6 +149,8 @@ _SIGS = [
                             ctypes.POINTER(c_int), _P]),
     ("bt_optic_create", c_int, [c_size_t, ctypes.POINTER(c_int), _PP, c_double_p, c_double_p, _PP, _PP,
                                 _PP, _PP]),
+    ("bt_optic_create_ex", c_int, [c_size_t, ctypes.POINTER(c_int), _PP, c_double_p, c_double_p, _PP, _PP,
+                                   _PP, _PP, _PP]),
     ("bt_optic_destroy", None, [_P]),
     ("bt_optic_nstages", c_int, [_P, ctypes.POINTER(c_int)]),
     ("bt_optic_trace", c_int, [_P, ctypes.POINTER(BtRayVector), c_int, _P]),

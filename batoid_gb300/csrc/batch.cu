@@ -258,7 +258,7 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
     double* pool = reinterpret_cast<double*>(smem + hdr->off_pool);
     BatchSmem L = bt_batch_smem_layout(blob_bytes, T, J);
     double* mc = reinterpret_cast<double*>(smem + L.mc);
-    double* bsum = reinterpret_cast<double*>(smem + L.bacc);  // [nwarps][32]
+    double* opdbuf = A.scratch + (size_t)blockIdx.x * A.scratch_stride;  // this block's per-ray OPD (NaN: vignetted)
     double* gcorr = reinterpret_cast<double*>(smem + L.gcorr);
     double* zv = reinterpret_cast<double*>(smem + L.zv) + warp * 32;
     double* G = reinterpret_cast<double*>(smem + L.G);
@@ -308,7 +308,6 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
             }
         }
         mcell[tid] = -1;
-        double bj = 0.0;  // lane j < J: this warp's share of (B^T v)_j
         for (int e = lane; e < NT; e += 32) gw[e] = 0.0;
         __syncthreads();
 
@@ -337,22 +336,44 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
                 __syncthreads();  // reference frame and t0 visible to all
                 continue;
             }
-            bool valid = false, inref = false;
-            double opd = 0.0;
-            if (active) {
-                valid = !r.vig;
-                inref = bt_in_annulus(gx, gy, A.r_in2, A.r_out2);
-                if (valid) opd = (s_t0 - r.t) / wl;
-            }
-            // B^T v: lane j accumulates sum_k Z_j(ray k) opd_k over the warp's
-            // 32 rays (a row of the basis table per lane, contiguous in k)
-            {
-                const int wbase = base + warp * 32;
-                const double* zrow = Z + (size_t)(lane < J ? lane : 0) * nray;
-                for (int k = 0; k < 32; k++) {
-                    const double ok = __shfl_sync(0xffffffffu, opd, k);
-                    if (lane < J && ok != 0.0) bj += __ldg(zrow + wbase + k) * ok;
+            if (active) opdbuf[i] = r.vig ? (double)NAN : (s_t0 - r.t) / wl;
+        }
+        __syncthreads();
+        // B^T v: warp w sums rows j = w, w + nwarps, ... of Z^T opd, every
+        // lane over points i = lane, lane + 32, ... (independent accumulators)
+        {
+            const int nj = (J - warp + nwarps - 1) / nwarps;  // rows of this warp
+            for (int q0 = 0; q0 < nj; q0 += 8) {
+                double acc[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++) acc[q] = 0.0;
+                for (int i = lane; i < nray; i += 32) {
+                    const double o = opdbuf[i];
+                    if (o == o) {
+#pragma unroll
+                        for (int q = 0; q < 8; q++)
+                            if (q0 + q < nj) acc[q] += __ldg(Z + (size_t)(warp + (q0 + q) * nwarps) * nray + i) * o;
+                    }
                 }
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    if (q0 + q < nj) {
+                        const double v = bt_warp_sum(acc[q]);
+                        if (lane == 0) bv[warp + (q0 + q) * nwarps] = v;
+                    }
+                }
+            }
+        }
+        // vignetting that disagrees with the fit annulus corrects G_ref
+        for (int base = 0; base < nray; base += T) {
+            const int i = base + tid;
+            bool valid = false, inref = false;
+            if (i < nray) {
+                double gx, gy;
+                bt_grid_point(nx, i, A.pupil, &gx, &gy);
+                const double o = opdbuf[i];
+                valid = (o == o);
+                inref = bt_in_annulus(gx, gy, A.r_in2, A.r_out2);
             }
             unsigned mm = __ballot_sync(0xffffffffu, valid != inref);
             while (mm) {
@@ -366,14 +387,7 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
                 bt_gram_update(gw, zv, sign, lane, NT);
             }
         }
-        bsum[warp * 32 + lane] = bj;
         __syncthreads();
-        // B^T v
-        for (int j = tid; j < J; j += T) {
-            double acc = 0.0;
-            for (int w = 0; w < nwarps; w++) acc += bsum[w * 32 + j];
-            bv[j] = acc;
-        }
         // B^T B
         const double* GR = A.gref + (size_t)nx * J * J;
         for (int e = tid; e < NT; e += T) {

@@ -11,6 +11,8 @@
 #define BT_BATCH_MAX_VAR 8
 #define BT_BATCH_MAX_NX 512
 #define BT_BATCH_MAX_SMEM (227 * 1024)
+// most resident blocks per SM the OPD scratch is sized for
+#define BT_BATCH_MAX_CTAS_PER_SM 8
 // A Cholesky pivot at or below this fraction of the largest diagonal entry
 // of B^T B marks the fit rank-deficient.
 #define BT_BATCH_PIVOT_TOL 1e-12
@@ -32,6 +34,8 @@ struct BatchArgs {
     const long long* basis_off;   // [nx_cap + 1], -1 where absent
     const double* gref;           // [nx_cap + 1][jmax][jmax]
     // schedule and outputs
+    double* scratch;        // per block: OPD of every ray of its current job
+    long long scratch_stride;  // doubles per block (>= the largest nx * nx)
     const int* order;   // [njobs] job ids (s * nfields + f) in scheduling order
     int* counter;       // queue head, zeroed before each launch
     double* coefs;      // [njobs][jmax + 1]
@@ -65,8 +69,7 @@ __host__ __device__ inline BatchSmem bt_batch_smem_layout(int blob_bytes, int T,
     size_t off = ((size_t)blob_bytes + 127) & ~(size_t)127;
     L.mc = off;
     off += (size_t)16 * T * sizeof(double);
-    L.bacc = off;  // per-warp partial sums of B^T v
-    off += (size_t)(T / 32) * 32 * sizeof(double);
+    L.bacc = off;  // unused
     L.gcorr = off;
     off += (size_t)(T / 32) * (J * (J + 1) / 2) * sizeof(double);
     L.zv = off;

@@ -104,7 +104,8 @@ enum bt_stage_kind {
     BT_ST_INTERSECT = 0,  // Detector / Baffle / plain Interface
     BT_ST_REFLECT = 1,    // Mirror
     BT_ST_REFRACT = 2,    // RefractiveInterface
-    BT_ST_OBSCURE = 3     // obscuration only (no transform, no surface)
+    BT_ST_OBSCURE = 3,    // obscuration only (no transform, no surface)
+    BT_ST_SCREEN = 4      // OPDScreen: intersect, deflect by the screen's gradient
 };
 
 typedef struct bt_stage {
@@ -115,7 +116,7 @@ typedef struct bt_stage {
     int32_t obsc_end;
     int32_t identity;    // 1: dr == 0 and drot == I; 2: drot == I (translation); 0: general
     int32_t coated;      // 1: multiply flux by coat_r (reflect) / coat_t
-    int32_t pad_;
+    int32_t screen;      // screen: root descriptor of the OPD surface, else -1
     double dr[3];
     double drot[9];      // column-major, as the reference passes it
     double coat_r;

@@ -838,22 +838,14 @@ __device__ __forceinline__ void bt_leaf_newton_eval(const bt_surf& s, const doub
         *uy = -f_horner2d(fx, fy, c + nx * ny + g, nx - 1, ny - 1);
         return;
     }
-    case BT_S_BICUBIC: {
-        double z = 0.0, gx = 0.0, gy = 0.0;
-        if (!bt_table_eval(s, x, y, &z, &gx, &gy, true, true)) {
-            const double fill = (s.p[4] != 0.0) ? (double)NAN : 0.0;
-            z = fill; gx = fill; gy = fill;
-        }
+    default: {
+        double z, gx, gy;
+        bt_leaf_eval(s, pool, x, y, true, true, &z, &gx, &gy);
         *sag = z;
-        *ux = (float)(-gx);
-        *uy = (float)(-gy);
+        *ux = (float)gx;
+        *uy = (float)gy;
         return;
     }
-    default:
-        *sag = NAN;
-        *ux = NAN;
-        *uy = NAN;
-        return;
     }
 }
 
@@ -918,33 +910,11 @@ __device__ __forceinline__ void bt_leaf_slope_precise(const bt_surf& s, const do
         *uy = -ff_to_double(ff_horner2d(xf, yf, c + nx * ny + g, nx - 1, ny - 1));
         return;
     }
-    case BT_S_PLANE:
-        *ux = 0.0;
-        *uy = 0.0;
-        return;
-    case BT_S_TILTED:
-        *ux = -s.p[0] / s.p[2];
-        *uy = -s.p[1] / s.p[2];
-        return;
-    case BT_S_PARABOLOID:
-        if (s.p[0] == 0.0) { *ux = 0.0; *uy = 0.0; return; }
-        *ux = -x * s.p[1];
-        *uy = -y * s.p[1];
-        return;
-    case BT_S_BICUBIC: {
-        double z = 0.0, gx = 0.0, gy = 0.0;
-        if (!bt_table_eval(s, x, y, &z, &gx, &gy, false, true)) {
-            const double fill = (s.p[4] != 0.0) ? (double)NAN : 0.0;
-            gx = fill; gy = fill;
-        }
-        *ux = -gx;
-        *uy = -gy;
+    default: {
+        double z;
+        bt_leaf_eval(s, pool, x, y, false, true, &z, ux, uy);
         return;
     }
-    default:
-        *ux = NAN;
-        *uy = NAN;
-        return;
     }
 }
 
@@ -1080,21 +1050,11 @@ __device__ __forceinline__ bool bt_leaf_tti_fast(const Prog& P, int si, double x
     case BT_S_BICUBIC:
     case BT_S_MODAL:
         return bt_newton_mixed(P, si, x, y, z, vx, vy, vz, dt, niter);
-    case BT_S_PLANE:
-        // src/plane.cpp:23-30
-        if (vz == 0) return false;
-        dt = -z / vz;
-        return true;
-    case BT_S_TILTED: {
-        // src/tilted.cpp:29-37
-        const double num = z - x * s.p[0] - y * s.p[1];
-        const double den = vx * s.p[0] + vy * s.p[1] - vz;
-        if (den == 0) return false;
-        dt = num / den;
-        return true;
+    default: {
+        double ux, uy;
+        bool slope_ok;
+        return bt_leaf_tti(P, si, x, y, z, vx, vy, vz, dt, niter, &ux, &uy, &slope_ok);
     }
-    default:
-        return false;
     }
 }
 

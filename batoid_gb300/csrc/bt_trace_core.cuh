@@ -23,6 +23,44 @@ __device__ __forceinline__ void store_ray(const RV& o, long long i, const RaySta
     o.fail[i] = r.fail;
 }
 
+// Phase screen (src/batoid.cpp:677-810): the direction cosines relative to
+// an orthonormal basis around the surface normal change by the screen's
+// gradient; the screen's sag adds to the time.  Out of line: only OPDScreen
+// stages reach it.
+static __device__ __noinline__ void bt_screen_deflect(const Prog P, int surf, int screen, double x, double y,
+                                                      double* vx, double* vy, double* vz, double* t) {
+    const double norm = sqrt(*vx * *vx + *vy * *vy + *vz * *vz);
+    const double norm_inv = 1 / norm;
+    double e3x, e3y, e3z;
+    bt_normal_precise(P, surf, x, y, &e3x, &e3y, &e3z);
+    const double e1norm = sqrt(e3z * e3z + e3x * e3x);
+    const double e1x = e3z / e1norm, e1y = 0, e1z = -e3x / e1norm;
+    const double e2x = e3y * e1z - e3z * e1y;
+    const double e2y = e3z * e1x - e3x * e1z;
+    const double e2z = e3x * e1y - e3y * e1x;
+    double cos1 = *vx * norm_inv * e1x + *vy * norm_inv * e1y + *vz * norm_inv * e1z;
+    double cos2 = *vx * norm_inv * e2x + *vy * norm_inv * e2y + *vz * norm_inv * e2z;
+    double cos3 = *vx * norm_inv * e3x + *vy * norm_inv * e3y + *vz * norm_inv * e3z;
+    double sag, ux, uy;
+    bt_surf_eval(P, screen, x, y, true, true, &sag, &ux, &uy);
+    const double dPdx = -ux, dPdy = -uy;
+    const double dPd1 = dPdx * e1x + dPdy * e1y;
+    const double dPd2 = dPdx * e2x + dPdy * e2y;
+    if (cos3 < 0) {
+        cos1 += dPd1;
+        cos2 += dPd2;
+        cos3 = -sqrt(1 - cos1 * cos1 - cos2 * cos2);
+    } else {
+        cos1 -= dPd1;
+        cos2 -= dPd2;
+        cos3 = sqrt(1 - cos1 * cos1 - cos2 * cos2);
+    }
+    *vx = cos1 * norm * e1x + cos2 * norm * e2x + cos3 * norm * e3x;
+    *vy = cos1 * norm * e1y + cos2 * norm * e2y + cos3 * norm * e3y;
+    *vz = cos1 * norm * e1z + cos2 * norm * e2z + cos3 * norm * e3z;
+    *t += sag;
+}
+
 // One stage of the trace for one ray.  Semantics of src/batoid.cpp:175-506:
 // failed rays are skipped and keep their coordinates in the previous frame;
 // a ray that misses the surface is flagged failed+vignetted and likewise
@@ -54,9 +92,11 @@ __device__ __forceinline__ void run_stage(const Prog& P, const bt_stage& st, Ray
             x += vx * dt;
             y += vy * dt;
             z += vz * dt;
-            const double t = r.t + dt;
+            double t = r.t + dt;
             if (st.kind == BT_ST_INTERSECT) {
                 if (st.coated) r.f *= st.coat_t;
+            } else if (st.kind == BT_ST_SCREEN) {
+                bt_screen_deflect(P, st.surf, st.screen, x, y, &vx, &vy, &vz, &t);
             } else {
                 double nx, ny, nz;
                 bt_normal_precise(P, st.surf, x, y, &nx, &ny, &nz);

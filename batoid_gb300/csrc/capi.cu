@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 #include <mutex>
+#include <algorithm>
 #include "../../include/batoid_gb300.h"
 #include "bt_internal.h"
 #include "bt_batch.h"
@@ -559,6 +560,7 @@ static bt_stage blank_stage(int kind) {
     st.kind = kind;
     st.surf = -1;
     st.medium = -1;
+    st.screen = -1;
     st.obsc_begin = 0;
     st.obsc_end = 0;
     st.identity = 1;
@@ -629,7 +631,8 @@ static int run_single(const ProgBuilder& pb, const bt_rayvector* rv, int niter, 
 }
 
 static int surface_op(int kind, const bt_surface* s, const double* dr, const double* drot, const bt_medium_h* m2,
-                      const bt_rayvector* rv, const bt_coating* coating, int niter, void* stream, const char* what) {
+                      const bt_rayvector* rv, const bt_coating* coating, int niter, void* stream, const char* what,
+                      const bt_surface* screen = nullptr) {
     if (!s) return fail(BT_ERR_ARG, std::string(what) + ": null surface");
     int rc = check_rv(rv);
     if (rc != BT_OK) return rc;
@@ -644,6 +647,11 @@ static int surface_op(int kind, const bt_surface* s, const double* dr, const dou
     if (kind == BT_ST_REFRACT) {
         if (!m2) return fail(BT_ERR_ARG, "refract: null medium");
         st.medium = pb.add_medium(m2);
+    }
+    if (kind == BT_ST_SCREEN) {
+        if (!screen) return fail(BT_ERR_ARG, "refractScreen: null screen");
+        st.screen = pb.add_surface(screen);
+        if (st.screen < 0) return BT_ERR_CUDA;
     }
     if (coating) {
         st.coated = 1;
@@ -672,6 +680,13 @@ extern "C" int bt_refract(const bt_surface* s, const double dr[3], const double 
     (void)max_threads;
     (void)m1;  // n1 comes from |v| (src/batoid.cpp:454-458)
     return surface_op(BT_ST_REFRACT, s, dr, drot, m2, rv, coating, niter, stream, "refract");
+}
+
+extern "C" int bt_refract_screen(const bt_surface* s, const double dr[3], const double drot[9],
+                                 const bt_surface* screen, const bt_rayvector* rv, int max_threads, int niter,
+                                 void* stream) {
+    (void)max_threads;
+    return surface_op(BT_ST_SCREEN, s, dr, drot, nullptr, rv, nullptr, niter, stream, "refractScreen", screen);
 }
 
 extern "C" int bt_rsplit(const bt_surface* s, const double dr[3], const double drot[9], const bt_medium_h* m1,
@@ -932,23 +947,40 @@ struct bt_optic {
     cudaEvent_t done[2] = {nullptr, nullptr};
 };
 
+extern "C" int bt_optic_create_ex(size_t nstages, const int* kinds, const bt_surface* const* surfaces,
+                                  const double* dr, const double* drot, const bt_medium_h* const* media,
+                                  const bt_obscuration* const* obscurations, const bt_coating* const* coatings,
+                                  const bt_surface* const* screens, bt_optic** out);
+
 extern "C" int bt_optic_create(size_t nstages, const int* kinds, const bt_surface* const* surfaces, const double* dr,
                                const double* drot, const bt_medium_h* const* media,
                                const bt_obscuration* const* obscurations, const bt_coating* const* coatings,
                                bt_optic** out) {
+    return bt_optic_create_ex(nstages, kinds, surfaces, dr, drot, media, obscurations, coatings, nullptr, out);
+}
+
+extern "C" int bt_optic_create_ex(size_t nstages, const int* kinds, const bt_surface* const* surfaces,
+                                  const double* dr, const double* drot, const bt_medium_h* const* media,
+                                  const bt_obscuration* const* obscurations, const bt_coating* const* coatings,
+                                  const bt_surface* const* screens, bt_optic** out) {
     if (!out) return fail(BT_ERR_ARG, "optic: null output");
     if (nstages > BT_MAX_STAGES) return fail(BT_ERR_UNSUPPORTED, "optic: too many stages");
     if (nstages > 0 && (!kinds || !surfaces || !dr || !drot)) return fail(BT_ERR_ARG, "optic: null stage arrays");
     ProgBuilder pb;
     for (size_t k = 0; k < nstages; k++) {
         const int kind = kinds[k];
-        if (kind != BT_ST_INTERSECT && kind != BT_ST_REFLECT && kind != BT_ST_REFRACT)
+        if (kind != BT_ST_INTERSECT && kind != BT_ST_REFLECT && kind != BT_ST_REFRACT && kind != BT_ST_SCREEN)
             return fail(BT_ERR_ARG, "optic: bad stage kind");
         if (!surfaces[k]) return fail(BT_ERR_ARG, "optic: null surface");
         bt_stage st = blank_stage(kind);
         set_transform(st, dr + 3 * k, drot + 9 * k);
         st.surf = pb.add_surface(surfaces[k]);
         if (st.surf < 0) return BT_ERR_CUDA;
+        if (kind == BT_ST_SCREEN) {
+            if (!screens || !screens[k]) return fail(BT_ERR_ARG, "optic: screen stage without a screen surface");
+            st.screen = pb.add_surface(screens[k]);
+            if (st.screen < 0) return BT_ERR_CUDA;
+        }
         if (kind == BT_ST_REFRACT) {
             if (!media || !media[k]) return fail(BT_ERR_ARG, "optic: refracting stage without a medium");
             st.medium = pb.add_medium(media[k]);
@@ -1312,6 +1344,8 @@ struct bt_batch {
     double* d_basis = nullptr;
     double* d_gref = nullptr;
     int* d_counter = nullptr;
+    double* d_scratch = nullptr;  // per block: OPD of each ray of its job
+    long long scratch_stride = 0;
     std::mutex mu;
     cudaGraphExec_t gexec = nullptr;
     std::vector<unsigned char> gkey;
@@ -1325,6 +1359,7 @@ static void batch_free(bt_batch* b) {
     if (b->d_basis) cudaFree(b->d_basis);
     if (b->d_gref) cudaFree(b->d_gref);
     if (b->d_counter) cudaFree(b->d_counter);
+    if (b->d_scratch) cudaFree(b->d_scratch);
     delete b;
 }
 
@@ -1520,6 +1555,20 @@ extern "C" int bt_batch_prepare(bt_batch* b, int n, const int* nx_values, void* 
         b->d_basis = nullptr;
         return cuda_fail(e, "batch prepare");
     }
+    // OPD scratch for the largest grid, one slot per block the launch may run
+    long long maxray = 0;
+    for (int nx : list) maxray = std::max(maxray, (long long)nx * nx);
+    if (maxray > b->scratch_stride) {
+        double* sc = nullptr;
+        e = cudaMalloc((void**)&sc, sizeof(double) * (size_t)maxray * bt_sm_count() * BT_BATCH_MAX_CTAS_PER_SM);
+        if (e != cudaSuccess) {
+            cudaFree(basis);
+            return cuda_fail(e, "batch prepare: scratch");
+        }
+        if (b->d_scratch) cudaFree(b->d_scratch);
+        b->d_scratch = sc;
+        b->scratch_stride = maxray;
+    }
     if (b->d_basis) cudaFree(b->d_basis);
     b->d_basis = basis;
     b->off = off;
@@ -1540,7 +1589,8 @@ static int batch_args(bt_batch* b, int nstates, const double* xf, const double* 
     if ((long long)nstates * nfields > 0x7fffffffLL) return fail(BT_ERR_UNSUPPORTED, "batch: too many jobs");
     if (threads < 32 || threads > BT_BATCH_MAX_THREADS || threads % 32 != 0)
         return fail(BT_ERR_ARG, "batch: threads must be 32..128, a multiple of 32");
-    if (ctas_per_sm < 1) return fail(BT_ERR_ARG, "batch: ctas_per_sm must be >= 1");
+    if (ctas_per_sm < 1 || ctas_per_sm > BT_BATCH_MAX_CTAS_PER_SM)
+        return fail(BT_ERR_ARG, "batch: ctas_per_sm must be 1..8");
     if (niter < 0) return fail(BT_ERR_ARG, "batch: negative niter");
     if (bt_batch_smem_layout(b->blob_bytes, threads, b->jmax).total > (size_t)bt_batch_smem_max())
         return fail(BT_ERR_UNSUPPORTED, "batch: shared memory exceeds the limit for this block size");
@@ -1561,6 +1611,8 @@ static int batch_args(bt_batch* b, int nstates, const double* xf, const double* 
     a->gref = b->d_gref;
     a->order = order;
     a->counter = b->d_counter;
+    a->scratch = b->d_scratch;
+    a->scratch_stride = b->scratch_stride;
     a->coefs = coefs;
     a->status = status;
     a->njobs = njobs;

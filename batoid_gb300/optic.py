@@ -93,7 +93,7 @@ def _interaction(iface, reverse):
     if isinstance(iface, RefractiveInterface):
         return _lib.STAGE_REFRACT, (iface.inMedium if reverse else iface.outMedium)
     if isinstance(iface, OPDScreen):
-        raise NotImplementedError("OPDScreen (refractScreen) is not implemented")
+        return _lib.STAGE_SCREEN, None
     return _lib.STAGE_INTERSECT, None
 
 
@@ -109,6 +109,7 @@ class _Program:
         media = (_lib.c_void_p * max(n, 1))()
         obscs = (_lib.c_void_p * max(n, 1))()
         coats = (_lib.c_void_p * max(n, 1))()
+        screens = (_lib.c_void_p * max(n, 1))()
         dr = np.zeros((max(n, 1), 3))
         drot = np.zeros((max(n, 1), 9))
         self._keep = []
@@ -123,7 +124,8 @@ class _Program:
             media[k] = medium._medium.ptr if medium is not None else None
             obscs[k] = iface.obscuration._obsc.ptr if iface.obscuration is not None else None
             coats[k] = None
-            self._keep.append((iface.surface, medium, iface.obscuration))
+            screens[k] = iface.screen._surface.ptr if kind == _lib.STAGE_SCREEN else None
+            self._keep.append((iface.surface, medium, iface.obscuration, getattr(iface, 'screen', None)))
             prev = iface.coordSys
             if forced_key is None:
                 key = iface.name
@@ -138,7 +140,7 @@ class _Program:
         dr = np.ascontiguousarray(dr)
         drot = np.ascontiguousarray(drot)
         # the stage arrays, also used to build batched plans of this optic
-        self.arrays = dict(kinds=kinds, surfs=surfs, dr=dr, drot=drot, media=media, obscs=obscs)
+        self.arrays = dict(kinds=kinds, surfs=surfs, dr=dr, drot=drot, media=media, obscs=obscs, screens=screens)
         self._coats = coats
         self._handle = None
 
@@ -148,7 +150,7 @@ class _Program:
         if self._handle is None:
             a = self.arrays
             self._handle = _make_optic(self.nstages, a["kinds"], a["surfs"], a["dr"], a["drot"], a["media"],
-                                       a["obscs"], self._coats)
+                                       a["obscs"], self._coats, a["screens"])
         return self._handle
 
     def trace(self, rv):
@@ -181,11 +183,11 @@ class _Program:
                                                   D.stream_ptr()))
 
 
-def _make_optic(n, kinds, surfs, dr, drot, media, obscs, coats):
+def _make_optic(n, kinds, surfs, dr, drot, media, obscs, coats, screens=None):
     from ._handle import Handle
-    h = _lib.new_handle(_lib.lib().bt_optic_create, n, kinds, surfs,
+    h = _lib.new_handle(_lib.lib().bt_optic_create_ex, n, kinds, surfs,
                         dr.ctypes.data_as(_lib.c_double_p), drot.ctypes.data_as(_lib.c_double_p),
-                        media, obscs, coats)
+                        media, obscs, coats, screens)
     return Handle(h, "bt_optic_destroy")
 
 
@@ -424,13 +426,19 @@ class Baffle(Interface):
 
 
 class OPDScreen(Interface):
-    """Phase-screen interface.  Its refractScreen interaction is outside the
-    implemented path; constructing one works, tracing through it raises."""
+    """Interface adding an optical path difference (the screen surface's
+    sag, meters) and the matching deflection (batoid/optic.py:867-929)."""
 
     def __init__(self, surface, screen, **kwargs):
         Interface.__init__(self, surface, **kwargs)
         self.screen = screen
         assert self.inMedium == self.outMedium
+
+    def interact(self, rv, reverse=False):
+        return self.surface.refractScreen(rv, self.screen, coordSys=self.coordSys)
+
+    def refract(self, rv, reverse=False):
+        return self.interact(rv, reverse=reverse)
 
 
 class CompoundOptic(Optic):

@@ -62,6 +62,11 @@ class Surface(ABC):
     def refract(self, rv, inMedium, outMedium, coordSys=None, coating=None):
         return refract(self, rv, inMedium, outMedium, coordSys, coating)
 
+    def refractScreen(self, rv, screen, coordSys=None):
+        """Rays through a phase screen on this surface (batoid/surface.py:135-150)."""
+        from .trace import refractScreen
+        return refractScreen(self, rv, screen, coordSys)
+
     def rSplit(self, rv, inMedium, outMedium, coating, coordSys=None):
         """(refracted, reflected) rays (batoid/surface.py:107-133)."""
         from .trace import rSplit

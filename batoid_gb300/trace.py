@@ -103,3 +103,15 @@ def rSplit(surface, rv, inMedium, outMedium, coating, coordSys=None):
     rv.coordSys = coordSys
     rvSplit.coordSys = coordSys
     return rv, rvSplit
+
+
+def refractScreen(surface, rv, screen, coordSys=None):
+    """Intersect, deflect by the screen's OPD gradient, add its OPD to t
+    (batoid/trace.py:139-153; src/batoid.cpp:677-810)."""
+    if coordSys is None:
+        coordSys = rv.coordSys
+    keep, pdr, prot = _ct_args(CoordTransform(rv.coordSys, coordSys))
+    _lib.check(_lib.lib().bt_refract_screen(surface._surface.ptr, pdr, prot, screen._surface.ptr, rv._rv, 1,
+                                            _niter(), D.stream_ptr()))
+    rv.coordSys = coordSys
+    return rv

@@ -150,6 +150,12 @@ int bt_apply_reverse_transform_arrays(const double dr[3], const double drot[9],
                                       int max_threads, void* stream);    /* src/batoid.cpp:24-38 */
 int bt_finish_parallel(const double dr[3], const double drot[9], const double vv[3],
                        double* x, double* y, double* z, size_t n, void* stream); /* src/batoid.cpp:40-69 */
+/* refractScreen(surface, dr, drot, screen, rv, max_threads, niter)
+ * (src/batoid.cpp:677-810; batoid/trace.py:139-153): intersect, then deflect
+ * the direction cosines by the gradient of the screen surface's sag and add
+ * the sag to the time. */
+int bt_refract_screen(const bt_surface* s, const double dr[3], const double drot[9], const bt_surface* screen,
+                      const bt_rayvector* rv, int max_threads, int niter, void* stream);
 /* rSplit(surface, dr, drot, m1, m2, coating, rv, rvSplit, max_threads, niter)
  * (src/batoid.cpp:509-674; pysrc/batoid.cpp): intersect, then the refracted
  * ray replaces rv's ray and the reflected ray is written to rv_split, which
@@ -187,6 +193,7 @@ int bt_rv_equal(const bt_rayvector* a, const bt_rayvector* b, int* out, void* st
 #define BT_STAGE_INTERSECT 0   /* Detector, Baffle, Interface (batoid/optic.py:541-546) */
 #define BT_STAGE_REFLECT 1     /* Mirror (batoid/optic.py:814-816) */
 #define BT_STAGE_REFRACT 2     /* RefractiveInterface (batoid/optic.py:776-781) */
+#define BT_STAGE_SCREEN 4      /* OPDScreen (batoid/optic.py:912-918) */
 /* Packs nstages interfaces, in trace order, into a device-resident program.
  * Per stage: kind, surface, transform from the previous stage's frame
  * (dr 3 doubles, drot 9 doubles column-major), outgoing medium (REFRACT
@@ -195,6 +202,12 @@ int bt_optic_create(size_t nstages, const int* kinds, const bt_surface* const* s
                     const double* dr, const double* drot,
                     const bt_medium_h* const* media, const bt_obscuration* const* obscurations,
                     const bt_coating* const* coatings, bt_optic** out);
+/* Same, with screens[k] the OPD surface of each BT_STAGE_SCREEN stage
+ * (screens may be NULL when no stage is a screen). */
+int bt_optic_create_ex(size_t nstages, const int* kinds, const bt_surface* const* surfaces,
+                       const double* dr, const double* drot,
+                       const bt_medium_h* const* media, const bt_obscuration* const* obscurations,
+                       const bt_coating* const* coatings, const bt_surface* const* screens, bt_optic** out);
 void bt_optic_destroy(bt_optic* o);
 int bt_optic_nstages(const bt_optic* o, int* out);
 /* In-place trace of all stages in one launch (CompoundOptic.trace). */
@@ -320,7 +333,7 @@ int bt_batch_prepare(bt_batch* b, int n, const int* nx_values, void* stream);
  * jobs, order holding each once).  Outputs coefs[job][jmax+1] (waves, entry
  * 0 = 0) and status[job] (0, BT_ERR_ARG for a grid size not prepared,
  * BT_ERR_RANK, -1 if not run).  threads: 32..128, a multiple of 32;
- * ctas_per_sm >= 1.  Stream-ordered. */
+ * ctas_per_sm 1..8.  Stream-ordered. */
 int bt_batch_zernike(bt_batch* b, int nstates, const double* xf, const double* det, const double* amps,
                      const int* nx, const double* wavelength, int nfields, const double* fields,
                      const int* order, int nqueue, double* coefs, int* status, int threads, int ctas_per_sm,

@@ -67,3 +67,22 @@ def rsplit_cases(bt):
         (bt.Asphere(-0.6, -0.5, [1e-3, -2e-4]), glass, air, bt.SimpleCoating(0.1, 0.85), cs, 1 / 1.46),
         (bt.Plane(), glass, air, bt.SimpleCoating(0.04, 0.96), bt.CoordSys(rot=bt.RotX(0.8)), 1 / 1.46),
     ]
+
+
+def screen_cases(bt):
+    """(surface, screen, coordSys) cases for refractScreen."""
+    return [
+        (bt.Plane(), bt.Sphere(5000.0), bt.CoordSys(origin=[0.0, 0.0, 0.05])),
+        (bt.Sphere(2.0), bt.Paraboloid(300.0), bt.CoordSys(origin=[0.01, 0.0, 0.02], rot=bt.RotY(0.05))),
+    ]
+
+
+def screen_optic(bt):
+    """A phase screen between two planes of a two-element system."""
+    CS = bt.CoordSys
+    air = bt.ConstMedium(1.0)
+    return bt.CompoundOptic([
+        bt.OPDScreen(bt.Plane(), bt.Sphere(4000.0), name="S", coordSys=CS(origin=[0, 0, 0.1]), inMedium=air,
+                     outMedium=air),
+        bt.Detector(bt.Plane(), name="D", coordSys=CS(origin=[0, 0, 1.0]), inMedium=air, outMedium=air),
+    ], name="screened", inMedium=air, outMedium=air)

@@ -302,6 +302,10 @@ def split_fixture(batoid):
         a, b = batoid.trace.rSplit(surf, rv, m1, m2, coat, coordSys=cs)
         out.update(rv_to_dict(a, f"rs{c}_refr"))
         out.update(rv_to_dict(b, f"rs{c}_refl"))
+    for c, (surf, screen, cs) in enumerate(S.screen_cases(batoid)):
+        rv = make_rv(batoid, S.rsplit_rays())
+        out.update(rv_to_dict(batoid.trace.refractScreen(surf, rv, screen, coordSys=cs), f"scr{c}"))
+    out.update(rv_to_dict(S.screen_optic(batoid).trace(make_rv(batoid, S.split_rays())), "scr_optic"))
     optic = S.split_optic(batoid)
     fwd, rev = optic.traceSplit(make_rv(batoid, S.split_rays()), minFlux=1e-4)
     for tag, lst in (("F", fwd), ("R", rev)):

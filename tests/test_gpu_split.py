@@ -47,3 +47,17 @@ def test_tracesplit_matches_reference():
     direct = [r for r in fwd if r.path == ["L1_entrance", "L1_exit", "L2_entrance", "L2_exit", "D"]]
     assert len(direct) == 1
     np.testing.assert_allclose(direct[0].flux, 0.98 ** 4, rtol=1e-14)
+
+
+@pytest.mark.parametrize("case", [0, 1])
+def test_refract_screen_matches_reference(case):
+    g = golden("split")
+    surf, screen, cs = S.screen_cases(bt)[case]
+    rv = bt.trace.refractScreen(surf, bt.RayVector(*S.rsplit_rays()), screen, coordSys=cs)
+    _match(rv, g, f"scr{case}")
+
+
+def test_opd_screen_in_fused_optic_trace():
+    g = golden("split")
+    out = S.screen_optic(bt).trace(bt.RayVector(*S.split_rays()))
+    _match(out, g, "scr_optic")
