@@ -18,8 +18,8 @@ import torch
 from . import _device as D
 from . import _lib
 
-DEFAULT = (128, 3)
-CANDIDATES = [(64, 4), (64, 6), (128, 2), (128, 3), (128, 4)]
+DEFAULT = (256, 2)
+CANDIDATES = [(128, 3), (128, 4), (256, 1), (256, 2)]
 _memo = {}
 
 
@@ -48,7 +48,7 @@ def _store(table):
 
 def _key(pt):
     name = torch.cuda.get_device_name(D.device())
-    return (f"{name}|stages={pt.prog.nstages}|var={len(pt.var_stages)}|modes={pt.nmodes}|"
+    return (f"{name}|k2|stages={pt.prog.nstages}|var={len(pt.var_stages)}|modes={pt.nmodes}|"
             f"fields={len(pt.fields)}|jmax={pt.jmax}")
 
 
@@ -81,8 +81,11 @@ def time_config(pt, inp, threads, ctas, reps=2):
     return best
 
 
-def batch_config(pt, nstates=48, force=False):
-    """(threads, ctas_per_sm) for this plan on this device."""
+def batch_config(pt, nstates=384, force=False):
+    """(threads, ctas_per_sm) for this plan on this device.  The sample must
+    give every block many jobs (384 states x 9 fields: ~11 per block at 2
+    blocks per SM); with only one or two jobs per block the makespan is the
+    tail and favours fewer, longer-running blocks."""
     if os.environ.get("BATOID_GB300_AUTOTUNE", "1") == "0":
         return DEFAULT
     key = _key(pt)

@@ -297,7 +297,7 @@ class PerturbedTelescope:
                  order=torch.from_numpy(order).to(D.device()), nstates=S)
         return t
 
-    def launch(self, inp, coefs, status, threads=128, ctas_per_sm=3, niter=None, graph=False, order=None):
+    def launch(self, inp, coefs, status, threads=256, ctas_per_sm=2, niter=None, graph=False, order=None):
         """Stream-ordered launch on device inputs from ``device_inputs``;
         ``order`` (device int32 job ids) runs only those jobs."""
         from .global_vars import _batoid_niter

@@ -323,11 +323,16 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
             const bool active = chief ? (tid == 0) : (i < nray);
             RayState r;
             double gx = 0.0, gy = 0.0;
+            int cm = -1;
+            double cn = 0.0, cin = 0.0;
+            if (active) bt_batch_ray(A, F, nx, i, wl, r, &gx, &gy);
+            // stage-synchronous: all warps of the block run the same stage's
+            // code together (instruction-cache working set of one stage)
+            for (int k = 0; k < A.ntrace; k++) {
+                if (active) run_stage(P, stages[k], r, A.niter, cm, cn, cin);
+                __syncthreads();
+            }
             if (active) {
-                bt_batch_ray(A, F, nx, i, wl, r, &gx, &gy);
-                int cm = -1;
-                double cn = 0.0, cin = 0.0;
-                for (int k = 0; k < A.ntrace; k++) run_stage(P, stages[k], r, A.niter, cm, cn, cin);
                 if (chief) bt_batch_target(A, s, r, sph);
                 bt_sphere_stage(P, sph, r);
             }

@@ -4,9 +4,9 @@
 #include <stdint.h>
 #include <cuda_runtime.h>
 
-#define BT_BATCH_MAX_THREADS 128
+#define BT_BATCH_MAX_THREADS 256
 // resident blocks per SM the register budget is sized for (128 registers)
-#define BT_BATCH_MIN_BLOCKS 4
+#define BT_BATCH_MIN_BLOCKS 2
 #define BT_BATCH_MAX_J 32
 #define BT_BATCH_MAX_VAR 8
 #define BT_BATCH_MAX_NX 512

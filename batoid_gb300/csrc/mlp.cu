@@ -14,7 +14,9 @@
 //     accumulator to the epilogue;
 //   * warps 4..11 read it back with tcgen05.ld (warp w owns TMEM lanes
 //     32(w%4)..32(w%4)+31 = tile rows, and half (w-4)/4 of the columns) and
-//     run the epilogue while the next tile accumulates in the other buffer.
+//     run the epilogue while the next tile accumulates in the other buffer;
+//     bf16 outputs go through a per-warp 32 x 64 staging tile in shared
+//     memory (128-byte swizzle) and leave by TMA store, whole lines at a time.
 // Every wait is bounded: on expiry the CTA records BT_ERR_TIMEOUT in the
 // device status word, stops issuing, waits (bounded) for the copies and
 // MMAs it started, frees its TMEM and returns.
@@ -30,6 +32,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
+#include <string.h>
 #include "bt_internal.h"
 #include "bt_stage_smem.cuh"
 #include "bt_mlp.h"
@@ -40,6 +43,7 @@
 #define MLP_THREADS 384
 #define MLP_EPI_WARP0 4
 #define MLP_NEPI 8
+#define MLP_STG_BYTES (32 * 64 * 2)  // per epilogue warp: 32 rows x 64 bf16 columns
 
 cudaError_t bt_read_mlp_device_status(int* status, cudaStream_t stream) {
     int zero = 0;
@@ -77,6 +81,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
     *abort = 1;
     atomicExch(&bt_dev_status, 5 /* BT_ERR_TIMEOUT */);
     return false;
+}
+
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, const void* src, int x, int y) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];"
+                 ::"l"((uint64_t)map), "r"(x), "r"(y), "r"(bt_smem_addr(src))
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
@@ -160,15 +171,17 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bt_smem_addr(bar)) : "memory");
 }
 
-// Persistent: one CTA per SM walks the tile list (M fastest, so CTAs running
-// together share the weight tile in L2).  Warp 0 lane 0 streams operands
+// Persistent: one CTA per SM walks the tile list (N fastest, so the CTAs
+// running together cover whole row blocks of A: A streams from DRAM once and
+// the small weight operand stays in L2).  Warp 0 lane 0 streams operands
 // into the ring; warp 1 lane 0 issues the MMAs of tile i into TMEM
 // accumulator buffer i % 2; warps 4..11 drain the other buffer (epilogue)
 // meanwhile.  Barriers: full/empty per ring stage, acc_full/acc_empty per
 // accumulator buffer; the first use of each "empty" barrier waits on the
 // phase before the barrier's first, which counts as completed.
 __global__ void __launch_bounds__(MLP_THREADS, 1)
-k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, MlpGemmArgs g) {
+k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+           const __grid_constant__ CUtensorMap tmH, MlpGemmArgs g) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t full[MLP_STAGES];
     __shared__ __align__(8) uint64_t empty[MLP_STAGES];
@@ -185,6 +198,7 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     const uint32_t a_bytes = MLP_BM * MLP_BK * 2, b_bytes = (uint32_t)BN * MLP_BK * 2;
     unsigned char* sA = base;
     unsigned char* sB = base + NS * a_bytes;
+    unsigned char* sStg = base + NS * (a_bytes + b_bytes);  // epilogue staging, MLP_STG_BYTES per warp
     const int tiles_m = g.M / MLP_BM, tiles_n = g.N / BN;
     const int ntiles = tiles_m * tiles_n * (g.K / g.kchunk);
     const int nk = g.kchunk / MLP_BK;
@@ -218,7 +232,7 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
         int gk = 0;
         for (int t = blockIdx.x; t < ntiles && !*abort; t += gridDim.x) {
             const int kz = t / (tiles_m * tiles_n), r = t - kz * tiles_m * tiles_n;
-            const int m0 = (r % tiles_m) * MLP_BM, n0 = (r / tiles_m) * BN;
+            const int m0 = (r / tiles_n) * MLP_BM, n0 = (r % tiles_n) * BN;
             const int kbeg = kz * g.kchunk;
             for (int kb = 0; kb < nk; kb++, gk++) {
                 const int s = gk % NS;
@@ -264,13 +278,15 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     } else if (warp >= MLP_EPI_WARP0) {
         // epilogue: warp w reads TMEM lanes 32 (w % 4).. and half (w - 4) / 4 of the columns
         const int q = warp & 3, half = (warp - MLP_EPI_WARP0) >> 2;
+        unsigned char* stg = sStg + (warp - MLP_EPI_WARP0) * MLP_STG_BYTES;
+        const bool tma_out = (g.mode == MLP_EPI_GELU || g.mode == MLP_EPI_DGELU);
         int it = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
             const int b = it & 1;
             if (!mbar_wait(&acc_full[b], (it >> 1) & 1, abort)) break;
             tc_fence_after();
             const int kz = t / (tiles_m * tiles_n), r = t - kz * tiles_m * tiles_n;
-            const int m0 = (r % tiles_m) * MLP_BM, n0 = (r / tiles_m) * BN;
+            const int m0 = (r / tiles_n) * MLP_BM, n0 = (r % tiles_n) * BN;
             const int m = m0 + q * 32 + lane;
             const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
             const int c0 = half * (BN / 2);
@@ -284,36 +300,62 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
                     for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(o + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
                 } else if (g.mode == MLP_EPI_BIAS) {
                     float* o = g.out32 + (size_t)m * g.N + nb;
+                    const float4* b4 = reinterpret_cast<const float4*>(g.bias + nb);
 #pragma unroll
-                    for (int i = 0; i < 32; i += 4)
-                        *reinterpret_cast<float4*>(o + i) = make_float4(v[i] + g.bias[nb + i], v[i + 1] + g.bias[nb + i + 1],
-                                                                        v[i + 2] + g.bias[nb + i + 2], v[i + 3] + g.bias[nb + i + 3]);
+                    for (int i = 0; i < 32; i += 4) {
+                        const float4 bb = __ldg(b4 + i / 4);
+                        *reinterpret_cast<float4*>(o + i) = make_float4(v[i] + bb.x, v[i + 1] + bb.y, v[i + 2] + bb.z, v[i + 3] + bb.w);
+                    }
                 } else {
                     float h[32];
                     if (g.mode == MLP_EPI_GELU) {
+                        const float4* b4 = reinterpret_cast<const float4*>(g.bias + nb);
 #pragma unroll
-                        for (int i = 0; i < 32; i++) {
-                            const float z = v[i] + g.bias[nb + i];
-                            v[i] = z;
-                            h[i] = gelu_f(z);
+                        for (int i = 0; i < 32; i += 4) {
+                            const float4 bb = __ldg(b4 + i / 4);
+                            v[i] += bb.x;
+                            v[i + 1] += bb.y;
+                            v[i + 2] += bb.z;
+                            v[i + 3] += bb.w;
                         }
+#pragma unroll
+                        for (int i = 0; i < 32; i++) h[i] = gelu_f(v[i]);
                         if (g.zs) {
                             float* zs = g.zs + (size_t)m * g.N + nb;
 #pragma unroll
                             for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(zs + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
                         }
                     } else {  // MLP_EPI_DGELU
-                        const float* zs = g.zs + (size_t)m * g.N + nb;
+                        const float4* z4 = reinterpret_cast<const float4*>(g.zs + (size_t)m * g.N + nb);
 #pragma unroll
-                        for (int i = 0; i < 32; i++) h[i] = v[i] * dgelu_f(zs[i]);
+                        for (int i = 0; i < 32; i += 4) {
+                            const float4 zz = z4[i / 4];
+                            h[i] = v[i] * dgelu_f(zz.x);
+                            h[i + 1] = v[i + 1] * dgelu_f(zz.y);
+                            h[i + 2] = v[i + 2] * dgelu_f(zz.z);
+                            h[i + 3] = v[i + 3] * dgelu_f(zz.w);
+                        }
                     }
-                    __nv_bfloat16* o = g.h16 + (size_t)m * g.N + nb;
+                    // row `lane` of the 32 x 64 staging tile; 16-byte chunk j of
+                    // the row sits at chunk j ^ (row % 8) (128-byte swizzle)
+                    const int hh = ((c - c0) >> 5) & 1;
+                    if (hh == 0) {
+                        // the previous store from this tile has finished reading it
+                        if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                        __syncwarp();
+                    }
 #pragma unroll
-                    for (int i = 0; i < 32; i += 8) {
+                    for (int k = 0; k < 4; k++) {
                         __align__(16) __nv_bfloat162 p[4];
 #pragma unroll
-                        for (int k = 0; k < 4; k++) p[k] = __floats2bfloat162_rn(h[i + 2 * k], h[i + 2 * k + 1]);
-                        *reinterpret_cast<uint4*>(o + i) = *reinterpret_cast<uint4*>(p);
+                        for (int e = 0; e < 4; e++) p[e] = __floats2bfloat162_rn(h[8 * k + 2 * e], h[8 * k + 2 * e + 1]);
+                        const int j = hh * 4 + k;
+                        *reinterpret_cast<uint4*>(stg + lane * 128 + ((j ^ (lane & 7)) << 4)) = *reinterpret_cast<uint4*>(p);
+                    }
+                    if (hh == 1) {
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        __syncwarp();
+                        if (lane == 0) tma_store_2d(&tmH, stg, nb - 32, m0 + q * 32);
                     }
                     if (g.h16t) {
 #pragma unroll
@@ -325,6 +367,8 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
             __syncwarp();
             if (lane == 0) mbar_arrive(&acc_empty[b]);
         }
+        // bf16 tiles stored by TMA are complete before the CTA exits
+        if (tma_out && lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     }
     __syncwarp();
     mbar_wait(&done, 0, abort);
@@ -373,7 +417,8 @@ static bool make_map(CUtensorMap* map, const void* ptr, int rows, int cols, int 
 static int mlp_stages(int bn) { return 4; }
 
 size_t bt_mlp_gemm_smem(int bn) {
-    return 1024 + (size_t)mlp_stages(bn) * (MLP_BM * MLP_BK * 2 + (size_t)bn * MLP_BK * 2);
+    return 1024 + (size_t)mlp_stages(bn) * (MLP_BM * MLP_BK * 2 + (size_t)bn * MLP_BK * 2) +
+           (size_t)MLP_NEPI * MLP_STG_BYTES;
 }
 
 cudaError_t bt_launch_mlp_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, const MlpGemmArgs& a, int splitk,
@@ -381,8 +426,16 @@ cudaError_t bt_launch_mlp_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, c
     if (a.M % MLP_BM || (a.bn != 128 && a.bn != 256) || a.N % a.bn || splitk < 1 || a.K % (splitk * MLP_BK))
         return cudaErrorInvalidValue;
     if (((uintptr_t)A & 15) || ((uintptr_t)B & 15)) return cudaErrorInvalidValue;
-    CUtensorMap ta, tb;
+    CUtensorMap ta, tb, th;
     if (!make_map(&ta, A, a.M, a.K, MLP_BM) || !make_map(&tb, B, a.N, a.K, a.bn)) return cudaErrorInvalidValue;
+    memset(&th, 0, sizeof(th));
+    if (a.mode == MLP_EPI_GELU || a.mode == MLP_EPI_DGELU) {
+        // bf16 output [M][N], stored in boxes of 64 columns x 32 rows
+        if (!a.h16 || ((uintptr_t)a.h16 & 15) || !make_map(&th, a.h16, a.M, a.N, 32)) return cudaErrorInvalidValue;
+    }
+    if ((a.mode == MLP_EPI_BIAS || a.mode == MLP_EPI_GELU) && (!a.bias || ((uintptr_t)a.bias & 15)))
+        return cudaErrorInvalidValue;
+    if (a.mode == MLP_EPI_DGELU && (!a.zs || ((uintptr_t)a.zs & 15))) return cudaErrorInvalidValue;
     MlpGemmArgs g = a;
     g.kchunk = a.K / splitk;
     g.stages = mlp_stages(a.bn);
@@ -397,7 +450,7 @@ cudaError_t bt_launch_mlp_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, c
     }
     const long long ntiles = (long long)(a.M / MLP_BM) * (a.N / a.bn) * splitk;
     const int grid = (int)(ntiles < bt_sm_count() ? ntiles : bt_sm_count());
-    k_mlp_gemm<<<grid, MLP_THREADS, smem, stream>>>(ta, tb, g);
+    k_mlp_gemm<<<grid, MLP_THREADS, smem, stream>>>(ta, tb, th, g);
     return cudaGetLastError();
 }
 

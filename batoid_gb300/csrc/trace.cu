@@ -25,12 +25,21 @@ cudaError_t bt_read_device_status(int* status, cudaStream_t stream) {
     return e;
 }
 
-#define TRACE_THREADS 128
-#define BT_TRACE_MINB_DEFAULT 4
+#define TRACE_THREADS 256
+#define BT_TRACE_MINB_DEFAULT 2
 
-// MINB = resident blocks per SM the register budget is sized for: 4 gives
+// MINB = resident blocks per SM the register budget is sized for: 2 gives
 // 128 registers (16 warps per SM, a few spills), 1 gives the compiler's
-// choice (154 registers, no spills, 12 warps per SM).
+// choice (no spills, fewer warps per SM).
+//
+// Stage-synchronous: the block's rays advance one stage at a time with a
+// barrier between stages, so all warps of the block run the same stage's
+// code together.  The code for all stage and surface kinds is far larger
+// than the instruction cache; warps spread over different stages missed in
+// it most of the time (ncu: instruction-cache hit rate 67 % and
+// "no instruction" the second stall reason), and the barrier keeps the
+// working set to one stage's code.  Rays of a stage differ only in Newton
+// iteration counts, so the barrier wait is short.
 template <int MINB>
 __global__ void __launch_bounds__(TRACE_THREADS, MINB)
 k_trace(const unsigned char* __restrict__ gblob, int blob_bytes, RV in, RV out,
@@ -39,27 +48,36 @@ k_trace(const unsigned char* __restrict__ gblob, int blob_bytes, RV in, RV out,
     __shared__ __align__(8) uint64_t bar;
     if (!bt_stage_blob(smem, gblob, blob_bytes, &bar)) return;
     const Prog P = prog_from_blob(smem);
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < in.n; i += stride) {
+    const int T = blockDim.x;
+    const long long stride = (long long)gridDim.x * T;
+    // block-uniform trip counts: every thread reaches every barrier
+    for (long long base = (long long)blockIdx.x * T; base < in.n; base += stride) {
+        const long long i = base + threadIdx.x;
+        const bool act = i < in.n;
         RayState r;
-        r.x = in.x[i];
-        r.y = in.y[i];
-        r.z = in.z[i];
-        r.vx = in.vx[i];
-        r.vy = in.vy[i];
-        r.vz = in.vz[i];
-        r.t = in.t[i];
-        r.w = in.w[i];
-        r.f = in.f[i];
-        r.vig = in.vig[i] != 0;
-        r.fail = in.fail[i] != 0;
+        if (act) {
+            r.x = in.x[i];
+            r.y = in.y[i];
+            r.z = in.z[i];
+            r.vx = in.vx[i];
+            r.vy = in.vy[i];
+            r.vz = in.vz[i];
+            r.t = in.t[i];
+            r.w = in.w[i];
+            r.f = in.f[i];
+            r.vig = in.vig[i] != 0;
+            r.fail = in.fail[i] != 0;
+        }
         int cached_medium = -1;
         double cached_n = 0.0, cached_inv_n = 0.0;
         for (int s = 0; s < P.nstages; s++) {
-            run_stage(P, P.stages[s], r, niter, cached_medium, cached_n, cached_inv_n);
-            if (s < nsnaps) store_ray(snaps.s[s], i, r);
+            if (act) {
+                run_stage(P, P.stages[s], r, niter, cached_medium, cached_n, cached_inv_n);
+                if (s < nsnaps) store_ray(snaps.s[s], i, r);
+            }
+            __syncthreads();
         }
-        if (nsnaps == 0) store_ray(out, i, r);
+        if (act && nsnaps == 0) store_ray(out, i, r);
     }
 }
 
@@ -88,20 +106,20 @@ cudaError_t bt_launch_trace(const unsigned char* d_blob, int blob_bytes, const R
     if (in.n <= 0) return cudaSuccess;
     static SnapSet empty;
     const SnapSet& ss = snaps ? *snaps : empty;
-    // register budget variant; BATOID_GB300_TRACE_MINB=1 or 4 overrides
+    // register budget variant; BATOID_GB300_TRACE_MINB=1 or 2 overrides
     static int minb = 0;
     if (minb == 0) {
         const char* env = getenv("BATOID_GB300_TRACE_MINB");
-        minb = (env && atoi(env) == 1) ? 1 : (env && atoi(env) == 4) ? 4 : BT_TRACE_MINB_DEFAULT;
+        minb = (env && atoi(env) == 1) ? 1 : (env && atoi(env) == 2) ? 2 : BT_TRACE_MINB_DEFAULT;
     }
-    auto kern = (minb == 1) ? k_trace<1> : k_trace<4>;
+    auto kern = (minb == 1) ? k_trace<1> : k_trace<2>;
     if (blob_bytes > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, blob_bytes);
         if (e != cudaSuccess) return e;
     }
-    // Persistent grid: the blob is staged once per block and amortised over
-    // the grid-stride loop.
-    const int grid = grid_for(in.n, TRACE_THREADS, 16);
+    // Persistent grid (2 blocks per SM): the blob is staged once per block
+    // and amortised over the grid-stride loop.
+    const int grid = grid_for(in.n, TRACE_THREADS, 2);
     kern<<<grid, TRACE_THREADS, blob_bytes, stream>>>(d_blob, blob_bytes, in, out, ss, nsnaps, niter);
     return cudaGetLastError();
 }

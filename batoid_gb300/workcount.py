@@ -135,3 +135,14 @@ def optic_flops_per_ray(optic, niter=5):
 
 def optic_stages(optic):
     return len(optic._stages())
+
+
+def wavefront_flops_per_ray(optic, jmax, niter=5):
+    """Algorithmic FP64 flops per pupil ray of one wavefront + Zernike fit
+    (reference batoid/analysis.py wavefront and zernike): the optic's trace,
+    the reference sphere (transform, Sphere intersection, propagation; OPD
+    as a time difference, 2 flops) and the fit's projection onto the basis
+    (jmax multiply-adds).  The reference solves the fit with numpy lstsq;
+    only the normal-equation projection is counted, so this undercounts the
+    reference's fit arithmetic."""
+    return optic_flops_per_ray(optic, niter) + TRANSFORM + 29 + PROPAGATE + 2 + 2 * jmax

@@ -268,7 +268,7 @@ def batch_states(pt, nstates, seed=31337):
     return np.concatenate([rigid, bend], axis=1), nx, wl
 
 
-def bench_batched(bt, nstates=4096, reps=3, cpu=True):
+def bench_batched(bt, nstates=4096, reps=3, cpu=True, fp64_peak_tflops=None):
     """Batched wavefronts: 4096 perturbed states x 9 fields, Zernike fit
     (jmax 28, annular) per (state, field), one persistent graph-captured
     launch per batch.  Device-timed with the states' tables resident; e2e
@@ -290,7 +290,10 @@ def bench_batched(bt, nstates=4096, reps=3, cpu=True):
     status = torch.empty(nstates * F, dtype=torch.int32, device=D.device())
     stream = torch.cuda.Stream()
     with torch.cuda.stream(stream):
-        pt.launch(inp, coefs, status, threads, ctas, graph=True)   # capture + first replay
+        # capture + first replay, marked for profilers (ncu --nvtx-include "batched_wavefronts/")
+        torch.cuda.nvtx.range_push("batched_wavefronts")
+        pt.launch(inp, coefs, status, threads, ctas, graph=True)
+        torch.cuda.nvtx.range_pop()
         stream.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -321,6 +324,13 @@ def bench_batched(bt, nstates=4096, reps=3, cpu=True):
                 "d2h_bytes": int(coefs.numel() * 8 + status.numel() * 4),
                 "path": "PerturbedTelescope.zernike (host tables, copies, launch, copies back)"},
     }
+    if fp64_peak_tflops:
+        from batoid_gb300 import workcount as WC
+        fpr = WC.wavefront_flops_per_ray(pt.perturbed(dofs[0]), J)
+        ach = fpr * rays / (ms * 1e-3) / 1e12
+        out["roofline"] = {"bound": "fp64", "achieved": ach, "peak": fp64_peak_tflops, "unit": "TFLOP/s",
+                           "frac": ach / fp64_peak_tflops, "flops_per_ray": fpr,
+                           "peak_source": "DFMA loop measured in this run (bt_measure_fp64_peak)"}
     if cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import wavefront as owf
@@ -402,7 +412,10 @@ def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24,
     out = torch.empty((N, 29), dtype=torch.float64, device=D.device())
     err = torch.empty(N, dtype=torch.float32, device=D.device())
     with torch.cuda.stream(stream):
+        # untimed first pass, marked for profilers (ncu --nvtx-include "surrogate_inference/")
+        torch.cuda.nvtx.range_push("surrogate_inference")
         sur.predict_device(feat_d, grp_d, w_d, out, err)
+        torch.cuda.nvtx.range_pop()
         stream.synchronize()
         e0.record(stream)
         for _ in range(10):
@@ -595,7 +608,8 @@ def run_gpu(args):
         huygens = bench_huygens(bt, opt, cpu=not args.no_cpu_baseline)
     batched = None
     if rank == 0 and not args.no_batch:
-        batched = bench_batched(bt, nstates=args.batch_states, cpu=not args.no_cpu_baseline)
+        batched = bench_batched(bt, nstates=args.batch_states, cpu=not args.no_cpu_baseline,
+                                fp64_peak_tflops=fpeak.value)
     surrogate = None
     if rank == 0 and not args.no_surrogate:
         surrogate = bench_surrogate(bt, train_samples=args.surrogate_samples, epochs=args.surrogate_epochs)

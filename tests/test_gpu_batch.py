@@ -98,8 +98,10 @@ def test_launch_shapes_agree_and_graph_replay_is_exact(pt):
     a = run(128, 3, False)
     b = run(64, 6, False)
     c = run(64, 4, False)
+    d = run(256, 2, False)
     np.testing.assert_allclose(b, a, rtol=0, atol=1e-9)
     np.testing.assert_allclose(c, a, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(d, a, rtol=0, atol=1e-9)
     s = torch.cuda.Stream()
     with torch.cuda.stream(s):
         g1 = run(128, 3, True)

@@ -63,6 +63,34 @@ def test_gemm_epilogues(N, bn):
     torch.testing.assert_close(h16t, h16.t().contiguous(), rtol=0, atol=0)
 
 
+@pytest.mark.parametrize("bn", [128, 256])
+def test_gemm_persistent_many_tiles(bn):
+    """More tiles than SMs: every CTA walks several tiles, so both TMEM
+    accumulators and the epilogue's staging tiles are reused."""
+    dev = D.device()
+    g = torch.Generator(device="cpu").manual_seed(bn + 7)
+    M, N, K = 128 * 200, 512, 192
+    A = torch.randn(M, K, generator=g).to(dev).to(BF)
+    B = torch.randn(N, K, generator=g).to(dev).to(BF)
+    bias = torch.randn(N, generator=g).to(dev)
+    z = A.float() @ B.float().T + bias
+    tol = 1e-4 * z.abs().max().item()
+    zs = torch.empty(M, N, device=dev)
+    h16 = torch.empty(M, N, device=dev, dtype=BF)
+    h16t = torch.empty(N, M, device=dev, dtype=BF)
+    _gemm(A, B, M, N, K, bn, 2, bias=bias, zs=zs, h16=h16, h16t=h16t)
+    assert (zs - z).abs().max().item() <= tol
+    torch.testing.assert_close(h16, _gelu(zs).to(BF), rtol=1.6e-2, atol=1e-2)
+    torch.testing.assert_close(h16t, h16.t().contiguous(), rtol=0, atol=0)
+    # inference form: no pre-activations, no transposed copy
+    h2 = torch.zeros(M, N, device=dev, dtype=BF)
+    _gemm(A, B, M, N, K, bn, 2, bias=bias, h16=h2)
+    torch.testing.assert_close(h2, h16, rtol=0, atol=0)
+    out = torch.empty(M, N, device=dev)
+    _gemm(A, B, M, N, K, bn, 1, bias=bias, out32=out)
+    assert (out - z).abs().max().item() <= tol
+
+
 def test_gemm_rejects_bad_shapes():
     dev = D.device()
     A = torch.zeros(100, 64, device=dev, dtype=BF)
