@@ -131,6 +131,9 @@ _SIGS = [
     ("bt_apply_forward_transform_arrays", c_int, [_D3, _D3, _P, _P, _P, c_size_t, c_int, _P]),
     ("bt_apply_reverse_transform_arrays", c_int, [_D3, _D3, _P, _P, _P, c_size_t, c_int, _P]),
     ("bt_finish_parallel", c_int, [_D3, _D3, _D3, _P, _P, _P, c_size_t, _P]),
+    ("bt_stop_points_grid", c_int, [c_int, c_int, c_double, c_double, _D3, _D3, _P, _P, _P]),
+    ("bt_stop_points_rings", c_int, [c_int, _P, _P, _P, ctypes.c_longlong, _P, _P, _P]),
+    ("bt_stop_points_spokes", c_int, [_P, c_int, _P, c_int, _P, _P, _P]),
     ("bt_obscure", c_int, [_P, ctypes.POINTER(BtRayVector), c_int, _P]),
     ("bt_refract_screen", c_int, [_P, _D3, _D3, _P, ctypes.POINTER(BtRayVector), c_int, c_int, _P]),
     ("bt_rsplit", c_int, [_P, _D3, _D3, _P, _P, _P, ctypes.POINTER(BtRayVector), ctypes.POINTER(BtRayVector), c_int,

@@ -52,6 +52,12 @@ cudaError_t bt_launch_transform_arrays(const double dr[3], const double drot[9],
                                        double* z, long long n, bool forward, cudaStream_t stream);
 cudaError_t bt_launch_finish_parallel(const double dr[3], const double drot[9], const double vv[3],
                                       double* x, double* y, double* z, long long n, cudaStream_t stream);
+cudaError_t bt_launch_stop_grid(int nx, int ny, double valx, double valy, const double lx[2], const double ly[2],
+                                double* x, double* y, cudaStream_t stream);
+cudaError_t bt_launch_stop_rings(int nring, const double* r, const double* step, const long long* off, long long n,
+                                 double* x, double* y, cudaStream_t stream);
+cudaError_t bt_launch_stop_spokes(const double* rings, int nr, const double* spokes, int ns, double* x, double* y,
+                                  cudaStream_t stream);
 cudaError_t bt_launch_position_at_time(const RV& rv, double t, double* xo, double* yo, double* zo,
                                        cudaStream_t stream);
 cudaError_t bt_launch_propagate(const RV& rv, double t, cudaStream_t stream);

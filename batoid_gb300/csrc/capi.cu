@@ -852,6 +852,32 @@ extern "C" int bt_finish_parallel(const double dr[3], const double drot[9], cons
     return BT_OK;
 }
 
+extern "C" int bt_stop_points_grid(int nx, int ny, double valx, double valy, const double lx[2], const double ly[2],
+                                   double* x, double* y, void* stream) {
+    if (nx < 1 || ny < 1) return fail(BT_ERR_ARG, "stop points (grid): nx and ny must be positive");
+    if (!lx || !ly || !x || !y) return fail(BT_ERR_ARG, "stop points (grid): null argument");
+    CUDA_TRY(bt_launch_stop_grid(nx, ny, valx, valy, lx, ly, x, y, (cudaStream_t)stream), "stop points (grid)");
+    return BT_OK;
+}
+
+extern "C" int bt_stop_points_rings(int nring, const double* r, const double* step, const long long* off,
+                                    long long n, double* x, double* y, void* stream) {
+    if (n == 0) return BT_OK;
+    if (nring < 1 || n < 0) return fail(BT_ERR_ARG, "stop points (rings): bad ring count or size");
+    if (!r || !step || !off || !x || !y) return fail(BT_ERR_ARG, "stop points (rings): null argument");
+    CUDA_TRY(bt_launch_stop_rings(nring, r, step, off, n, x, y, (cudaStream_t)stream), "stop points (rings)");
+    return BT_OK;
+}
+
+extern "C" int bt_stop_points_spokes(const double* rings, int nr, const double* spokes, int ns, double* x, double* y,
+                                     void* stream) {
+    if (nr == 0 || ns == 0) return BT_OK;
+    if (nr < 0 || ns < 0) return fail(BT_ERR_ARG, "stop points (spokes): negative size");
+    if (!rings || !spokes || !x || !y) return fail(BT_ERR_ARG, "stop points (spokes): null argument");
+    CUDA_TRY(bt_launch_stop_spokes(rings, nr, spokes, ns, x, y, (cudaStream_t)stream), "stop points (spokes)");
+    return BT_OK;
+}
+
 extern "C" int bt_rv_position_at_time(const bt_rayvector* rv, double t, double* xo, double* yo, double* zo,
                                       int max_threads, void* stream) {
     (void)max_threads;
@@ -1297,11 +1323,11 @@ extern "C" int bt_mlp_colsum(const void* xt, int rows, int cols, float* out, voi
     return BT_OK;
 }
 
-extern "C" int bt_surrogate_combine(const float* feat, int nfeat, int nlin, const int* grp, const double* theta,
+extern "C" int bt_surrogate_combine(const float* feat, int nfeat, int nlin, const int* grp, const float* theta,
                                     const float* y, int ldy, const double* wl, double scale, int J, int err_col,
                                     double* out, float* err_nm, int n, void* stream) {
     if (n < 0 || (n > 0 && (!feat || !grp || !theta || !y || !wl || !out)) || nlin > nfeat || J < 1 || J > ldy ||
-        err_col >= ldy)
+        err_col >= ldy || ((uintptr_t)theta & 7))
         return fail(BT_ERR_ARG, "surrogate combine: bad arguments");
     CUDA_TRY(bt_launch_surrogate_combine(feat, nfeat, nlin, grp, theta, y, ldy, wl, scale, J, err_col, out, err_nm, n,
                                          (cudaStream_t)stream), "surrogate combine");

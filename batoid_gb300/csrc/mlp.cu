@@ -291,28 +291,38 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
             const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
             const int c0 = half * (BN / 2);
             for (int c = c0; c < c0 + BN / 2; c += 32) {
+                const int nb = n0 + c;
+                // this chunk's bias (or pre-activations) are requested before
+                // the TMEM load so that both latencies overlap
+                float4 pre[8];
+                if (g.mode == MLP_EPI_BIAS || g.mode == MLP_EPI_GELU) {
+                    const float4* b4 = reinterpret_cast<const float4*>(g.bias + nb);
+#pragma unroll
+                    for (int k = 0; k < 8; k++) pre[k] = __ldg(b4 + k);
+                } else if (g.mode == MLP_EPI_DGELU) {
+                    const float4* z4 = reinterpret_cast<const float4*>(g.zs + (size_t)m * g.N + nb);
+#pragma unroll
+                    for (int k = 0; k < 8; k++) pre[k] = z4[k];
+                }
                 float v[32];
                 tmem_ld32(trow + (uint32_t)c, v);
-                const int nb = n0 + c;
                 if (g.mode == MLP_EPI_F32) {
                     float* o = g.out32 + (size_t)kz * g.M * g.N + (size_t)m * g.N + nb;
 #pragma unroll
                     for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(o + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
                 } else if (g.mode == MLP_EPI_BIAS) {
                     float* o = g.out32 + (size_t)m * g.N + nb;
-                    const float4* b4 = reinterpret_cast<const float4*>(g.bias + nb);
 #pragma unroll
                     for (int i = 0; i < 32; i += 4) {
-                        const float4 bb = __ldg(b4 + i / 4);
+                        const float4 bb = pre[i / 4];
                         *reinterpret_cast<float4*>(o + i) = make_float4(v[i] + bb.x, v[i + 1] + bb.y, v[i + 2] + bb.z, v[i + 3] + bb.w);
                     }
                 } else {
                     float h[32];
                     if (g.mode == MLP_EPI_GELU) {
-                        const float4* b4 = reinterpret_cast<const float4*>(g.bias + nb);
 #pragma unroll
                         for (int i = 0; i < 32; i += 4) {
-                            const float4 bb = __ldg(b4 + i / 4);
+                            const float4 bb = pre[i / 4];
                             v[i] += bb.x;
                             v[i + 1] += bb.y;
                             v[i + 2] += bb.z;
@@ -326,10 +336,9 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
                             for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(zs + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
                         }
                     } else {  // MLP_EPI_DGELU
-                        const float4* z4 = reinterpret_cast<const float4*>(g.zs + (size_t)m * g.N + nb);
 #pragma unroll
                         for (int i = 0; i < 32; i += 4) {
-                            const float4 zz = z4[i / 4];
+                            const float4 zz = pre[i / 4];
                             h[i] = v[i] * dgelu_f(zz.x);
                             h[i + 1] = v[i + 1] * dgelu_f(zz.y);
                             h[i + 2] = v[i + 2] * dgelu_f(zz.z);
@@ -608,19 +617,34 @@ cudaError_t bt_launch_mlp_adam(const float* partials, int nsplit, const float* g
 //   out[n][0] = 0, out[n][1 + j] = lin_j + y[n][j] * scale / (wl[n] * 1e9)   (waves)
 //   err_nm[n] = scale * exp(y[n][err_col])
 // FP64 for the linear part, which carries most of the signal.
+// Linear model in float-float on the FP32 pipe (theta as hi/lo float
+// pairs; each term's product error recovered with an FMA, the sum
+// compensated: ~48-bit accuracy, far below the model's own error), the
+// network's residual added in FP64 with one reciprocal per sample.
 __global__ void k_surrogate_combine(const float* __restrict__ feat, int nfeat, int nlin, const int* __restrict__ grp,
-                                    const double* __restrict__ theta, const float* __restrict__ y, int ldy,
+                                    const float2* __restrict__ theta, const float* __restrict__ y, int ldy,
                                     const double* __restrict__ wl, double scale, int J, int err_col,
                                     double* __restrict__ out, float* __restrict__ err_nm, int n) {
     const long long total = (long long)n * J;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
          e += (long long)gridDim.x * blockDim.x) {
         const int s = (int)(e / J), j = (int)(e - (long long)s * J);
-        const double* th = theta + (size_t)grp[s] * (nlin + 1) * J;
-        double acc = th[j];
+        const float2* th = theta + (size_t)grp[s] * (nlin + 1) * J + j;
+        float hi = th[0].x, lo = th[0].y;
         const float* f = feat + (size_t)s * nfeat;
-        for (int k = 0; k < nlin; k++) acc += th[(size_t)(k + 1) * J + j] * (double)f[k];
-        out[(size_t)s * (J + 1) + 1 + j] = acc + (double)y[(size_t)s * ldy + j] * scale / (wl[s] * 1e9);
+        for (int k = 0; k < nlin; k++) {
+            const float2 t = th[(size_t)(k + 1) * J];
+            const float fk = f[k];
+            const float p = t.x * fk;
+            const float pe = fmaf(t.y, fk, fmaf(t.x, fk, -p));
+            const float sum = hi + p;
+            const float bb = sum - hi;
+            lo += ((hi - (sum - bb)) + (p - bb)) + pe;
+            hi = sum;
+        }
+        const double lin = (double)hi + (double)lo;
+        const double to_waves = scale / (wl[s] * 1e9);
+        out[(size_t)s * (J + 1) + 1 + j] = fma((double)y[(size_t)s * ldy + j], to_waves, lin);
         if (j == 0) {
             out[(size_t)s * (J + 1)] = 0.0;
             if (err_nm) err_nm[s] = (float)(scale * exp((double)y[(size_t)s * ldy + err_col]));
@@ -628,11 +652,12 @@ __global__ void k_surrogate_combine(const float* __restrict__ feat, int nfeat, i
     }
 }
 
-cudaError_t bt_launch_surrogate_combine(const float* feat, int nfeat, int nlin, const int* grp, const double* theta,
+cudaError_t bt_launch_surrogate_combine(const float* feat, int nfeat, int nlin, const int* grp, const float* theta,
                                         const float* y, int ldy, const double* wl, double scale, int J, int err_col,
                                         double* out, float* err_nm, int n, cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
-    k_surrogate_combine<<<mlp_grid((long long)n * J), 256, 0, stream>>>(feat, nfeat, nlin, grp, theta, y, ldy, wl,
+    k_surrogate_combine<<<mlp_grid((long long)n * J), 256, 0, stream>>>(feat, nfeat, nlin, grp,
+                                                                         reinterpret_cast<const float2*>(theta), y, ldy, wl,
                                                                          scale, J, err_col, out, err_nm, n);
     return cudaGetLastError();
 }

@@ -114,6 +114,75 @@ cudaError_t bt_launch_finish_parallel(const double dr[3], const double drot[9], 
     return cudaGetLastError();
 }
 
+// Stop-surface sample points of the factories, generated on the device so
+// that only the factory's parameters cross from the host.
+//
+// Grid (batoid/rayVector.py:411-444): point i = (ix, iy) = (i % nx, i / nx)
+// of fftshift(fftfreq(n, d)) = (k - n/2) * (1 / (n d)) (numpy multiplies
+// the integer k by the reciprocal), then x = lx . (u, w), y = ly . (u, w).
+__global__ void k_stop_grid(int nx, long long n, double valx, double valy, double lx0, double lx1, double ly0,
+                            double ly1, int hx, int hy, double* X, double* Y) {
+    GRID_LOOP(i, n) {
+        const long long iy = i / nx, ix = i - iy * nx;
+        const double u = (double)(ix - hx) * valx, w = (double)(iy - hy) * valy;
+        X[i] = fma(lx1, w, lx0 * u);
+        Y[i] = fma(ly1, w, ly0 * u);
+    }
+}
+
+// Rings of points (hexapolar, batoid/utils.py:512-535): ring k holds points
+// off[k] .. off[k+1]-1 at radius r[k] and azimuths j * step[k].
+__global__ void k_stop_rings(int nring, const double* __restrict__ r, const double* __restrict__ step,
+                             const long long* __restrict__ off, long long n, double* X, double* Y) {
+    GRID_LOOP(i, n) {
+        int lo = 0, hi = nring - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (off[mid] <= i) lo = mid;
+            else hi = mid - 1;
+        }
+        const double th = (double)(i - off[lo]) * step[lo];
+        X[i] = r[lo] * cos(th);
+        Y[i] = r[lo] * sin(th);
+    }
+}
+
+// Spokes x rings (batoid/rayVector.py:786-814): meshgrid(rings, spokes)
+// raveled, point i on ring i % nr of spoke i / nr.
+__global__ void k_stop_spokes(const double* __restrict__ rings, int nr, const double* __restrict__ spokes,
+                              long long n, double* X, double* Y) {
+    GRID_LOOP(i, n) {
+        const long long s = i / nr;
+        const double rr = rings[i - s * nr], th = spokes[s];
+        X[i] = rr * cos(th);
+        Y[i] = rr * sin(th);
+    }
+}
+
+cudaError_t bt_launch_stop_grid(int nx, int ny, double valx, double valy, const double lx[2], const double ly[2],
+                                double* x, double* y, cudaStream_t stream) {
+    const long long n = (long long)nx * ny;
+    if (n <= 0) return cudaSuccess;
+    k_stop_grid<<<rv_grid(n), RV_THREADS, 0, stream>>>(nx, n, valx, valy, lx[0], lx[1], ly[0], ly[1], nx / 2, ny / 2,
+                                                       x, y);
+    return cudaGetLastError();
+}
+
+cudaError_t bt_launch_stop_rings(int nring, const double* r, const double* step, const long long* off, long long n,
+                                 double* x, double* y, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    k_stop_rings<<<rv_grid(n), RV_THREADS, 0, stream>>>(nring, r, step, off, n, x, y);
+    return cudaGetLastError();
+}
+
+cudaError_t bt_launch_stop_spokes(const double* rings, int nr, const double* spokes, int ns, double* x, double* y,
+                                  cudaStream_t stream) {
+    const long long n = (long long)nr * ns;
+    if (n <= 0) return cudaSuccess;
+    k_stop_spokes<<<rv_grid(n), RV_THREADS, 0, stream>>>(rings, nr, spokes, n, x, y);
+    return cudaGetLastError();
+}
+
 // src/rayVector.cpp:26-54
 __global__ void k_position_at_time(RV rv, double t, double* xo, double* yo, double* zo) {
     GRID_LOOP(i, rv.n) {

@@ -17,7 +17,7 @@ from . import _device as D
 from . import _lib
 from .constants import globalCoordSys, vacuum
 from .coordTransform import CoordTransform
-from .utils import fieldToDirCos, hexapolar
+from .utils import fieldToDirCos, hexapolar_rings
 
 _FIELDS = ("x", "y", "z", "vx", "vy", "vz", "t", "wavelength", "flux")
 _FLAGS = ("vignetted", "failed")
@@ -245,19 +245,24 @@ class RayVector:
             rng = _rng(rng)
             xx = rng.uniform(-0.5, 0.5, size=nrandom)
             yy = rng.uniform(-0.5, 0.5, size=nrandom)
-        else:
-            x_d = 1. if nx <= 2 else (nx - (2 if nx % 2 == 0 else 1)) / nx
-            y_d = 1. if ny <= 2 else (ny - (2 if ny % 2 == 0 else 1)) / ny
-            xx = np.fft.fftshift(np.fft.fftfreq(nx, x_d))
-            yy = np.fft.fftshift(np.fft.fftfreq(ny, y_d))
-            xx, yy = np.meshgrid(xx, yy)
-            xx = xx.ravel()
-            yy = yy.ravel()
-        stack = np.stack([xx, yy])
-        x = np.dot(lx, stack)
-        y = np.dot(ly, stack)
-        return cls._fromStopPoints(x, y, stopSurface, coordSys, wavelength, medium, backDist,
-                                   source, dirCos, flux)
+            stack = np.stack([xx, yy])
+            x = np.dot(lx, stack)
+            y = np.dot(ly, stack)
+            return cls._fromStopPoints(x, y, stopSurface, coordSys, wavelength, medium, backDist,
+                                       source, dirCos, flux)
+        # fftshift(fftfreq(n, d)) lattice, generated on the device
+        nx, ny = int(nx), int(ny)
+        x_d = 1. if nx <= 2 else (nx - (2 if nx % 2 == 0 else 1)) / nx
+        y_d = 1. if ny <= 2 else (ny - (2 if ny % 2 == 0 else 1)) / ny
+        valx, valy = 1.0 / (nx * x_d), 1.0 / (ny * y_d)
+        a_lx, p_lx = _lib.vec(lx, 2)
+        a_ly, p_ly = _lib.vec(ly, 2)
+
+        def gen(dx, dy):
+            _lib.check(_lib.lib().bt_stop_points_grid(nx, ny, valx, valy, p_lx, p_ly, D.ptr(dx), D.ptr(dy),
+                                                      D.stream_ptr()))
+        return cls._fromStopPoints(None, None, stopSurface, coordSys, wavelength, medium, backDist,
+                                   source, dirCos, flux, gen=(nx * ny, gen))
 
     @classmethod
     def asFan(cls, nx=None, ny=None, **kwargs):
@@ -286,16 +291,21 @@ class RayVector:
         backDist, medium, stopSurface, coordSys, dirCos, _ = _defaults(
             optic, backDist, medium, stopSurface, coordSys, dirCos, source, theta_x, theta_y,
             projection, wavelength, strict_stop=True)
-        if nrandom is None:
-            rr, th = hexapolar(outer=outer, inner=inner, nrad=nrad, naz=naz, kfold=kfold, rth=True)
-        else:
+        if nrandom is not None:
             rng = _rng(rng)
             rr = np.sqrt(rng.uniform(inner ** 2, outer ** 2, size=nrandom))
             th = rng.uniform(0, 2 * np.pi, size=nrandom)
-        x = rr * np.cos(th)
-        y = rr * np.sin(th)
-        return cls._fromStopPoints(x, y, stopSurface, coordSys, wavelength, medium, backDist,
-                                   source, dirCos, flux)
+            return cls._fromStopPoints(rr * np.cos(th), rr * np.sin(th), stopSurface, coordSys, wavelength,
+                                       medium, backDist, source, dirCos, flux)
+        # hexapolar rings (batoid/utils.py:512-535), points generated on the device
+        r_tab, step, off = hexapolar_rings(outer=outer, inner=inner, nrad=nrad, naz=naz, kfold=kfold)
+        d_r, d_step, d_off = D.to_device(r_tab), D.to_device(step), torch.from_numpy(off).to(D.device())
+
+        def gen(dx, dy):
+            _lib.check(_lib.lib().bt_stop_points_rings(len(r_tab), D.ptr(d_r), D.ptr(d_step), D.ptr(d_off),
+                                                       int(off[-1]), D.ptr(dx), D.ptr(dy), D.stream_ptr()))
+        return cls._fromStopPoints(None, None, stopSurface, coordSys, wavelength, medium, backDist,
+                                   source, dirCos, flux, gen=(int(off[-1]), gen))
 
     @classmethod
     def asSpokes(cls, optic=None, backDist=None, medium=None, stopSurface=None, coordSys=None,
@@ -321,14 +331,18 @@ class RayVector:
                 flux = w * area / (2 * spokes)
             if isinstance(spokes, Integral):
                 spokes = np.linspace(0, 2 * np.pi, spokes, endpoint=False)
-        rings, spokes = np.meshgrid(rings, spokes)
-        flux = np.broadcast_to(flux, rings.shape).ravel()
-        rings = rings.ravel()
-        spokes = spokes.ravel()
-        x = rings * np.cos(spokes)
-        y = rings * np.sin(spokes)
-        return cls._fromStopPoints(x, y, stopSurface, coordSys, wavelength, medium, backDist,
-                                   source, dirCos, flux)
+        # meshgrid(rings, spokes) raveled: point i on ring i % nr of spoke i / nr
+        rings = np.ascontiguousarray(np.atleast_1d(rings), dtype=float).ravel()
+        spokes = np.ascontiguousarray(np.atleast_1d(spokes), dtype=float).ravel()
+        nr, ns = len(rings), len(spokes)
+        flux = np.broadcast_to(flux, (ns, nr)).ravel()
+        d_rings, d_spokes = D.to_device(rings), D.to_device(spokes)
+
+        def gen(dx, dy):
+            _lib.check(_lib.lib().bt_stop_points_spokes(D.ptr(d_rings), nr, D.ptr(d_spokes), ns, D.ptr(dx),
+                                                        D.ptr(dy), D.stream_ptr()))
+        return cls._fromStopPoints(None, None, stopSurface, coordSys, wavelength, medium, backDist,
+                                   source, dirCos, flux, gen=(nr * ns, gen))
 
     @classmethod
     def fromStop(cls, x, y, optic=None, backDist=None, medium=None, stopSurface=None,
@@ -371,19 +385,24 @@ class RayVector:
 
     @classmethod
     def _fromStopPoints(cls, x, y, stopSurface, coordSys, wavelength, medium, backDist, source,
-                        dirCos, flux):
+                        dirCos, flux, gen=None):
         """Common tail of the factories: stop sag, transform into ``coordSys``,
-        back-propagation (batoid/rayVector.py:817-858)."""
+        back-propagation (batoid/rayVector.py:817-858).  The stop points are
+        host arrays ``x, y`` or, with ``gen = (n, fill)``, written on the
+        device by ``fill(dx, dy)``."""
         if source is not None:
             raise NotImplementedError("point sources are not implemented (the reference's "
                                       "source branch is also a no-op, batoid/rayVector.py:847-858)")
-        n_rays = len(x)
+        n_rays = len(x) if gen is None else gen[0]
         ret = RayVector._empty(n_rays, coordSys)
         dx = ret._d[0]
         dy = ret._d[1]
         dz = ret._d[2]
-        dx.copy_(D.to_device(x))
-        dy.copy_(D.to_device(y))
+        if gen is None:
+            dx.copy_(D.to_device(x))
+            dy.copy_(D.to_device(y))
+        elif n_rays > 0:
+            gen[1](dx, dy)
         stopSurface.surface._sag_device(dx, dy, dz)
         ct = CoordTransform(stopSurface.coordSys, coordSys)
         L = _lib.lib()

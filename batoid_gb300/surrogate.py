@@ -239,6 +239,7 @@ class WavefrontSurrogate:
         G = self.F * len(self.wavelengths)
         c = coefs.reshape(-1, self.J + 1)[:, 1:]
         self.theta = np.zeros((G, nd + 1, self.J))
+        self._theta_d = None  # device copy rebuilt on the next prediction
         for g in range(G):
             sel = grp == g
             if not np.any(sel):
@@ -297,7 +298,11 @@ class WavefrontSurrogate:
         if err is None:
             err = torch.empty(n, dtype=torch.float32, device=D.device())
         if not hasattr(self, "_theta_d") or self._theta_d is None:
-            self._theta_d = D.to_device(self.theta.ravel())
+            # float-float pairs (hi, lo) of the FP64 linear model
+            th = np.ascontiguousarray(self.theta.ravel(), dtype=np.float64)
+            hi = th.astype(np.float32)
+            lo = (th - hi.astype(np.float64)).astype(np.float32)
+            self._theta_d = torch.from_numpy(np.stack([hi, lo], axis=1).ravel()).to(D.device())
         _lib.check(_lib.lib().bt_surrogate_combine(_p(feat_d), feat_d.shape[1], self.pt.ndof, _p(grp_d),
                                                    _p(self._theta_d), y.data_ptr(), PAD, _p(w_d), self.scale, self.J,
                                                    self.J, _p(out), _p(err), n, D.stream_ptr()))

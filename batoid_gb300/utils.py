@@ -148,9 +148,7 @@ def dirCosToField(alpha, beta, gamma, projection='postel'):
         raise ValueError("Bad projection: {}".format(projection)) from None
 
 
-def hexapolar(outer=1.0, inner=0.0, nrad=5, naz=30, kfold=6, rth=False):
-    """Rings of points with a multiple of ``kfold`` points per ring
-    (batoid/utils.py:483-535)."""
+def _hexapolar_layout(outer, inner, nrad, naz, kfold):
     rhos = np.linspace(outer, inner, nrad)
     nphis = []
     for rho in rhos:
@@ -158,6 +156,26 @@ def hexapolar(outer=1.0, inner=0.0, nrad=5, naz=30, kfold=6, rth=False):
         nphis.append(nphi if nphi else kfold)
     if inner == 0.0:
         nphis[-1] = 1
+    return rhos, nphis
+
+
+def hexapolar_rings(outer=1.0, inner=0.0, nrad=5, naz=30, kfold=6):
+    """Ring table of ``hexapolar``: radius, azimuth step and first point of
+    each ring (offsets has nrad + 1 entries).  Point j of ring k sits at
+    azimuth j * step[k] (numpy's linspace(0, 2 pi, n, endpoint=False))."""
+    rhos, nphis = _hexapolar_layout(outer, inner, nrad, naz, kfold)
+    r = np.array(rhos, dtype=float)
+    if inner == 0.0:
+        r[-1] = 0.0
+    step = np.array([(2 * np.pi - 0.0) / k for k in nphis], dtype=float)
+    off = np.concatenate([[0], np.cumsum(nphis)]).astype(np.int64)
+    return r, step, off
+
+
+def hexapolar(outer=1.0, inner=0.0, nrad=5, naz=30, kfold=6, rth=False):
+    """Rings of points with a multiple of ``kfold`` points per ring
+    (batoid/utils.py:483-535)."""
+    rhos, nphis = _hexapolar_layout(outer, inner, nrad, naz, kfold)
     rr = np.concatenate([np.full(k, rho) for rho, k in zip(rhos, nphis)])
     th = np.concatenate([np.linspace(0, 2 * np.pi, k, endpoint=False) for k in nphis])
     if inner == 0.0:

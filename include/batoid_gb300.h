@@ -150,6 +150,23 @@ int bt_apply_reverse_transform_arrays(const double dr[3], const double drot[9],
                                       int max_threads, void* stream);    /* src/batoid.cpp:24-38 */
 int bt_finish_parallel(const double dr[3], const double drot[9], const double vv[3],
                        double* x, double* y, double* z, size_t n, void* stream); /* src/batoid.cpp:40-69 */
+/* Stop-surface sample points of the ray factories, generated on the device
+ * (replaces the numpy point generation of RayVector.asGrid / asPolar /
+ * asSpokes, batoid/rayVector.py:411-444, batoid/utils.py:512-535,
+ * batoid/rayVector.py:786-814; the reference builds these arrays on the host
+ * and copies them).  x, y: device arrays of nx*ny, n, nr*ns points.
+ *   grid:   point i = (i % nx, i / nx): u = (i%nx - nx/2) valx,
+ *           w = (i/nx - ny/2) valy (valx = 1/(nx dx), numpy fftfreq),
+ *           x = lx[0] u + lx[1] w, y = ly[0] u + ly[1] w;
+ *   rings:  ring k holds points off[k]..off[k+1]-1 at radius r[k], azimuth
+ *           j step[k] (r, step, off: device arrays of nring, nring, nring+1);
+ *   spokes: point i at radius rings[i % nr], azimuth spokes[i / nr] (device). */
+int bt_stop_points_grid(int nx, int ny, double valx, double valy, const double lx[2], const double ly[2],
+                        double* x, double* y, void* stream);
+int bt_stop_points_rings(int nring, const double* r, const double* step, const long long* off, long long n,
+                         double* x, double* y, void* stream);
+int bt_stop_points_spokes(const double* rings, int nr, const double* spokes, int ns, double* x, double* y,
+                          void* stream);
 /* refractScreen(surface, dr, drot, screen, rv, max_threads, niter)
  * (src/batoid.cpp:677-810; batoid/trace.py:139-153): intersect, then deflect
  * the direction cosines by the gradient of the screen surface's sag and add
@@ -386,10 +403,12 @@ int bt_mlp_adam(const float* partials, int nsplit, const float* grad, long long 
 /* Surrogate output assembly: for sample s in group grp[s], Zernike
  * coefficients out[s][0..J] (waves; entry 0 = 0) = linear model
  * theta[grp][0][j] + sum_k theta[grp][1+k][j] feat[s][k] (k < nlin; theta
- * is [groups][nlin+1][J] FP64) plus the network's residual y[s][j] (nm
+ * is [groups][nlin+1][J] float-float pairs (hi, lo), 8-byte aligned, with
+ * hi + lo the FP64 coefficient; evaluated to ~48 bits on the FP32 pipe)
+ * plus the network's residual y[s][j] (nm
  * divided by `scale`) converted to waves at wl[s]; err_nm[s] (may be null)
  * = scale * exp(y[s][err_col]), the predicted residual norm in nm. */
-int bt_surrogate_combine(const float* feat, int nfeat, int nlin, const int* grp, const double* theta, const float* y,
+int bt_surrogate_combine(const float* feat, int nfeat, int nlin, const int* grp, const float* theta, const float* y,
                          int ldy, const double* wl, double scale, int J, int err_col, double* out, float* err_nm,
                          int n, void* stream);
 

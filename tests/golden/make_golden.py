@@ -333,6 +333,18 @@ def analysis_fixture(batoid):
     return out
 
 
+def factories_fixture(batoid):
+    """RayVector.asGrid / asPolar / asSpokes / fromStop of the 12-surface
+    system (tests/_factories.py cases), as the reference builds them."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _factories as F
+    opt = W.tma_optic(batoid, zernike_factory=ref_zernike_factory(batoid))
+    out = {}
+    for name, kind, kw in F.cases():
+        out.update(rv_to_dict(F.make(batoid, opt, kind, kw), name))
+    return out
+
+
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     ref_root = args[0] if args else "/root/reference"
@@ -341,6 +353,9 @@ def main():
     batoid.global_vars._batoid_max_threads = 1
     if "--only-split" in sys.argv:
         np.savez_compressed(os.path.join(HERE, "split.npz"), **split_fixture(batoid))
+        return
+    if "--only-factories" in sys.argv:
+        np.savez_compressed(os.path.join(HERE, "factories.npz"), **factories_fixture(batoid))
         return
     if "--only-analysis" in sys.argv:
         np.savez_compressed(os.path.join(HERE, "analysis.npz"), **analysis_fixture(batoid))
@@ -352,6 +367,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "zemax.npz"), **zemax_fixture(batoid, ref_root))
     np.savez_compressed(os.path.join(HERE, "split.npz"), **split_fixture(batoid))
     np.savez_compressed(os.path.join(HERE, "analysis.npz"), **analysis_fixture(batoid))
+    np.savez_compressed(os.path.join(HERE, "factories.npz"), **factories_fixture(batoid))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

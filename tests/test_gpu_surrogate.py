@@ -64,3 +64,29 @@ def test_fallback_rows_are_the_trace(trained):
     e = rms_nm(out.reshape(-1, sur.J + 1)[acc], truth.reshape(-1, sur.J + 1)[acc], w[acc])
     # the calibrated estimate bounds most accepted errors
     assert np.mean(e <= thr) > 0.9
+
+
+def test_combine_linear_model_matches_fp64(trained):
+    """The device's float-float linear model against the host's FP64 one:
+    with a zero network output the coefficients are the linear model."""
+    import torch
+    from batoid_gb300 import _device as D, _lib
+    from batoid_gb300.surrogate import PAD
+    sur, _ = trained
+    d, wi = sur.sample_states(300, seed=6)
+    feat, grp, w = sur.features(d, wi)
+    n = len(feat)
+    sur.predict(feat[:1], grp[:1], w[:1])  # builds the device theta
+    y = torch.zeros((n, PAD), dtype=torch.float32, device=D.device())
+    out = torch.empty((n, sur.J + 1), dtype=torch.float64, device=D.device())
+    fd = torch.from_numpy(np.ascontiguousarray(feat)).to(D.device())
+    gd = torch.from_numpy(np.ascontiguousarray(grp)).to(D.device())
+    wd = D.to_device(w)
+    _lib.check(_lib.lib().bt_surrogate_combine(fd.data_ptr(), feat.shape[1], sur.pt.ndof, gd.data_ptr(),
+                                               sur._theta_d.data_ptr(), y.data_ptr(), PAD, wd.data_ptr(), sur.scale,
+                                               sur.J, sur.J, out.data_ptr(), None, n, D.stream_ptr()))
+    got = D.to_host(out)
+    want = sur.linear(feat, grp)
+    assert np.all(got[:, 0] == 0.0)
+    scale = np.abs(want).max()
+    np.testing.assert_allclose(got[:, 1:], want, rtol=0, atol=1e-12 * scale)
