@@ -39,7 +39,7 @@
 
 #define MLP_BM 128
 #define MLP_BK 64
-#define MLP_STAGES 4
+#define MLP_STAGES 6  // most ring stages (BN 128: 6 x 32 KB; BN 256: 4 x 48 KB)
 #define MLP_THREADS 384
 #define MLP_EPI_WARP0 4
 #define MLP_NEPI 8
@@ -423,7 +423,7 @@ static bool make_map(CUtensorMap* map, const void* ptr, int rows, int cols, int 
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-static int mlp_stages(int bn) { return 4; }
+static int mlp_stages(int bn) { return bn == 128 ? MLP_STAGES : 4; }
 
 size_t bt_mlp_gemm_smem(int bn) {
     return 1024 + (size_t)mlp_stages(bn) * (MLP_BM * MLP_BK * 2 + (size_t)bn * MLP_BK * 2) +
@@ -478,6 +478,25 @@ __global__ void k_mlp_pack(const float* __restrict__ x, int rows, int cols, int 
         const __nv_bfloat16 b = __float2bfloat16_rn(v);
         out[e] = b;
         if (out_t) out_t[(size_t)c * rows_out + r] = b;
+    }
+}
+
+// Row-major form only (no transposed copy), 8 columns per thread and one
+// 16-byte store; needs ld_out % 8 == 0, a 16-byte aligned `out` and
+// rows_out * ld_out / 8 < 2^31.
+__global__ void k_mlp_pack8(const float* __restrict__ x, int rows, int cols, int cpr, int nchunk,
+                            __nv_bfloat16* __restrict__ out) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nchunk; e += gridDim.x * blockDim.x) {
+        const int r = e / cpr, c0 = (e - r * cpr) * 8;
+        __align__(16) __nv_bfloat162 b[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int c = c0 + 2 * k;
+            const float v0 = (r < rows && c < cols) ? x[(size_t)r * cols + c] : 0.f;
+            const float v1 = (r < rows && c + 1 < cols) ? x[(size_t)r * cols + c + 1] : 0.f;
+            b[k] = __floats2bfloat162_rn(v0, v1);
+        }
+        *reinterpret_cast<uint4*>(out + (size_t)e * 8) = *reinterpret_cast<const uint4*>(b);
     }
 }
 
@@ -587,6 +606,11 @@ static int mlp_grid(long long n) {
 
 cudaError_t bt_launch_mlp_pack(const float* x, int rows, int cols, int ld_out, int rows_out, __nv_bfloat16* out,
                                __nv_bfloat16* out_t, cudaStream_t stream) {
+    const long long nchunk = (long long)rows_out * ld_out / 8;
+    if (!out_t && ld_out % 8 == 0 && ((uintptr_t)out & 15) == 0 && nchunk < (1LL << 31)) {
+        k_mlp_pack8<<<mlp_grid(nchunk), 256, 0, stream>>>(x, rows, cols, ld_out / 8, (int)nchunk, out);
+        return cudaGetLastError();
+    }
     k_mlp_pack<<<mlp_grid((long long)rows_out * ld_out), 256, 0, stream>>>(x, rows, cols, ld_out, rows_out, out, out_t);
     return cudaGetLastError();
 }
@@ -617,13 +641,15 @@ cudaError_t bt_launch_mlp_adam(const float* partials, int nsplit, const float* g
 //   out[n][0] = 0, out[n][1 + j] = lin_j + y[n][j] * scale / (wl[n] * 1e9)   (waves)
 //   err_nm[n] = scale * exp(y[n][err_col])
 // FP64 for the linear part, which carries most of the signal.
-// Linear model in float-float on the FP32 pipe (theta as hi/lo float
-// pairs; each term's product error recovered with an FMA, the sum
-// compensated: ~48-bit accuracy, far below the model's own error), the
-// network's residual added in FP64 with one reciprocal per sample.
+// Everything on the FP32 pipe: the linear model in float-float (theta as
+// hi/lo float pairs; each term's product error recovered with an FMA, the
+// sum compensated: ~48-bit accuracy, far below the model's own error), the
+// network's residual (a bf16 network's output) converted to waves in FP32
+// and added into the float-float sum.  Only the final conversion of each
+// coefficient to double uses the FP64 pipe.
 __global__ void k_surrogate_combine(const float* __restrict__ feat, int nfeat, int nlin, const int* __restrict__ grp,
                                     const float2* __restrict__ theta, const float* __restrict__ y, int ldy,
-                                    const double* __restrict__ wl, double scale, int J, int err_col,
+                                    const double* __restrict__ wl, float scale, int J, int err_col,
                                     double* __restrict__ out, float* __restrict__ err_nm, int n) {
     const long long total = (long long)n * J;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
@@ -642,12 +668,14 @@ __global__ void k_surrogate_combine(const float* __restrict__ feat, int nfeat, i
             lo += ((hi - (sum - bb)) + (p - bb)) + pe;
             hi = sum;
         }
-        const double lin = (double)hi + (double)lo;
-        const double to_waves = scale / (wl[s] * 1e9);
-        out[(size_t)s * (J + 1) + 1 + j] = fma((double)y[(size_t)s * ldy + j], to_waves, lin);
+        const float r = y[(size_t)s * ldy + j] * (scale / ((float)wl[s] * 1e9f));
+        const float sum = hi + r;
+        const float bb = sum - hi;
+        lo += (hi - (sum - bb)) + (r - bb);
+        out[(size_t)s * (J + 1) + 1 + j] = (double)sum + (double)lo;
         if (j == 0) {
             out[(size_t)s * (J + 1)] = 0.0;
-            if (err_nm) err_nm[s] = (float)(scale * exp((double)y[(size_t)s * ldy + err_col]));
+            if (err_nm) err_nm[s] = scale * expf(y[(size_t)s * ldy + err_col]);
         }
     }
 }
@@ -658,6 +686,6 @@ cudaError_t bt_launch_surrogate_combine(const float* feat, int nfeat, int nlin, 
     if (n <= 0) return cudaSuccess;
     k_surrogate_combine<<<mlp_grid((long long)n * J), 256, 0, stream>>>(feat, nfeat, nlin, grp,
                                                                          reinterpret_cast<const float2*>(theta), y, ldy, wl,
-                                                                         scale, J, err_col, out, err_nm, n);
+                                                                         (float)scale, J, err_col, out, err_nm, n);
     return cudaGetLastError();
 }
