@@ -39,7 +39,7 @@
 
 #define MLP_BM 128
 #define MLP_BK 64
-#define MLP_STAGES 6  // most ring stages (BN 128: 6 x 32 KB; BN 256: 4 x 48 KB)
+#define MLP_STAGES 4
 #define MLP_THREADS 384
 #define MLP_EPI_WARP0 4
 #define MLP_NEPI 8
@@ -423,7 +423,7 @@ static bool make_map(CUtensorMap* map, const void* ptr, int rows, int cols, int 
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-static int mlp_stages(int bn) { return bn == 128 ? MLP_STAGES : 4; }
+static int mlp_stages(int bn) { return MLP_STAGES; }
 
 size_t bt_mlp_gemm_smem(int bn) {
     return 1024 + (size_t)mlp_stages(bn) * (MLP_BM * MLP_BK * 2 + (size_t)bn * MLP_BK * 2) +
