@@ -15,8 +15,9 @@
 //   * warps 4..11 read it back with tcgen05.ld (warp w owns TMEM lanes
 //     32(w%4)..32(w%4)+31 = tile rows, and half (w-4)/4 of the columns) and
 //     run the epilogue while the next tile accumulates in the other buffer;
-//     bf16 outputs go through a per-warp 32 x 64 staging tile in shared
-//     memory (128-byte swizzle) and leave by TMA store, whole lines at a time.
+//     outputs go through a per-warp 4 KB staging tile in shared memory
+//     (32 rows x 64 bf16 or 32 FP32 columns, 128-byte swizzle) and leave by
+//     TMA store, whole lines at a time.
 // Every wait is bounded: on expiry the CTA records BT_ERR_TIMEOUT in the
 // device status word, stops issuing, waits (bounded) for the copies and
 // MMAs it started, frees its TMEM and returns.
@@ -279,7 +280,6 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
         // epilogue: warp w reads TMEM lanes 32 (w % 4).. and half (w - 4) / 4 of the columns
         const int q = warp & 3, half = (warp - MLP_EPI_WARP0) >> 2;
         unsigned char* stg = sStg + (warp - MLP_EPI_WARP0) * MLP_STG_BYTES;
-        const bool tma_out = (g.mode == MLP_EPI_GELU || g.mode == MLP_EPI_DGELU);
         int it = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
             const int b = it & 1;
@@ -306,17 +306,28 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
                 }
                 float v[32];
                 tmem_ld32(trow + (uint32_t)c, v);
-                if (g.mode == MLP_EPI_F32) {
-                    float* o = g.out32 + (size_t)kz * g.M * g.N + (size_t)m * g.N + nb;
+                if (g.mode == MLP_EPI_F32 || g.mode == MLP_EPI_BIAS) {
+                    // row `lane` of a 32 x 32 FP32 staging tile (128-byte
+                    // rows, chunk j at j ^ (row % 8)), stored by TMA
+                    if (g.mode == MLP_EPI_BIAS) {
 #pragma unroll
-                    for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(o + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
-                } else if (g.mode == MLP_EPI_BIAS) {
-                    float* o = g.out32 + (size_t)m * g.N + nb;
-#pragma unroll
-                    for (int i = 0; i < 32; i += 4) {
-                        const float4 bb = pre[i / 4];
-                        *reinterpret_cast<float4*>(o + i) = make_float4(v[i] + bb.x, v[i + 1] + bb.y, v[i + 2] + bb.z, v[i + 3] + bb.w);
+                        for (int i = 0; i < 32; i += 4) {
+                            const float4 bb = pre[i / 4];
+                            v[i] += bb.x;
+                            v[i + 1] += bb.y;
+                            v[i + 2] += bb.z;
+                            v[i + 3] += bb.w;
+                        }
                     }
+                    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                    __syncwarp();
+#pragma unroll
+                    for (int j = 0; j < 8; j++)
+                        *reinterpret_cast<float4*>(stg + lane * 128 + ((j ^ (lane & 7)) << 4)) =
+                            make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) tma_store_2d(&tmH, stg, nb, kz * g.M + m0 + q * 32);
                 } else {
                     float h[32];
                     if (g.mode == MLP_EPI_GELU) {
@@ -376,8 +387,8 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
             __syncwarp();
             if (lane == 0) mbar_arrive(&acc_empty[b]);
         }
-        // bf16 tiles stored by TMA are complete before the CTA exits
-        if (tma_out && lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+        // tiles stored by TMA are complete before the CTA exits
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     }
     __syncwarp();
     mbar_wait(&done, 0, abort);
@@ -423,6 +434,21 @@ static bool make_map(CUtensorMap* map, const void* ptr, int rows, int cols, int 
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Row-major FP32 matrix [rows][cols] viewed as (cols, rows) with a box of
+// 32 x 32 elements (128-byte rows) and 128-byte swizzle: the epilogue's
+// FP32 staging tile.
+static bool make_map_f32(CUtensorMap* map, const void* ptr, long long rows, int cols) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)cols * 4};
+    cuuint32_t box[2] = {32, 32};
+    cuuint32_t estr[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 static int mlp_stages(int bn) { return MLP_STAGES; }
 
 size_t bt_mlp_gemm_smem(int bn) {
@@ -434,6 +460,7 @@ cudaError_t bt_launch_mlp_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, c
                                cudaStream_t stream) {
     if (a.M % MLP_BM || (a.bn != 128 && a.bn != 256) || a.N % a.bn || splitk < 1 || a.K % (splitk * MLP_BK))
         return cudaErrorInvalidValue;
+    if (splitk > 1 && a.mode != MLP_EPI_F32) return cudaErrorInvalidValue;  // only partials are split
     if (((uintptr_t)A & 15) || ((uintptr_t)B & 15)) return cudaErrorInvalidValue;
     CUtensorMap ta, tb, th;
     if (!make_map(&ta, A, a.M, a.K, MLP_BM) || !make_map(&tb, B, a.N, a.K, a.bn)) return cudaErrorInvalidValue;
@@ -441,6 +468,12 @@ cudaError_t bt_launch_mlp_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, c
     if (a.mode == MLP_EPI_GELU || a.mode == MLP_EPI_DGELU) {
         // bf16 output [M][N], stored in boxes of 64 columns x 32 rows
         if (!a.h16 || ((uintptr_t)a.h16 & 15) || !make_map(&th, a.h16, a.M, a.N, 32)) return cudaErrorInvalidValue;
+    } else {
+        // FP32 output [splitk x M][N] (split-K partials stacked) or [M][N],
+        // stored in boxes of 32 columns x 32 rows
+        const long long rows = (long long)a.M * (a.mode == MLP_EPI_F32 ? splitk : 1);
+        if (!a.out32 || ((uintptr_t)a.out32 & 15) || !make_map_f32(&th, a.out32, rows, a.N))
+            return cudaErrorInvalidValue;
     }
     if ((a.mode == MLP_EPI_BIAS || a.mode == MLP_EPI_GELU) && (!a.bias || ((uintptr_t)a.bias & 15)))
         return cudaErrorInvalidValue;

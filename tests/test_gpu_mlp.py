@@ -98,6 +98,12 @@ def test_gemm_rejects_bad_shapes():
     out = torch.empty(100, 128, device=dev)
     with pytest.raises(_lib.BatoidError):
         _gemm(A, B, 100, 128, 64, 128, 0, out32=out)
+    # split K only for the FP32 partials
+    A = torch.zeros(128, 128, device=dev, dtype=BF)
+    bias = torch.zeros(128, device=dev)
+    out = torch.empty(128, 128, device=dev)
+    with pytest.raises(_lib.BatoidError):
+        _gemm(A, torch.zeros(128, 128, device=dev, dtype=BF), 128, 128, 128, 128, 1, splitk=2, bias=bias, out32=out)
 
 
 def test_gradients_match_numpy_oracle():
