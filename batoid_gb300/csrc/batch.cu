@@ -258,7 +258,8 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
     double* pool = reinterpret_cast<double*>(smem + hdr->off_pool);
     BatchSmem L = bt_batch_smem_layout(blob_bytes, T, J);
     double* mc = reinterpret_cast<double*>(smem + L.mc);
-    double* opdbuf = A.scratch + (size_t)blockIdx.x * A.scratch_stride;  // this block's per-ray OPD (NaN: vignetted)
+    __shared__ int s_last;
+    const int nchunk = A.nchunk;
     double* gcorr = reinterpret_cast<double*>(smem + L.gcorr);
     double* zv = reinterpret_cast<double*>(smem + L.zv) + warp * 32;
     double* G = reinterpret_cast<double*>(smem + L.G);
@@ -274,20 +275,25 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
     const int modal_off = (A.modal_surf >= 0) ? P.surfs[A.modal_surf].off : 0;
     double* gw = gcorr + warp * NT;
 
+    // work items: (queue entry q, chunk c of its rays); nchunk = 1 gives a
+    // whole job per item
     for (;;) {
         if (tid == 0) s_q = atomicAdd(A.counter, 1);
         __syncthreads();
-        const int q = s_q;
-        if (q >= A.nqueue) break;
+        const int item = s_q;
+        if (item >= A.nqueue * nchunk) break;
+        const int q = item / nchunk, chunk = item - q * nchunk;
         const int job = A.order[q];
         const int s = job / A.nfields, f = job - s * A.nfields;
         const int nx = A.nxs[s];
         const double wl = A.wl[s];
         const long long boff = (nx >= 1 && nx <= A.nx_cap) ? A.basis_off[nx] : -1;
         if (boff < 0) {
-            // grid size without prepared fit tables
-            if (tid == 0) A.status[job] = BT_BATCH_BAD_NX;
-            for (int j = tid; j <= J; j += T) A.coefs[(size_t)job * (J + 1) + j] = NAN;
+            // grid size without prepared fit tables (reported by chunk 0)
+            if (chunk == 0) {
+                if (tid == 0) A.status[job] = BT_BATCH_BAD_NX;
+                for (int j = tid; j <= J; j += T) A.coefs[(size_t)job * (J + 1) + j] = NAN;
+            }
             __syncthreads();
             continue;
         }
@@ -314,13 +320,21 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
         const double* F = A.field + (size_t)f * 18;
         const int nray = nx * nx;
         const double* Z = A.basis + boff;
+        // this job's per-ray OPD (NaN: vignetted): the block's own row, or
+        // the queue entry's row shared by the job's chunks
+        double* opdbuf = A.scratch + (size_t)(nchunk > 1 ? q : blockIdx.x) * A.scratch_stride;
+        // this chunk's rays [r0, r1), whole rounds of T
+        const int per = ((nray + nchunk - 1) / nchunk + T - 1) / T * T;
+        const int r0 = chunk * per < nray ? chunk * per : nray;
+        const int r1 = r0 + per < nray ? r0 + per : nray;
         // chief ray: the grid's centre point (batoid/analysis.py:340-343),
         // traced by thread 0 in a first pass of its own
         const int cridx = (nx % 2 == 0) ? (nx / 2) * nx + nx / 2 : (nx * nx - 1) / 2;
-        for (int base = -T; base < nray; base += T) {
-            const bool chief = base < 0;
+        // (a chunk without rays only counts itself)
+        for (int base = (r0 < r1 ? r0 - T : r1); base < r1; base += T) {
+            const bool chief = base < r0;
             const int i = chief ? cridx : base + tid;
-            const bool active = chief ? (tid == 0) : (i < nray);
+            const bool active = chief ? (tid == 0) : (i < r1);
             RayState r;
             double gx = 0.0, gy = 0.0;
             int cm = -1;
@@ -344,6 +358,15 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
             if (active) opdbuf[i] = r.vig ? (double)NAN : (s_t0 - r.t) / wl;
         }
         __syncthreads();
+        if (nchunk > 1) {
+            // the block finishing a job's last chunk fits it: every chunk's
+            // OPDs are visible device-wide before its count is
+            __threadfence();
+            if (tid == 0) s_last = (atomicAdd(A.jobcnt + q, 1) == nchunk - 1);
+            __syncthreads();
+            if (!s_last) continue;
+            __threadfence();
+        }
         // B^T v: warp w sums rows j = w, w + nwarps, ... of Z^T opd, every
         // lane over points i = lane, lane + 32, ... (independent accumulators)
         {
@@ -353,7 +376,7 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
 #pragma unroll
                 for (int q = 0; q < 8; q++) acc[q] = 0.0;
                 for (int i = lane; i < nray; i += 32) {
-                    const double o = opdbuf[i];
+                    const double o = __ldcg(opdbuf + i);
                     if (o == o) {
 #pragma unroll
                         for (int q = 0; q < 8; q++)
@@ -376,7 +399,7 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
             if (i < nray) {
                 double gx, gy;
                 bt_grid_point(nx, i, A.pupil, &gx, &gy);
-                const double o = opdbuf[i];
+                const double o = __ldcg(opdbuf + i);
                 valid = (o == o);
                 inref = bt_in_annulus(gx, gy, A.r_in2, A.r_out2);
             }
@@ -476,11 +499,15 @@ cudaError_t bt_launch_batch_zernike(const unsigned char* d_blob, int blob_bytes,
     if (a.nqueue <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(int), stream);
     if (e != cudaSuccess) return e;
+    if (a.nchunk > 1) {
+        e = cudaMemsetAsync(a.jobcnt, 0, sizeof(int) * (size_t)a.nqueue, stream);
+        if (e != cudaSuccess) return e;
+    }
     e = cudaMemsetAsync(a.status, 0xff, sizeof(int) * (size_t)a.njobs, stream);
     if (e != cudaSuccess) return e;
     const size_t smem = bt_batch_smem_layout(blob_bytes, threads, a.jmax).total;
     long long grid = (long long)bt_sm_count() * ctas_per_sm;
-    if (grid > a.nqueue) grid = a.nqueue;
+    if (grid > (long long)a.nqueue * a.nchunk) grid = (long long)a.nqueue * a.nchunk;
     if (grid < 1) grid = 1;
     k_batch_zernike<<<(int)grid, threads, smem, stream>>>(d_blob, blob_bytes, a);
     return cudaGetLastError();

@@ -34,10 +34,12 @@ struct BatchArgs {
     const long long* basis_off;   // [nx_cap + 1], -1 where absent
     const double* gref;           // [nx_cap + 1][jmax][jmax]
     // schedule and outputs
-    double* scratch;        // per block: OPD of every ray of its current job
-    long long scratch_stride;  // doubles per block (>= the largest nx * nx)
+    double* scratch;        // OPD of every ray of a job: one row per block, or per queue entry when split
+    long long scratch_stride;  // doubles per row (>= the largest nx * nx)
     const int* order;   // [njobs] job ids (s * nfields + f) in scheduling order
-    int* counter;       // queue head, zeroed before each launch
+    int* counter;       // queue head (work items), zeroed before each launch
+    int* jobcnt;        // [nqueue] finished chunks per job when split, zeroed before each launch
+    int nchunk;         // blocks sharing one job's rays (1: a job per block)
     double* coefs;      // [njobs][jmax + 1]
     int* status;        // [njobs]
     int njobs;          // nstates * nfields (status / coefs extent)

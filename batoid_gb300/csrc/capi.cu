@@ -1370,6 +1370,7 @@ struct bt_batch {
     double* d_basis = nullptr;
     double* d_gref = nullptr;
     int* d_counter = nullptr;
+    int* d_jobcnt = nullptr;  // finished chunks per queue entry (split jobs)
     double* d_scratch = nullptr;  // per block: OPD of each ray of its job
     long long scratch_stride = 0;
     std::mutex mu;
@@ -1385,6 +1386,7 @@ static void batch_free(bt_batch* b) {
     if (b->d_basis) cudaFree(b->d_basis);
     if (b->d_gref) cudaFree(b->d_gref);
     if (b->d_counter) cudaFree(b->d_counter);
+    if (b->d_jobcnt) cudaFree(b->d_jobcnt);
     if (b->d_scratch) cudaFree(b->d_scratch);
     delete b;
 }
@@ -1523,6 +1525,8 @@ extern "C" int bt_batch_create(const bt_batch_desc* d, bt_batch** out) {
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_gref, ngref * sizeof(double));
     if (e == cudaSuccess) e = cudaMemset(b->d_gref, 0, ngref * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_counter, sizeof(int));
+    if (e == cudaSuccess)
+        e = cudaMalloc((void**)&b->d_jobcnt, sizeof(int) * (size_t)bt_sm_count() * BT_BATCH_MAX_CTAS_PER_SM);
     if (e == cudaSuccess) e = bt_batch_set_smem_limit();
     if (e != cudaSuccess) {
         cudaGetLastError();  // leave no error behind for the next launch check
@@ -1614,7 +1618,8 @@ static int batch_args(bt_batch* b, int nstates, const double* xf, const double* 
     if (nstates < 0 || nfields < 0) return fail(BT_ERR_ARG, "batch: negative sizes");
     if ((long long)nstates * nfields > 0x7fffffffLL) return fail(BT_ERR_UNSUPPORTED, "batch: too many jobs");
     if (threads < 32 || threads > BT_BATCH_MAX_THREADS || threads % 32 != 0)
-        return fail(BT_ERR_ARG, "batch: threads must be 32..128, a multiple of 32");
+        return fail(BT_ERR_ARG, "batch: threads must be 32.." + std::to_string(BT_BATCH_MAX_THREADS) +
+                                    ", a multiple of 32");
     if (ctas_per_sm < 1 || ctas_per_sm > BT_BATCH_MAX_CTAS_PER_SM)
         return fail(BT_ERR_ARG, "batch: ctas_per_sm must be 1..8");
     if (niter < 0) return fail(BT_ERR_ARG, "batch: negative niter");
@@ -1643,6 +1648,16 @@ static int batch_args(bt_batch* b, int nstates, const double* xf, const double* 
     a->status = status;
     a->njobs = njobs;
     a->nqueue = (nqueue <= 0 || nqueue > njobs) ? njobs : nqueue;
+    a->jobcnt = b->d_jobcnt;
+    // fewer jobs than blocks: each job's rays are split over several blocks
+    // (scratch rows and chunk counters per queue entry, both sized for
+    // SMs x BT_BATCH_MAX_CTAS_PER_SM entries)
+    const long long blocks = (long long)bt_sm_count() * ctas_per_sm;
+    a->nchunk = 1;
+    if (a->nqueue > 0 && a->nqueue < blocks) {
+        const long long c = (blocks + a->nqueue - 1) / a->nqueue;
+        a->nchunk = (int)(c < 32 ? c : 32);
+    }
     a->nfields = nfields;
     a->nx_cap = BT_BATCH_MAX_NX;
     a->nvar = b->nvar;

@@ -349,8 +349,10 @@ int bt_batch_prepare(bt_batch* b, int n, const int* nx_values, void* stream);
  * s*nfields+f to run, in scheduling order (nqueue <= 0: all nstates*nfields
  * jobs, order holding each once).  Outputs coefs[job][jmax+1] (waves, entry
  * 0 = 0) and status[job] (0, BT_ERR_ARG for a grid size not prepared,
- * BT_ERR_RANK, -1 if not run).  threads: 32..128, a multiple of 32;
- * ctas_per_sm 1..8.  Stream-ordered. */
+ * BT_ERR_RANK, -1 if not run).  threads: 32..256, a multiple of 32;
+ * ctas_per_sm 1..8.  With fewer jobs than thread blocks (SMs x
+ * ctas_per_sm) each job's rays are split over several blocks; results are
+ * the same.  Stream-ordered. */
 int bt_batch_zernike(bt_batch* b, int nstates, const double* xf, const double* det, const double* amps,
                      const int* nx, const double* wavelength, int nfields, const double* fields,
                      const int* order, int nqueue, double* coefs, int* status, int threads, int ctas_per_sm,

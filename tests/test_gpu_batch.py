@@ -137,3 +137,34 @@ def test_autotuner_picks_a_valid_shape(pt, tmp_path, monkeypatch):
     cfg = autotune.batch_config(pt, nstates=8)
     assert cfg in autotune.CANDIDATES
     assert (tmp_path / "autotune.json").exists()
+
+
+def test_split_jobs_match_whole_jobs(pt):
+    """Fewer jobs than blocks splits each job's rays over several blocks (the
+    last one to finish fits); more jobs than blocks gives each job to one
+    block.  Both schedules give the same fits."""
+    S = 120  # 360 jobs > 152 blocks at 256 threads x 1 per SM: whole jobs
+    dofs = _dofs(pt, S, 17)
+    rng = np.random.default_rng(4)
+    nx = rng.integers(24, 61, S)
+    wl = rng.choice([400e-9, 650e-9, 900e-9], S)
+    pt.prepare(nx)
+    inp = pt.device_inputs(dofs, nx, wl)
+    F, J = len(pt.fields), pt.jmax
+    coefs = torch.empty(S * F * (J + 1), dtype=torch.float64, device=D.device())
+    status = torch.empty(S * F, dtype=torch.int32, device=D.device())
+    pt.launch(inp, coefs, status, 256, 1)
+    torch.cuda.synchronize()
+    assert np.all(D.to_host(status) == 0)
+    whole = D.to_host(coefs).reshape(S * F, J + 1)
+    # 10 of the jobs on their own: split over ~15 blocks each
+    sub = np.array([0, 7, 33, 58, 101, 150, 222, 299, 300, 359], dtype=np.int32)
+    order = torch.from_numpy(sub).to(D.device())
+    c2 = torch.full((S * F * (J + 1),), float("nan"), dtype=torch.float64, device=D.device())
+    s2 = torch.empty(S * F, dtype=torch.int32, device=D.device())
+    pt.launch(inp, c2, s2, 256, 1, order=order)
+    torch.cuda.synchronize()
+    st = D.to_host(s2)
+    assert np.all(st[sub] == 0)
+    got = D.to_host(c2).reshape(S * F, J + 1)[sub]
+    np.testing.assert_allclose(got, whole[sub], rtol=0, atol=1e-9)
