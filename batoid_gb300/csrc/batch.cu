@@ -343,7 +343,7 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
             // stage-synchronous: all warps of the block run the same stage's
             // code together (instruction-cache working set of one stage)
             for (int k = 0; k < A.ntrace; k++) {
-                if (active) run_stage(P, stages[k], r, A.niter, cm, cn, cin);
+                if (active) run_stage<true>(P, stages[k], r, A.niter, cm, cn, cin);
                 __syncthreads();
             }
             if (active) {

@@ -67,6 +67,7 @@ static __device__ __noinline__ void bt_screen_deflect(const Prog P, int surf, in
 // keeps its previous coordinates; TIR writes the position, NaN velocity.
 // A medium's index and its reciprocal depend only on the ray's wavelength,
 // so they are computed once per ray per medium.
+template <bool PRESTEP = false>
 __device__ __forceinline__ void run_stage(const Prog& P, const bt_stage& st, RayState& r, int niter,
                                           int& cached_medium, double& cached_n, double& cached_inv_n) {
     if (st.kind != BT_ST_OBSCURE && !r.fail) {
@@ -87,7 +88,7 @@ __device__ __forceinline__ void run_stage(const Prog& P, const bt_stage& st, Ray
             vz = r.vx * st.drot[2] + r.vy * st.drot[5] + r.vz * st.drot[8];
         }
         double dt = 0.0;
-        const bool ok = bt_surf_tti_fast(P, st.surf, x, y, z, vx, vy, vz, dt, niter);
+        const bool ok = bt_surf_tti_fast<PRESTEP>(P, st.surf, x, y, z, vx, vy, vz, dt, niter);
         if (ok) {
             x += vx * dt;
             y += vy * dt;

@@ -187,6 +187,10 @@ static void fill_quadric(bt_surf& r, double R, double conic) {
     // its absolute rounding error is ~|R/(1+k)| ulp(1)
     const double rc = R / cp1;
     r.p[10] = (R != 0.0 && cp1 != 0.0 && isfinite(rc) && fabs(rc) <= 100.0) ? 1.0 : 0.0;
+    // FP32 copies of (1+k)/R^2 and 1/R, packed in p[11], for the trace
+    // kernel's FP32 Newton pre-step on aspheres
+    const float f2[2] = {(float)r.p[8], (float)r.p[9]};
+    memcpy(&r.p[11], f2, sizeof(f2));
 }
 
 extern "C" int bt_quadric_create(double R, double conic, bt_surface** out) {
