@@ -84,3 +84,4 @@ cudaError_t bt_launch_zk_normal(const double* x, const double* y, const double* 
                                 cudaStream_t stream);
 
 int bt_sm_count();
+void bt_keep_pool();  // keep the default pool's freed scratch cached (once per process)

@@ -595,6 +595,7 @@ struct TempBlob {
     cudaError_t upload(const std::vector<unsigned char>& b, cudaStream_t s) {
         stream = s;
         bytes = (int)b.size();
+        bt_keep_pool();
         cudaError_t e = cudaMallocAsync((void**)&d, b.size(), s);
         if (e != cudaSuccess) { d = nullptr; return e; }
         return cudaMemcpyAsync(d, b.data(), b.size(), cudaMemcpyHostToDevice, s);
@@ -931,6 +932,7 @@ extern "C" int bt_rv_sum_amplitude(const bt_rayvector* rv, double x, double y, d
     if (rv->size == 0) return BT_OK;
     cudaStream_t s = (cudaStream_t)stream;
     double* d = nullptr;
+    bt_keep_pool();
     CUDA_TRY(cudaMallocAsync((void**)&d, 2 * sizeof(double), s), "sumAmplitude");
     cudaError_t e = bt_launch_sum_amplitude(to_rv(rv), x, y, z, t, ignore_vignetted != 0, d, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -951,6 +953,7 @@ extern "C" int bt_rv_equal(const bt_rayvector* a, const bt_rayvector* b, int* ou
     cudaStream_t s = (cudaStream_t)stream;
     int* d = nullptr;
     int one = 1;
+    bt_keep_pool();
     CUDA_TRY(cudaMallocAsync((void**)&d, sizeof(int), s), "equal");
     cudaError_t e = cudaMemcpyAsync(d, &one, sizeof(int), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = bt_launch_rv_equal(to_rv(a), to_rv(b), d, s);
@@ -1233,6 +1236,7 @@ extern "C" int bt_measure_fp64_peak(int iters, double* tflops, void* stream) {
     if (!tflops || iters < 8) return fail(BT_ERR_ARG, "fp64 probe: bad arguments");
     cudaStream_t s = (cudaStream_t)stream;
     double* sink = nullptr;
+    bt_keep_pool();
     CUDA_TRY(cudaMallocAsync((void**)&sink, sizeof(double), s), "fp64 probe");
     float ms = 0.f;
     double flops = 0.0;

@@ -196,6 +196,7 @@ cudaError_t bt_launch_huygens(const RV& rv, double px, double py, double pz, con
     const size_t rec_bytes = (size_t)rv.n * sizeof(HuyRec);
     const size_t part_bytes = (size_t)nsplit * npix * sizeof(double);
     char* scratch = nullptr;
+    bt_keep_pool();
     cudaError_t e = cudaMallocAsync((void**)&scratch, rec_bytes + 2 * part_bytes, stream);
     if (e != cudaSuccess) return e;
     HuyRec* rec = reinterpret_cast<HuyRec*>(scratch);

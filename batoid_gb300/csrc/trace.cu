@@ -83,6 +83,25 @@ k_trace(const unsigned char* __restrict__ gblob, int blob_bytes, RV in, RV out,
 
 static int g_sm_count = 0;
 
+// The library's short-lived scratch comes from the device's default memory
+// pool (cudaMallocAsync).  By default the pool returns freed memory to the
+// driver at every synchronisation, so each call would map its scratch anew;
+// keeping up to 256 MiB cached makes repeated calls reuse it.  A property of
+// this process's pool, set once.
+void bt_keep_pool() {
+    static bool done = false;
+    if (done) return;
+    done = true;
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    uint64_t keep = 256ull << 20;
+    if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) cudaGetLastError();
+}
+
 int bt_sm_count() {
     if (g_sm_count == 0) {
         int dev = 0;
