@@ -55,6 +55,24 @@ def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def reduce_step_time(ms, world, device):
+    """Timed region of the whole job: the max over ranks (every rank must
+    call it; identity for one rank)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank, world, per_unit, steps, ms):
+    """Whole-job rate: the units all ranks processed over the job's time
+    (weak scaling: every rank traces its own batch)."""
+    return units_per_rank * world * per_unit * steps / (ms * 1e-3)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
 
@@ -551,13 +569,10 @@ def run_gpu(args):
         dist.barrier()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reduce_step_time(ms, world, "cuda")
     ms_per_step = ms / args.steps
     total_rays = n * world
-    value = total_rays * nsurf * args.steps / (ms * 1e-3)
+    value = job_throughput(n, world, nsurf, args.steps, ms)
 
     # sanity: the benchmark traced real rays
     vig = float(rv_out.field("vignetted").float().mean().item())
