@@ -173,7 +173,7 @@ class MLP:
 
 class WavefrontSurrogate:
     """Zernike coefficients of a ``PerturbedTelescope`` from its dofs, field
-    and wavelength, with the batched trace as fallback and judge.
+    and wavelength, with the batched trace as fallback and ground truth.
 
     Model: c = c_lin + r, with c_lin a least-squares linear model in the
     normalised dofs per (field, wavelength) and r (in nm / scale) predicted
@@ -213,7 +213,7 @@ class WavefrontSurrogate:
         return dofs, widx
 
     def trace(self, dofs, widx, chunk=16384, threads=None, ctas_per_sm=None):
-        """Batched-trace coefficients (S, F, J+1) of states (the judge)."""
+        """Batched-trace coefficients (S, F, J+1) of states (the ground truth)."""
         out = []
         for a in range(0, len(dofs), chunk):
             out.append(self.pt.zernike(dofs[a:a + chunk], self.nx, self.wavelengths[widx[a:a + chunk]],

@@ -404,7 +404,7 @@ def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24,
     vc = sur.trace(vd, vw, threads=threads, ctas_per_sm=ctas)
     vf, vg, vwl = sur.features(vd, vw)
     kappa = sur.calibrate(vf, vg, vwl, vc)
-    # held-out: the batched trace (device-resident inputs, graph replay) is the judge and the baseline
+    # held-out: the batched trace (device-resident inputs, graph replay) is the ground truth and the baseline
     hd, hw = sur.sample_states(heldout_states, seed=303)
     inp = pt.device_inputs(hd, 32, W.WAVELENGTHS[hw])
     N = heldout_states * F
