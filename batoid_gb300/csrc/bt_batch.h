@@ -63,7 +63,7 @@ struct BatchArgs {
 };
 
 struct BatchSmem {
-    size_t mc, bacc, gcorr, zv, G, bv, mcf, mcell, total;
+    size_t mc, gcorr, zv, G, bv, mcf, mcell, total;
 };
 
 __host__ __device__ inline BatchSmem bt_batch_smem_layout(int blob_bytes, int T, int J) {
@@ -71,7 +71,6 @@ __host__ __device__ inline BatchSmem bt_batch_smem_layout(int blob_bytes, int T,
     size_t off = ((size_t)blob_bytes + 127) & ~(size_t)127;
     L.mc = off;
     off += (size_t)16 * T * sizeof(double);
-    L.bacc = off;  // unused
     L.gcorr = off;
     off += (size_t)(T / 32) * (J * (J + 1) / 2) * sizeof(double);
     L.zv = off;
