@@ -25,7 +25,7 @@ from .optic import Interface, RefractiveInterface, Mirror, Detector, Baffle, OPD
 from .lattice import Lattice
 from . import utils
 from .constants import globalCoordSys, vacuum
-from .analysis import (huygensPSF, wavefront, zernike, dkdu, drdth, dthdr, spot, fftPSF, zernikeGQ, zernikeTA,
+from .analysis import (huygensPSF, huygensPSFs, wavefront, zernike, dkdu, drdth, dthdr, spot, fftPSF, zernikeGQ, zernikeTA,
                        zernikeXYAberrations, doubleZernike, exitPupilPos, focalLength)
 from . import global_vars
 

@@ -8,11 +8,12 @@ runs on the host.
 from numbers import Real
 
 import numpy as np
+import torch
 
 from . import _device as D
 from . import _lib
 from .lattice import Lattice
-from .rayVector import RayVector
+from .rayVector import RayVector, concatenateRayVectors
 from .utils import bilinear_fit, fieldToDirCos
 from . import zpoly as _zk
 
@@ -41,24 +42,26 @@ def _chief_index(nx):
     return (nx // 2) * nx + nx // 2 if (nx % 2) == 0 else (nx * nx - 1) // 2
 
 
-def huygensPSF(optic, theta_x, theta_y, wavelength, projection='postel', nx=None, dx=None, dy=None,
-               nxOut=None, reference='chief'):
-    """PSF by the Huygens construction |sum_u exp(i phi_u)|^2 on a lattice
-    (batoid/analysis.py:181-305)."""
+def _huygens_lattice(optic, theta_x, theta_y, wavelength, projection, nx, dx, dy):
+    """(primitiveX, pad_factor) of huygensPSF (batoid/analysis.py:181-305)."""
     if dx is None:
         d = optic.pupilSize / (nx - 2) if (nx % 2) == 0 else optic.pupilSize / (nx - 1)
         primitiveU = np.array([[d, 0], [0, d]])
         primitiveK = dkdu(optic, theta_x, theta_y, wavelength, projection=projection).dot(primitiveU)
         pad_factor = 2
-        primitiveX = np.vstack(_reciprocalLatticeVectors(primitiveK[0], primitiveK[1], pad_factor * nx))
-    elif isinstance(dx, Real):
+        return np.vstack(_reciprocalLatticeVectors(primitiveK[0], primitiveK[1], pad_factor * nx)), pad_factor
+    if isinstance(dx, Real):
         if dy is None:
             dy = dx
-        primitiveX = np.vstack([[dx, 0], [0, dy]])
-        pad_factor = 1
-    else:
-        primitiveX = np.vstack([dx, dy])
-        pad_factor = 1
+        return np.vstack([[dx, 0], [0, dy]]), 1
+    return np.vstack([dx, dy]), 1
+
+
+def huygensPSF(optic, theta_x, theta_y, wavelength, projection='postel', nx=None, dx=None, dy=None,
+               nxOut=None, reference='chief'):
+    """PSF by the Huygens construction |sum_u exp(i phi_u)|^2 on a lattice
+    (batoid/analysis.py:181-305)."""
+    primitiveX, pad_factor = _huygens_lattice(optic, theta_x, theta_y, wavelength, projection, nx, dx, dy)
     if nxOut is None:
         nxOut = nx
     dirCos = fieldToDirCos(theta_x, theta_y, projection=projection)
@@ -74,6 +77,61 @@ def huygensPSF(optic, theta_x, theta_y, wavelength, projection='postel', nx=None
     re, im = huygens_amplitudes(rays, (point[0], point[1], 0.0), primitiveX, N, N, time)
     out = Lattice(np.zeros((N, N)), primitiveX)
     out.array = re * re + im * im
+    return out
+
+
+def huygensPSFs(optic, theta_x, theta_y, wavelength, projection='postel', nx=None, dx=None, dy=None,
+                nxOut=None, reference='chief'):
+    """huygensPSF for many field angles (arrays theta_x, theta_y): every
+    field's pupil grid is traced in one launch, the phasor sums of all
+    fields run back to back into one device buffer, and the amplitudes come
+    to the host in one copy.  Element f equals huygensPSF(optic,
+    theta_x[f], theta_y[f], wavelength, ...)."""
+    thx = np.atleast_1d(np.asarray(theta_x, dtype=float))
+    thy = np.atleast_1d(np.asarray(theta_y, dtype=float))
+    if thx.shape != thy.shape:
+        raise ValueError("theta_x and theta_y must have the same shape")
+    F = len(thx)
+    if F == 0:
+        return []
+    if nxOut is None:
+        nxOut = nx
+    lattices, grids = [], []
+    for f in range(F):
+        lattices.append(_huygens_lattice(optic, thx[f], thy[f], wavelength, projection, nx, dx, dy))
+        dirCos = fieldToDirCos(thx[f], thy[f], projection=projection)
+        grids.append(RayVector.asGrid(optic=optic, wavelength=wavelength, dirCos=dirCos, nx=nx))
+    rays = concatenateRayVectors(grids)
+    optic.trace(rays)
+    n = nx * nx
+    if reference == 'mean':
+        r = rays.r
+        vig = rays.vignetted
+        points = [np.mean(r[f * n:(f + 1) * n][~vig[f * n:(f + 1) * n]], axis=0) for f in range(F)]
+    else:
+        idx = torch.as_tensor([f * n + _chief_index(nx) for f in range(F)], device=D.device())
+        points = list(D.to_host(rays._d[0:3, idx]).T)
+    t0 = D.to_host(rays._d[6, torch.as_tensor([f * n for f in range(F)], device=D.device())])
+    sizes = [nxOut * pad for _, pad in lattices]
+    offs = np.concatenate([[0], np.cumsum([N * N for N in sizes])])
+    re = D.empty(int(offs[-1]))
+    im = D.empty(int(offs[-1]))
+    L = _lib.lib()
+    for f in range(F):
+        view = RayVector._fromBuffers(rays._d[:, f * n:(f + 1) * n], rays._b[:, f * n:(f + 1) * n], rays.coordSys)
+        pX = lattices[f][0]
+        lat = np.ascontiguousarray([pX[0][0], pX[0][1], pX[1][0], pX[1][1]], dtype=float)
+        N = sizes[f]
+        _lib.check(L.bt_huygens_amplitudes(
+            view._rv, float(points[f][0]), float(points[f][1]), 0.0, lat.ctypes.data_as(_lib.c_double_p), N, N,
+            float(t0[f]), 1, D.ptr(re) + 8 * int(offs[f]), D.ptr(im) + 8 * int(offs[f]), D.stream_ptr()))
+    re_h, im_h = D.to_host(re), D.to_host(im)
+    out = []
+    for f in range(F):
+        a, b = int(offs[f]), int(offs[f + 1])
+        N = sizes[f]
+        psf = (re_h[a:b] * re_h[a:b] + im_h[a:b] * im_h[a:b]).reshape(N, N)
+        out.append(Lattice(psf, lattices[f][0]))
     return out
 
 

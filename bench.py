@@ -242,10 +242,28 @@ def bench_huygens(bt, opt, nx=256, npix=128, pitch=2e-6, wavelength=620e-9, chec
             ref = rays.sumAmplitude(P, t0)
             err = abs(abs(ref) ** 2 - psf[a, b]) / peak
             max_err = max(max_err, err)
-        kept.append((rays, point, t0))
+        kept.append((rays, point, t0, psf))
+    # all fields in one call (analysis.huygensPSFs: one trace launch, one
+    # copy of the amplitudes to the host), same lattice and pixels
+    thx = np.deg2rad([f[0] for f in HUYGENS_FIELDS])
+    thy = np.deg2rad([f[1] for f in HUYGENS_FIELDS])
+    A.huygensPSFs(opt, thx, thy, wavelength, nx=nx, dx=pitch, nxOut=npix)  # warm-up
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    multi = A.huygensPSFs(opt, thx, thy, wavelength, nx=nx, dx=pitch, nxOut=npix)
+    ms_multi = (time.perf_counter() - t1) * 1e3
+    # the same through the public per-field call, timed the same way (host
+    # clock around ray generation, trace, sums and the copy back)
+    t1 = time.perf_counter()
+    for f in range(len(thx)):
+        A.huygensPSF(opt, thx[f], thy[f], wavelength, nx=nx, dx=pitch, nxOut=npix)
+    ms_per_field_api = (time.perf_counter() - t1) * 1e3
     out = {
         "workload": f"{len(HUYGENS_FIELDS)} fields x {nx}x{nx} pupil rays x {npix}x{npix} px at {pitch*1e6:.0f} um, "
                     f"{wavelength*1e9:.0f} nm, tma_corrector",
+        "api_wall_ms": {"huygensPSF_per_field": ms_per_field_api, "huygensPSFs_one_call": ms_multi},
+        "fields_per_s_one_call": len(HUYGENS_FIELDS) / (ms_multi * 1e-3),
+        "one_call_max_diff_rel_peak": max(float(np.abs(m.array - (k[3])).max() / k[3].max()) for m, k in zip(multi, kept)),
         "fields_per_s": len(HUYGENS_FIELDS) / (sums["ms_trace_and_psf"] * 1e-3),
         "ray_pixel_pairs_per_s": pairs / (sums["ms_psf_kernels"] * 1e-3),
         "ms_total": sums["ms_trace_and_psf"], "ms_psf": sums["ms_psf_kernels"],
@@ -256,7 +274,7 @@ def bench_huygens(bt, opt, nx=256, npix=128, pitch=2e-6, wavelength=620e-9, chec
         # oracle (C, all threads): per-pixel sumAmplitude on a pixel sample, extrapolated
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as ora
-        rays, point, t0 = kept[4]
+        rays, point, t0, _ = kept[4]
         host = ora.Rays(*[getattr(rays, k) for k in ora.Rays.FIELDS], rays.vignetted, rays.failed)
         npx = 64
         t1 = time.perf_counter()

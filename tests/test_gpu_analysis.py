@@ -72,3 +72,19 @@ def test_doubleZernike_reproduces_field_dependence(optic):
         for az in np.linspace(0, 2 * np.pi, 9, endpoint=False):
             mean += ww * bt.zernikeGQ(optic, rr * np.cos(az), rr * np.sin(az), WL, rings=4, jmax=11, eps=eps) / 18
     np.testing.assert_allclose(dz[1], mean, rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("dx,reference", [(2e-6, "chief"), (None, "chief"), (2e-6, "mean")])
+def test_huygens_psfs_match_per_field_calls(optic, dx, reference):
+    """Many fields in one trace launch and one copy back: each PSF equals
+    the single-field call's."""
+    thx = np.deg2rad([0.0, 0.6, -1.1])
+    thy = np.deg2rad([0.0, -0.4, 0.9])
+    kw = dict(nx=48, dx=dx, nxOut=24, reference=reference)
+    many = bt.huygensPSFs(optic, thx, thy, WL, **kw)
+    assert len(many) == 3
+    for f in range(3):
+        one = bt.huygensPSF(optic, thx[f], thy[f], WL, **kw)
+        assert many[f].array.shape == one.array.shape
+        np.testing.assert_allclose(many[f].primitiveVectors, one.primitiveVectors, rtol=1e-12, atol=0)
+        np.testing.assert_allclose(many[f].array, one.array, rtol=0, atol=1e-9 * one.array.max())
