@@ -162,6 +162,8 @@ _SIGS = [
     ("bt_optic_trace_host", c_int, [_P, ctypes.POINTER(BtRayVector), c_int, c_size_t, _P]),
     ("bt_huygens_amplitudes", c_int, [ctypes.POINTER(BtRayVector), c_double, c_double, c_double, c_double_p,
                                       c_int, c_int, c_double, c_int, _P, _P, _P]),
+    ("bt_huygens_amplitudes_fields", c_int, [ctypes.POINTER(BtRayVector), c_int, c_double_p, c_double_p,
+                                             c_double_p, c_int, c_int, c_int, _P, _P, _P]),
     ("bt_huygens_amplitudes_noalloc", c_int, [ctypes.POINTER(BtRayVector), c_double, c_double, c_double,
                                               c_double_p, c_int, c_int, c_double, c_int, _P, _P, _P]),
     ("bt_zernike_normal_equations", c_int, [_P, _P, _P, _P, c_int, _P, c_int, c_int, _P, _P, _P]),
@@ -182,6 +184,7 @@ _SIGS = [
     ("bt_surrogate_combine", c_int, [_P, c_int, c_int, _P, _P, _P, c_int, _P, c_double, c_int, c_int, _P, _P, c_int,
                                      _P]),
     ("bt_measure_fp64_peak", c_int, [c_int, c_double_p, _P]),
+    ("bt_measure_fp32_peak", c_int, [c_int, c_double_p, _P]),
     ("bt_check_device_status", c_int, [_P]),
 ]
 

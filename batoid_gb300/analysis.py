@@ -38,6 +38,13 @@ def dkdu(optic, theta_x, theta_y, wavelength, nrad=6, naz=36, projection='postel
     return soln[1:]
 
 
+def _check_reference(reference):
+    """The reference point is 'chief' or 'mean'; the reference fails on any
+    other value (its point is never set), so an unknown one is an error."""
+    if reference not in ('chief', 'mean'):
+        raise ValueError(f"reference must be 'chief' or 'mean', not {reference!r}")
+
+
 def _chief_index(nx):
     return (nx // 2) * nx + nx // 2 if (nx % 2) == 0 else (nx * nx - 1) // 2
 
@@ -61,6 +68,7 @@ def huygensPSF(optic, theta_x, theta_y, wavelength, projection='postel', nx=None
                nxOut=None, reference='chief'):
     """PSF by the Huygens construction |sum_u exp(i phi_u)|^2 on a lattice
     (batoid/analysis.py:181-305)."""
+    _check_reference(reference)
     primitiveX, pad_factor = _huygens_lattice(optic, theta_x, theta_y, wavelength, projection, nx, dx, dy)
     if nxOut is None:
         nxOut = nx
@@ -87,6 +95,7 @@ def huygensPSFs(optic, theta_x, theta_y, wavelength, projection='postel', nx=Non
     fields run back to back into one device buffer, and the amplitudes come
     to the host in one copy.  Element f equals huygensPSF(optic,
     theta_x[f], theta_y[f], wavelength, ...)."""
+    _check_reference(reference)
     thx = np.atleast_1d(np.asarray(theta_x, dtype=float))
     thy = np.atleast_1d(np.asarray(theta_y, dtype=float))
     if thx.shape != thy.shape:
@@ -112,26 +121,17 @@ def huygensPSFs(optic, theta_x, theta_y, wavelength, projection='postel', nx=Non
         idx = torch.as_tensor([f * n + _chief_index(nx) for f in range(F)], device=D.device())
         points = list(D.to_host(rays._d[0:3, idx]).T)
     t0 = D.to_host(rays._d[6, torch.as_tensor([f * n for f in range(F)], device=D.device())])
-    sizes = [nxOut * pad for _, pad in lattices]
-    offs = np.concatenate([[0], np.cumsum([N * N for N in sizes])])
-    re = D.empty(int(offs[-1]))
-    im = D.empty(int(offs[-1]))
-    L = _lib.lib()
-    for f in range(F):
-        view = RayVector._fromBuffers(rays._d[:, f * n:(f + 1) * n], rays._b[:, f * n:(f + 1) * n], rays.coordSys)
-        pX = lattices[f][0]
-        lat = np.ascontiguousarray([pX[0][0], pX[0][1], pX[1][0], pX[1][1]], dtype=float)
-        N = sizes[f]
-        _lib.check(L.bt_huygens_amplitudes(
-            view._rv, float(points[f][0]), float(points[f][1]), 0.0, lat.ctypes.data_as(_lib.c_double_p), N, N,
-            float(t0[f]), 1, D.ptr(re) + 8 * int(offs[f]), D.ptr(im) + 8 * int(offs[f]), D.stream_ptr()))
-    re_h, im_h = D.to_host(re), D.to_host(im)
-    out = []
-    for f in range(F):
-        a, b = int(offs[f]), int(offs[f + 1])
-        N = sizes[f]
-        psf = (re_h[a:b] * re_h[a:b] + im_h[a:b] * im_h[a:b]).reshape(N, N)
-        out.append(Lattice(psf, lattices[f][0]))
+    N = nxOut * lattices[0][1]
+    pts = np.ascontiguousarray([[p[0], p[1], 0.0] for p in points], dtype=float)
+    lat = np.ascontiguousarray([[pX[0][0], pX[0][1], pX[1][0], pX[1][1]] for pX, _ in lattices], dtype=float)
+    t0 = np.ascontiguousarray(t0, dtype=float)
+    re = D.empty(F * N * N)
+    im = D.empty(F * N * N)
+    _lib.check(_lib.lib().bt_huygens_amplitudes_fields(
+        rays._rv, F, pts.ctypes.data_as(_lib.c_double_p), lat.ctypes.data_as(_lib.c_double_p),
+        t0.ctypes.data_as(_lib.c_double_p), N, N, 1, D.ptr(re), D.ptr(im), D.stream_ptr()))
+    re_h, im_h = D.to_host(re).reshape(F, N, N), D.to_host(im).reshape(F, N, N)
+    out = [Lattice(re_h[f] * re_h[f] + im_h[f] * im_h[f], lattices[f][0]) for f in range(F)]
     return out
 
 
@@ -153,6 +153,7 @@ def wavefront(optic, theta_x, theta_y, wavelength, projection='postel', nx=32, s
               reference='chief'):
     """OPD in waves on the exit-pupil reference sphere (batoid/analysis.py:308-388)."""
     from .surface import Sphere
+    _check_reference(reference)
     dirCos = fieldToDirCos(theta_x, theta_y, projection=projection)
     rays = RayVector.asGrid(optic=optic, wavelength=wavelength, nx=nx, dirCos=dirCos)
     if sphereRadius is None:

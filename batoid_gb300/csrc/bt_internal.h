@@ -67,12 +67,17 @@ cudaError_t bt_launch_sum_amplitude(const RV& rv, double x, double y, double z, 
                                     double* d_out2, cudaStream_t stream);
 cudaError_t bt_launch_rv_equal(const RV& a, const RV& b, int* d_flag, cudaStream_t stream);
 cudaError_t bt_launch_dfma_probe(int iters, double* sink, float* ms, double* flops, cudaStream_t stream);
+cudaError_t bt_launch_ffma_probe(int iters, double* sink, float* ms, double* flops, cudaStream_t stream);
 
 // huygens.cu
 cudaError_t bt_launch_huygens(const RV& rv, double px, double py, double pz, const double lat[4], int na,
                               int nb, double t0, bool ignore_vig, double* out_re, double* out_im,
                               cudaStream_t stream);
 
+cudaError_t bt_launch_huygens_fields(const RV& rv, long long per_field, int nfields, const double* px,
+                                     const double* py, const double* pz, const double* lat, const double* t0,
+                                     int ps, int na, int nb, bool ignore_vig, double* out_re, double* out_im,
+                                     cudaStream_t stream);
 // huygens.cu, allocation-free variant (file-scope device scratch)
 cudaError_t bt_launch_huygens_noalloc(const RV& rv, double px, double py, double pz, const double lat[4], int na,
                                       int nb, double t0, bool ignore_vig, double* out_re, double* out_im,

@@ -1200,6 +1200,25 @@ extern "C" int bt_huygens_amplitudes(const bt_rayvector* rv, double px, double p
     return BT_OK;
 }
 
+// All fields of huygensPSFs in one launch set: field f's rays are the f-th
+// block of rv->n / nfields rays; points [nfields][3], lat [nfields][4] and
+// t0 [nfields] are host arrays; outputs [nfields][na*nb] on the device.
+extern "C" int bt_huygens_amplitudes_fields(const bt_rayvector* rv, int nfields, const double* points,
+                                            const double* lat, const double* t0, int na, int nb,
+                                            int ignore_vignetted, double* out_re, double* out_im, void* stream) {
+    int rc = check_rv(rv);
+    if (rc != BT_OK) return rc;
+    if (nfields < 1 || !points || !lat || !t0) return fail(BT_ERR_ARG, "huygens fields: bad field arrays");
+    if (na < 0 || nb < 0) return fail(BT_ERR_ARG, "huygens fields: bad lattice");
+    if (rv->size % nfields != 0) return fail(BT_ERR_ARG, "huygens fields: rays are not nfields equal blocks");
+    if ((long long)na * nb == 0) return BT_OK;
+    if (!out_re || !out_im) return fail(BT_ERR_ARG, "huygens fields: null output");
+    CUDA_TRY(bt_launch_huygens_fields(to_rv(rv), (long long)rv->size / nfields, nfields, points, points + 1, points + 2, lat, t0,
+                                      3, na, nb, ignore_vignetted != 0, out_re, out_im, (cudaStream_t)stream),
+             "huygens fields");
+    return BT_OK;
+}
+
 // Same result as bt_huygens_amplitudes, but allocates no device memory: the
 // scratch is a fixed 8 MiB array inside the library (see huygens.cu).
 extern "C" int bt_huygens_amplitudes_noalloc(const bt_rayvector* rv, double px, double py, double pz,
@@ -1244,6 +1263,22 @@ extern "C" int bt_measure_fp64_peak(int iters, double* tflops, void* stream) {
     cudaFreeAsync(sink, s);
     cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e, "fp64 probe");
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    return BT_OK;
+}
+
+extern "C" int bt_measure_fp32_peak(int iters, double* tflops, void* stream) {
+    if (!tflops || iters < 8) return fail(BT_ERR_ARG, "fp32 probe: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    double* sink = nullptr;
+    bt_keep_pool();
+    CUDA_TRY(cudaMallocAsync((void**)&sink, sizeof(double), s), "fp32 probe");
+    float ms = 0.f;
+    double flops = 0.0;
+    cudaError_t e = bt_launch_ffma_probe(iters, sink, &ms, &flops, s);
+    cudaFreeAsync(sink, s);
+    cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "fp32 probe");
     *tflops = flops / (ms * 1e-3) / 1e12;
     return BT_OK;
 }

@@ -39,10 +39,25 @@ __device__ __forceinline__ uint32_t turns_to_fix32(double turns) {
     return (uint32_t)(u & 0xffffffffull);
 }
 
-__global__ void k_huy_prep(RV rv, double px, double py, double pz, double l0, double l1, double l2, double l3,
-                           double t0, int ignore_vig, HuyRec* rec) {
+// Lattice and reference point of one field: amplitudes at
+// P(a, b) = (px, py, pz) + (b - nb/2) (l0, l1, 0) + (a - na/2) (l2, l3, 0).
+struct HuyField {
+    double px, py, pz, l0, l1, l2, l3, t0;
+};
+
+#define HUY_MAX_FIELDS 64
+
+// Up to HUY_MAX_FIELDS fields per launch set, passed by value (4 KB).
+struct HuyFields {
+    HuyField f[HUY_MAX_FIELDS];
+};
+
+// Rays [f * per_field, (f + 1) * per_field) belong to field f.
+__global__ void k_huy_prep(RV rv, long long per_field, const __grid_constant__ HuyFields F, int ignore_vig,
+                           HuyRec* rec) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < rv.n;
          i += (long long)gridDim.x * blockDim.x) {
+        const HuyField& fd = F.f[i / per_field];
         HuyRec r;
         r.pad0 = 0.f;
         r.pad1 = 0.f;
@@ -52,14 +67,14 @@ __global__ void k_huy_prep(RV rv, double px, double py, double pz, double l0, do
             const double v2 = vx * vx + vy * vy + vz * vz;
             const double w = rv.w[i];
             // same ordering as src/rayVector.cpp:208-214, in turns
-            double ph = (px - rv.x[i]) * vx;
-            ph += (py - rv.y[i]) * vy;
-            ph += (pz - rv.z[i]) * vz;
+            double ph = (fd.px - rv.x[i]) * vx;
+            ph += (fd.py - rv.y[i]) * vy;
+            ph += (fd.pz - rv.z[i]) * vz;
             ph /= v2;
-            ph -= t0 - rv.t[i];
+            ph -= fd.t0 - rv.t[i];
             ph /= w;
-            const double al = (l0 * vx + l1 * vy) / v2 / w;
-            const double be = (l2 * vx + l3 * vy) / v2 / w;
+            const double al = (fd.l0 * vx + fd.l1 * vy) / v2 / w;
+            const double be = (fd.l2 * vx + fd.l3 * vy) / v2 / w;
             r.th = turns_to_fix32(ph);
             r.A = turns_to_fix32(al);
             r.B = turns_to_fix32(be);
@@ -87,10 +102,13 @@ __device__ __forceinline__ void kahan_add(float& sum, float& comp, float v) {
     sum = t;
 }
 
-// grid: (tiles, nsplit).  part_* : [nsplit][na*nb] doubles.
+// grid: (tiles, nsplit, fields).  rec: per_field records per field;
+// part_* : [fields][nsplit][na*nb] doubles.
 __global__ void __launch_bounds__(HUY_THREADS)
-k_huy_main(const HuyRec* __restrict__ rec, long long nrays, int na, int nb, int ngroups_b,
+k_huy_main(const HuyRec* __restrict__ rec, long long per_field, int na, int nb, int ngroups_b,
            long long rays_per_split, double* part_re, double* part_im) {
+    rec += (long long)blockIdx.z * per_field;
+    const long long nrays = per_field;
     __shared__ HuyRec tile[HUY_TILE];
     const long long g = (long long)blockIdx.x * HUY_THREADS + threadIdx.x;  // pixel group
     const long long ngroups = (long long)na * ngroups_b;
@@ -143,8 +161,9 @@ k_huy_main(const HuyRec* __restrict__ rec, long long nrays, int na, int nb, int 
     }
     if (!active) return;
     const long long npix = (long long)na * nb;
-    double* pr = part_re + (long long)blockIdx.y * npix;
-    double* pi = part_im + (long long)blockIdx.y * npix;
+    const long long part = (long long)blockIdx.z * gridDim.y + blockIdx.y;
+    double* pr = part_re + part * npix;
+    double* pi = part_im + part * npix;
 #pragma unroll
     for (int k = 0; k < HUY_PX; k++) {
         const int b = b0 + k;
@@ -155,69 +174,127 @@ k_huy_main(const HuyRec* __restrict__ rec, long long nrays, int na, int nb, int 
     }
 }
 
-__global__ void k_huy_reduce(const double* part_re, const double* part_im, int nsplit, long long npix,
+// out_*: [fields][npix]; the splits of a pixel are added in a fixed order.
+__global__ void k_huy_reduce(const double* part_re, const double* part_im, int nsplit, long long npix, int nfields,
                              double* out_re, double* out_im) {
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix;
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix * nfields;
          p += (long long)gridDim.x * blockDim.x) {
+        const long long f = p / npix, q = p - f * npix;
+        const double* pr = part_re + f * nsplit * npix + q;
+        const double* pi = part_im + f * nsplit * npix + q;
         double re = 0.0, im = 0.0;
         for (int s = 0; s < nsplit; s++) {
-            re += part_re[(long long)s * npix + p];
-            im += part_im[(long long)s * npix + p];
+            re += pr[(long long)s * npix];
+            im += pi[(long long)s * npix];
         }
         out_re[p] = re;
         out_im[p] = im;
     }
 }
 
+// Ray splits per field: enough blocks for ~4 per SM over all fields, each
+// split a multiple of the ray tile.
+static void huy_split(long long per_field, long long tiles, int nfields, long long max_split_mem, long long* nsplit,
+                      long long* per) {
+    const int sms = bt_sm_count();
+    long long ns = (4LL * sms + tiles * nfields - 1) / (tiles * nfields);
+    const long long max_split = (per_field + HUY_TILE - 1) / HUY_TILE;
+    if (ns > max_split) ns = max_split;
+    if (ns > max_split_mem) ns = max_split_mem;
+    if (ns > 65535) ns = 65535;
+    if (ns < 1) ns = 1;
+    long long pr = (per_field + ns - 1) / ns;
+    pr = ((pr + HUY_TILE - 1) / HUY_TILE) * HUY_TILE;
+    *per = pr;
+    *nsplit = (per_field + pr - 1) / pr;
+}
+
+// prep + main + reduce for nfields (<= HUY_MAX_FIELDS) fields whose rays
+// are consecutive blocks of per_field rays; scratch holds the records
+// (rec_bytes, 256-aligned) and then the partial sums.
+static cudaError_t huy_run(const RV& rv, long long per_field, const HuyFields& F, int nfields, int na, int nb,
+                           bool ignore_vig, long long nsplit, long long per, char* scratch, size_t rec_bytes,
+                           double* out_re, double* out_im, cudaStream_t stream) {
+    const long long npix = (long long)na * nb;
+    const int ngroups_b = (nb + HUY_PX - 1) / HUY_PX;
+    const long long tiles = ((long long)na * ngroups_b + HUY_THREADS - 1) / HUY_THREADS;
+    const int sms = bt_sm_count();
+    HuyRec* rec = reinterpret_cast<HuyRec*>(scratch);
+    double* pre = reinterpret_cast<double*>(scratch + rec_bytes);
+    double* pim = pre + (size_t)nfields * nsplit * npix;
+    long long pg = (rv.n + 255) / 256;
+    if (pg > (long long)sms * 16) pg = (long long)sms * 16;
+    k_huy_prep<<<(int)pg, 256, 0, stream>>>(rv, per_field, F, ignore_vig ? 1 : 0, rec);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)tiles, (unsigned)nsplit, (unsigned)nfields);
+    k_huy_main<<<grid, HUY_THREADS, 0, stream>>>(rec, per_field, na, nb, ngroups_b, per, pre, pim);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    long long rg = (npix * nfields + 255) / 256;
+    if (rg > (long long)sms * 8) rg = (long long)sms * 8;
+    k_huy_reduce<<<(int)rg, 256, 0, stream>>>(pre, pim, (int)nsplit, npix, nfields, out_re, out_im);
+    return cudaGetLastError();
+}
+
+static HuyField huy_field(double px, double py, double pz, const double lat[4], double t0) {
+    HuyField f;
+    f.px = px; f.py = py; f.pz = pz;
+    f.l0 = lat[0]; f.l1 = lat[1]; f.l2 = lat[2]; f.l3 = lat[3];
+    f.t0 = t0;
+    return f;
+}
+
 cudaError_t bt_launch_huygens(const RV& rv, double px, double py, double pz, const double lat[4], int na,
                               int nb, double t0, bool ignore_vig, double* out_re, double* out_im,
                               cudaStream_t stream) {
+    return bt_launch_huygens_fields(rv, rv.n, 1, &px, &py, &pz, lat, &t0, 1, na, nb, ignore_vig, out_re, out_im,
+                                    stream);
+}
+
+// Many fields: field f's rays are rows [f * per_field, (f + 1) * per_field)
+// of rv, its point (px[f*ps], py[f*ps], pz[f*ps]) (ps = point stride), its
+// lattice lat[4f .. 4f+3] and reference time t0[f]; outputs [nfields][na*nb].
+// One launch set (prep, main, reduce) per HUY_MAX_FIELDS fields.
+cudaError_t bt_launch_huygens_fields(const RV& rv, long long per_field, int nfields, const double* px,
+                                     const double* py, const double* pz, const double* lat, const double* t0,
+                                     int ps, int na, int nb, bool ignore_vig, double* out_re, double* out_im,
+                                     cudaStream_t stream) {
     const long long npix = (long long)na * nb;
-    if (npix <= 0) return cudaSuccess;
-    if (rv.n <= 0) {
-        cudaError_t e = cudaMemsetAsync(out_re, 0, npix * sizeof(double), stream);
+    if (npix <= 0 || nfields <= 0) return cudaSuccess;
+    if (per_field <= 0) {
+        cudaError_t e = cudaMemsetAsync(out_re, 0, npix * nfields * sizeof(double), stream);
         if (e != cudaSuccess) return e;
-        return cudaMemsetAsync(out_im, 0, npix * sizeof(double), stream);
+        return cudaMemsetAsync(out_im, 0, npix * nfields * sizeof(double), stream);
     }
     const int ngroups_b = (nb + HUY_PX - 1) / HUY_PX;
-    const long long ngroups = (long long)na * ngroups_b;
-    const long long tiles = (ngroups + HUY_THREADS - 1) / HUY_THREADS;
-    const int sms = bt_sm_count();
-    long long nsplit = (4LL * sms + tiles - 1) / tiles;
-    long long max_split = (rv.n + HUY_TILE - 1) / HUY_TILE;
-    if (nsplit > max_split) nsplit = max_split;
-    if (nsplit > 65535) nsplit = 65535;
-    if (nsplit < 1) nsplit = 1;
-    long long per = (rv.n + nsplit - 1) / nsplit;
-    per = ((per + HUY_TILE - 1) / HUY_TILE) * HUY_TILE;
-    nsplit = (rv.n + per - 1) / per;
-
-    // scratch: ray records and per-split partial sums
-    const size_t rec_bytes = (size_t)rv.n * sizeof(HuyRec);
-    const size_t part_bytes = (size_t)nsplit * npix * sizeof(double);
+    const long long tiles = ((long long)na * ngroups_b + HUY_THREADS - 1) / HUY_THREADS;
+    const int chunk = nfields < HUY_MAX_FIELDS ? nfields : HUY_MAX_FIELDS;
+    // each field is split as a single-field call splits it, so that every
+    // field's amplitudes are bit-identical to that call's
+    long long nsplit, per;
+    huy_split(per_field, tiles, 1, 1LL << 40, &nsplit, &per);
+    // scratch: ray records and per-split partial sums of one chunk of fields
+    const size_t rec_bytes = (((size_t)per_field * chunk * sizeof(HuyRec)) + 255) & ~(size_t)255;
+    const size_t part_bytes = (size_t)chunk * nsplit * npix * sizeof(double);
     char* scratch = nullptr;
     bt_keep_pool();
     cudaError_t e = cudaMallocAsync((void**)&scratch, rec_bytes + 2 * part_bytes, stream);
     if (e != cudaSuccess) return e;
-    HuyRec* rec = reinterpret_cast<HuyRec*>(scratch);
-    double* pre = reinterpret_cast<double*>(scratch + rec_bytes);
-    double* pim = reinterpret_cast<double*>(scratch + rec_bytes + part_bytes);
-
-    long long pg = (rv.n + 255) / 256;
-    if (pg > (long long)sms * 16) pg = (long long)sms * 16;
-    k_huy_prep<<<(int)pg, 256, 0, stream>>>(rv, px, py, pz, lat[0], lat[1], lat[2], lat[3], t0,
-                                            ignore_vig ? 1 : 0, rec);
-    e = cudaGetLastError();
-    if (e == cudaSuccess) {
-        dim3 grid((unsigned)tiles, (unsigned)nsplit);
-        k_huy_main<<<grid, HUY_THREADS, 0, stream>>>(rec, rv.n, na, nb, ngroups_b, per, pre, pim);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) {
-        long long rg = (npix + 255) / 256;
-        if (rg > (long long)sms * 8) rg = (long long)sms * 8;
-        k_huy_reduce<<<(int)rg, 256, 0, stream>>>(pre, pim, (int)nsplit, npix, out_re, out_im);
-        e = cudaGetLastError();
+    HuyFields F;
+    for (int f0 = 0; f0 < nfields && e == cudaSuccess; f0 += HUY_MAX_FIELDS) {
+        const int nf = (nfields - f0) < HUY_MAX_FIELDS ? (nfields - f0) : HUY_MAX_FIELDS;
+        for (int k = 0; k < nf; k++) {
+            const int f = f0 + k;
+            F.f[k] = huy_field(px[(size_t)f * ps], py[(size_t)f * ps], pz[(size_t)f * ps], lat + 4 * (size_t)f, t0[f]);
+        }
+        RV sub = rv;
+        sub.n = per_field * nf;
+        const long long off = per_field * f0;
+        sub.x += off; sub.y += off; sub.z += off; sub.vx += off; sub.vy += off; sub.vz += off;
+        sub.t += off; sub.w += off; sub.f += off; sub.vig += off; sub.fail += off;
+        e = huy_run(sub, per_field, F, nf, na, nb, ignore_vig, nsplit, per, scratch, rec_bytes,
+                    out_re + (size_t)f0 * npix, out_im + (size_t)f0 * npix, stream);
     }
     cudaError_t e2 = cudaFreeAsync(scratch, stream);
     return e != cudaSuccess ? e : e2;
@@ -238,7 +315,10 @@ cudaError_t bt_launch_huygens(const RV& rv, double px, double py, double pz, con
 //
 // Set-up: the first call on a device (with that device current) looks up the
 // array's device address with cudaGetSymbolAddress and caches it per device;
-// make that first call before any stream capture.  All calls share the one
+// make that first call before any stream capture.  The cached address is not
+// looked up again: after cudaDeviceReset (or anything else that destroys the
+// device's primary context) it is stale, so a process that resets a device
+// must not call this entry point on that device again.  All calls share the one
 // array and it keeps the last call's contents: nothing in it has to start at
 // zero (every record and partial sum is written before it is read within a
 // call), but calls whose kernels overlap on the GPU -- on different streams
@@ -289,41 +369,16 @@ cudaError_t bt_launch_huygens_noalloc(const RV& rv, double px, double py, double
     *needed = rec_bytes + split_bytes;
     if (rec_bytes + split_bytes > HUY_NOALLOC_BYTES) return cudaErrorInvalidValue;
     const long long max_split_mem = (long long)((HUY_NOALLOC_BYTES - rec_bytes) / split_bytes);
-
     const int ngroups_b = (nb + HUY_PX - 1) / HUY_PX;
-    const long long ngroups = (long long)na * ngroups_b;
-    const long long tiles = (ngroups + HUY_THREADS - 1) / HUY_THREADS;
-    const int sms = bt_sm_count();
-    long long nsplit = (4LL * sms + tiles - 1) / tiles;
-    long long max_split = (rv.n + HUY_TILE - 1) / HUY_TILE;
-    if (nsplit > max_split) nsplit = max_split;
-    if (nsplit > max_split_mem) nsplit = max_split_mem;
-    if (nsplit > 65535) nsplit = 65535;
-    if (nsplit < 1) nsplit = 1;
-    long long per = (rv.n + nsplit - 1) / nsplit;
-    per = ((per + HUY_TILE - 1) / HUY_TILE) * HUY_TILE;
-    nsplit = (rv.n + per - 1) / per;
+    const long long tiles = ((long long)na * ngroups_b + HUY_THREADS - 1) / HUY_THREADS;
+    long long nsplit, per;
+    huy_split(rv.n, tiles, 1, max_split_mem, &nsplit, &per);
 
     void* base = nullptr;
     cudaError_t e = huy_noalloc_scratch(&base);
     if (e != cudaSuccess) return e;
-    char* scratch = static_cast<char*>(base);
-    HuyRec* rec = reinterpret_cast<HuyRec*>(scratch);
-    double* pre = reinterpret_cast<double*>(scratch + rec_bytes);
-    double* pim = pre + (size_t)nsplit * npix;
-
-    long long pg = (rv.n + 255) / 256;
-    if (pg > (long long)sms * 16) pg = (long long)sms * 16;
-    k_huy_prep<<<(int)pg, 256, 0, stream>>>(rv, px, py, pz, lat[0], lat[1], lat[2], lat[3], t0,
-                                            ignore_vig ? 1 : 0, rec);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    dim3 grid((unsigned)tiles, (unsigned)nsplit);
-    k_huy_main<<<grid, HUY_THREADS, 0, stream>>>(rec, rv.n, na, nb, ngroups_b, per, pre, pim);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    long long rg = (npix + 255) / 256;
-    if (rg > (long long)sms * 8) rg = (long long)sms * 8;
-    k_huy_reduce<<<(int)rg, 256, 0, stream>>>(pre, pim, (int)nsplit, npix, out_re, out_im);
-    return cudaGetLastError();
+    HuyFields F;
+    F.f[0] = huy_field(px, py, pz, lat, t0);
+    return huy_run(rv, rv.n, F, 1, na, nb, ignore_vig, nsplit, per, static_cast<char*>(base), rec_bytes, out_re,
+                   out_im, stream);
 }

@@ -92,28 +92,6 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, const void*
     asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }
 
-// TMA load of one box into the same shared-memory offset of every CTA in
-// `mask` (cluster multicast); each destination's barrier at `bar`'s offset
-// receives the bytes it gets.
-__device__ __forceinline__ void tma_load_2d_mc(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar,
-                                               uint16_t mask) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
-        " [%0], [%1, {%2, %3}], [%4], %5;"
-        ::"r"(bt_smem_addr(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(bt_smem_addr(bar)), "h"(mask)
-        : "memory");
-}
-
-__device__ __forceinline__ uint32_t cluster_rank() {
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-    return r;
-}
-
-__device__ __forceinline__ void cluster_sync() {
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
     asm volatile(
         "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
@@ -148,13 +126,6 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                  ::"r"(bt_smem_addr(bar)) : "memory");
-}
-
-// Arrive (when this CTA's MMAs so far complete) on the barrier at `bar`'s
-// offset in every CTA of `mask`.
-__device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t mask) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
-                 ::"r"(bt_smem_addr(bar)), "h"(mask) : "memory");
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -210,15 +181,6 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 // meanwhile.  Barriers: full/empty per ring stage, acc_full/acc_empty per
 // accumulator buffer; the first use of each "empty" barrier waits on the
 // phase before the barrier's first, which counts as completed.
-//
-// CL = 2: clusters of two CTAs take two adjacent 128-row tiles with the same
-// columns.  Each CTA loads its own A tile and half of the shared B tile,
-// multicast into both CTAs, so B is read from L2 once per pair.  A ring
-// stage is refilled only after both CTAs' MMAs released it: every MMA
-// commit arrives on the "empty" barrier of both CTAs (count 2).  With an
-// odd number of row tiles the last pair's second tile lies below M: its A
-// box reads the zero fill and its epilogue stores nothing.
-template <int CL>
 __global__ void __launch_bounds__(MLP_THREADS, 1)
 k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
            const __grid_constant__ CUtensorMap tmH, MlpGemmArgs g) {
@@ -242,17 +204,13 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     const int tiles_m = g.M / MLP_BM, tiles_n = g.N / BN;
     const int nk = g.kchunk / MLP_BK;
     volatile int* abort = &s_abort;
-    // work items: single tiles (CL 1) or pairs of row tiles (CL 2)
-    const int rank = (CL == 2) ? (int)cluster_rank() : 0;
-    const int rows_w = (tiles_m + CL - 1) / CL;
-    const int nwork = rows_w * tiles_n * (g.K / g.kchunk);
-    const int w0 = blockIdx.x / CL, wstep = gridDim.x / CL;
-    const uint16_t pair_mask = 0x3;
+    const int nwork = tiles_m * tiles_n * (g.K / g.kchunk);
+    const int w0 = blockIdx.x, wstep = gridDim.x;
 
     if (tid == 0) {
         for (int s = 0; s < NS; s++) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], CL);
+            mbar_init(&empty[s], 1);
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(&acc_full[b], 1);
@@ -269,7 +227,6 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     }
     tc_fence_before();
     __syncthreads();
-    if (CL == 2) cluster_sync();  // the peer's barriers are initialised before any multicast
     tc_fence_after();
     const uint32_t tmem = s_tmem;
 
@@ -277,19 +234,15 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
         // producer
         int gk = 0;
         for (int t = w0; t < nwork && !*abort; t += wstep) {
-            const int kz = t / (rows_w * tiles_n), r = t - kz * rows_w * tiles_n;
-            const int m0 = ((r / tiles_n) * CL + rank) * MLP_BM, n0 = (r % tiles_n) * BN;
+            const int kz = t / (tiles_m * tiles_n), r = t - kz * tiles_m * tiles_n;
+            const int m0 = (r / tiles_n) * MLP_BM, n0 = (r % tiles_n) * BN;
             const int kbeg = kz * g.kchunk;
             for (int kb = 0; kb < nk; kb++, gk++) {
                 const int s = gk % NS;
                 if (!mbar_wait(&empty[s], ((gk / NS) & 1) ^ 1, abort)) break;
                 mbar_expect_tx(&full[s], a_bytes + b_bytes);
                 tma_load_2d(sA + s * a_bytes, &tmA, kbeg + kb * MLP_BK, m0, &full[s]);
-                if (CL == 2)
-                    tma_load_2d_mc(sB + s * b_bytes + rank * (b_bytes / 2), &tmB, kbeg + kb * MLP_BK,
-                                   n0 + rank * (BN / 2), &full[s], pair_mask);
-                else
-                    tma_load_2d(sB + s * b_bytes, &tmB, kbeg + kb * MLP_BK, n0, &full[s]);
+                tma_load_2d(sB + s * b_bytes, &tmB, kbeg + kb * MLP_BK, n0, &full[s]);
             }
         }
         // copies still in flight complete before the CTA may exit
@@ -318,8 +271,7 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
 #pragma unroll
                 for (int k = 0; k < MLP_BK / 16; k++)
                     mma_bf16(d, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), idesc, (kb > 0 || k > 0) ? 1u : 0u);
-                if (CL == 2) mma_commit_mc(&empty[s], pair_mask);
-                else mma_commit(&empty[s]);
+                mma_commit(&empty[s]);
             }
             if (!ok) break;
             mma_commit(&acc_full[b]);
@@ -335,14 +287,12 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
             const int b = it & 1;
             if (!mbar_wait(&acc_full[b], (it >> 1) & 1, abort)) break;
             tc_fence_after();
-            const int kz = t / (rows_w * tiles_n), r = t - kz * rows_w * tiles_n;
-            const int m0 = ((r / tiles_n) * CL + rank) * MLP_BM, n0 = (r % tiles_n) * BN;
+            const int kz = t / (tiles_m * tiles_n), r = t - kz * tiles_m * tiles_n;
+            const int m0 = (r / tiles_n) * MLP_BM, n0 = (r % tiles_n) * BN;
             const int m = m0 + q * 32 + lane;
             const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
             const int c0 = half * (BN / 2);
-            // a tile below M (second of an odd last pair) has nothing to store
-            const int c_end = (m0 < g.M) ? c0 + BN / 2 : c0;
-            for (int c = c0; c < c_end; c += 32) {
+            for (int c = c0; c < c0 + BN / 2; c += 32) {
                 const int nb = n0 + c;
                 // this chunk's bias (or pre-activations) are requested before
                 // the TMEM load so that both latencies overlap
@@ -450,9 +400,6 @@ k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(2 * BN)) : "memory");
     }
-    // the peer's multicast copies and commit arrivals target this CTA's
-    // shared memory until it is done too
-    if (CL == 2) cluster_sync();
 }
 
 // ---------------------------------------------------------------------------
@@ -517,20 +464,10 @@ cudaError_t bt_launch_mlp_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, c
         return cudaErrorInvalidValue;
     if (splitk > 1 && a.mode != MLP_EPI_F32) return cudaErrorInvalidValue;  // only partials are split
     if (((uintptr_t)A & 15) || ((uintptr_t)B & 15)) return cudaErrorInvalidValue;
-    // Single CTAs by default.  CTA pairs with the B tile multicast
-    // (BATOID_GB300_GEMM_CLUSTER=1) are correct but were not faster on the
-    // surrogate's shapes (65,664 x 512 x 512: 44.9 vs 43.3 us): each SM still
-    // receives the whole B tile, and the tile rate is not bound by L2 reads.
-    static int cl_env = -1;
-    if (cl_env == -1) {
-        const char* e = getenv("BATOID_GB300_GEMM_CLUSTER");
-        cl_env = (e && atoi(e) != 0) ? 1 : 0;
-    }
     const long long ntiles = (long long)(a.M / MLP_BM) * (a.N / a.bn) * splitk;
     const int sms = bt_sm_count();
-    const bool pairs = sms >= 2 && cl_env == 1;
     CUtensorMap ta, tb, th;
-    if (!make_map(&ta, A, a.M, a.K, MLP_BM) || !make_map(&tb, B, a.N, a.K, pairs ? a.bn / 2 : a.bn))
+    if (!make_map(&ta, A, a.M, a.K, MLP_BM) || !make_map(&tb, B, a.N, a.K, a.bn))
         return cudaErrorInvalidValue;
     memset(&th, 0, sizeof(th));
     if (a.mode == MLP_EPI_GELU || a.mode == MLP_EPI_DGELU) {
@@ -554,43 +491,13 @@ cudaError_t bt_launch_mlp_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, c
     if (!attr_set) {
         const int lim = (int)(bt_mlp_gemm_smem(256) > bt_mlp_gemm_smem(128) ? bt_mlp_gemm_smem(256)
                                                                               : bt_mlp_gemm_smem(128));
-        cudaError_t e = cudaFuncSetAttribute(k_mlp_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mlp_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaError_t e = cudaFuncSetAttribute(k_mlp_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
         if (e != cudaSuccess) return e;
         attr_set = 1;
     }
-    if (!pairs) {
-        const int grid = (int)(ntiles < sms ? ntiles : sms);
-        k_mlp_gemm<1><<<grid, MLP_THREADS, smem, stream>>>(ta, tb, th, g);
-        return cudaGetLastError();
-    }
-    // clusters of 2 CTAs, one CTA per SM.  The work is split statically
-    // over the clusters, so launch no more than can be resident at once.
-    const long long npairs = (long long)((a.M / MLP_BM + 1) / 2) * (a.N / a.bn) * splitk;
-    cudaLaunchConfig_t cfg = {};
-    cfg.blockDim = dim3(MLP_THREADS, 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 2;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    static int resident = 0;
-    if (resident == 0) {
-        cfg.gridDim = dim3((unsigned)(sms & ~1), 1, 1);
-        int n = 0;
-        if (cudaOccupancyMaxActiveClusters(&n, (const void*)k_mlp_gemm<2>, &cfg) != cudaSuccess || n < 1) {
-            cudaGetLastError();
-            n = sms / 2;
-        }
-        resident = n;
-    }
-    const long long nclusters = npairs < resident ? npairs : resident;
-    cfg.gridDim = dim3((unsigned)(2 * nclusters), 1, 1);
-    return cudaLaunchKernelEx(&cfg, k_mlp_gemm<2>, ta, tb, th, g);
+    const int grid = (int)(ntiles < sms ? ntiles : sms);
+    k_mlp_gemm<<<grid, MLP_THREADS, smem, stream>>>(ta, tb, th, g);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

@@ -356,3 +356,39 @@ cudaError_t bt_launch_dfma_probe(int iters, double* sink, float* ms, double* flo
     if (e == cudaSuccess) e = cudaGetLastError();
     return e;
 }
+
+// FP32 counterpart: 8 independent FFMA chains per thread, 8 blocks of 256
+// threads per SM (64 warps, 16 per scheduler: enough to cover the FMA
+// latency on every scheduler).
+__global__ void k_ffma_probe(int iters, float b, float c, double* sink) {
+    float a[PROBE_CHAINS];
+#pragma unroll
+    for (int k = 0; k < PROBE_CHAINS; k++) a[k] = threadIdx.x * 1e-3f + k;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < PROBE_CHAINS; k++) a[k] = fmaf(a[k], b, c);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < PROBE_CHAINS; k++) s += a[k];
+    if (s == 12345.678f) sink[0] = s;  // keeps the chains live
+}
+
+cudaError_t bt_launch_ffma_probe(int iters, double* sink, float* ms, double* flops, cudaStream_t stream) {
+    const int blocks = bt_sm_count() * 8, threads = 256;
+    cudaEvent_t e0, e1;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e != cudaSuccess) return e;
+    cudaEventCreate(&e1);
+    k_ffma_probe<<<blocks, threads, 0, stream>>>(iters / 8, 0.9999f, 1e-4f, sink);  // warm-up
+    cudaEventRecord(e0, stream);
+    k_ffma_probe<<<blocks, threads, 0, stream>>>(iters, 0.9999f, 1e-4f, sink);
+    cudaEventRecord(e1, stream);
+    e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+    *flops = 2.0 * PROBE_CHAINS * (double)iters * blocks * threads;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return e;
+}

@@ -12,9 +12,12 @@ Two optics and their ray bundles:
 * ``tma_corrector``: 12 surfaces -- three aspheric mirrors (Sum(Asphere,
   Zernike) primary), three fused-silica lenses and a filter (8 faces:
   Sphere / Plane / Asphere / Quadric) and a flat detector.  Spacings, radii
-  and clear apertures follow the LSST design (batoid/data/LSST/LSST_r.yaml);
-  the mirrors carry seeded even asphere terms r^8..r^20 with |a| < 1e-18 on
-  top of the design's r^4/r^6/r^8 terms, and the primary a seeded Zernike
+  and clear apertures follow the LSST design (batoid/data/LSST/LSST_r.yaml),
+  with the mirror conics kept in [-1.3, 0.1]: M3 has conic 0.1 instead of
+  LSST's 0.155, and its r^4..r^20 terms absorb the difference (the Taylor
+  series of the two conics' sags), so the mirror's shape is LSST's to
+  ~1e-13 m.  Every mirror carries seeded even asphere terms r^6..r^20 with
+  |a| < 1e-18 added to those design terms, and the primary a seeded Zernike
   perturbation (Noll j = 4..28, N(0, 50 nm)).  Glass is 3-term Sellmeier
   fused silica.  Rays: pupil annulus 2.558-4.18 m uniform in area, field
   uniform in a 1.75 deg radius disk, 6 wavelengths equally spaced
@@ -59,8 +62,31 @@ def paraboloid_rays(n, seed=57721):
             np.zeros(n, bool))
 
 
-def _seeded_terms(rng, n):
-    return list(rng.uniform(-1e-18, 1e-18, n))
+def _conic_series(R, k, nmax=10):
+    """Taylor coefficients of the conic sag r^2 / (R (1 + sqrt(1 - (1+k) r^2/R^2)))
+    in r^2, r^4, ..., r^(2 nmax): sag = sum_n b_n (1+k)^(n-1) r^(2n) / R^(2n-1)
+    with b_n the series coefficients of (1 - sqrt(1 - u)) / u * u."""
+    b = np.zeros(nmax + 1)
+    # 1 - sqrt(1-u) = sum_{n>=1} C(2n-2, n-1) / (n 2^(2n-1)) u^n
+    from math import comb
+    for n in range(1, nmax + 1):
+        b[n] = comb(2 * n - 2, n - 1) / (n * 2 ** (2 * n - 1))
+    return np.array([b[n] * (1 + k) ** (n - 1) / R ** (2 * n - 1) for n in range(1, nmax + 1)])
+
+
+def _reconic(R, k_design, k_used):
+    """Asphere terms r^4..r^20 that make conic k_used carry the sag of conic
+    k_design (the difference of the two series; the r^2 terms agree)."""
+    return list((_conic_series(R, k_design) - _conic_series(R, k_used))[1:])
+
+
+def _mirror_terms(rng, design):
+    """Asphere coefficients r^4..r^20: the design's leading terms plus seeded
+    terms |a| < 1e-18 on r^6..r^20."""
+    c = np.zeros(9)
+    c[:len(design)] = design
+    c[1:] += rng.uniform(-1e-18, 1e-18, 8)
+    return list(c)
 
 
 def tma_zernike_coefs(seed=20231):
@@ -78,7 +104,7 @@ def tma_optic(bt, zernike_factory=None, seed=20231):
     silica = bt.SellmeierMedium(*SILICA)
     vac = bt.ConstMedium(1.0)
     zfac = zernike_factory or (lambda c, ro, ri: bt.Zernike(c, R_outer=ro, R_inner=ri))
-    m1_surf = bt.Sum(bt.Asphere(19.835, -1.215, [0.0, -1.381e-9] + _seeded_terms(rng, 7)),
+    m1_surf = bt.Sum(bt.Asphere(19.835, -1.215, _mirror_terms(rng, [0.0, -1.381e-9])),
                      zfac(tma_zernike_coefs(seed), 4.18, 2.558))
     z0 = np.zeros(3)
 
@@ -88,10 +114,11 @@ def tma_optic(bt, zernike_factory=None, seed=20231):
     items = [
         bt.Mirror(m1_surf, obscuration=bt.ObscNegation(bt.ObscAnnulus(2.558, 4.18)), name="M1", coordSys=cs(0.0),
                   inMedium=vac, outMedium=vac),
-        bt.Mirror(bt.Asphere(6.788, -0.222, [0.0, 1.274e-5, 9.68e-7] + _seeded_terms(rng, 6)),
+        bt.Mirror(bt.Asphere(6.788, -0.222, _mirror_terms(rng, [0.0, 1.274e-5, 9.68e-7])),
                   obscuration=bt.ObscNegation(bt.ObscAnnulus(0.9, 1.71)), name="M2", coordSys=cs(6.1562006),
                   inMedium=vac, outMedium=vac),
-        bt.Mirror(bt.Asphere(8.3445, 0.155, [0.0, 4.5e-7, 8.15e-9] + _seeded_terms(rng, 6)),
+        bt.Mirror(bt.Asphere(8.3445, 0.1, _mirror_terms(
+            rng, np.add(_reconic(8.3445, 0.155, 0.1), [0.0, 4.5e-7, 8.15e-9, 0, 0, 0, 0, 0, 0]))),
                   obscuration=bt.ObscNegation(bt.ObscAnnulus(0.55, 2.508)), name="M3", coordSys=cs(-0.2338),
                   inMedium=vac, outMedium=vac),
     ]

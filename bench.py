@@ -43,6 +43,7 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-huygens", action="store_true")
+    p.add_argument("--no-paraboloid", action="store_true")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--batch-states", type=int, default=4096)
     p.add_argument("--no-surrogate", action="store_true")
@@ -116,13 +117,23 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def time_cpu(workload, nrays, threads=None):
+def _oracle():
+    """The oracle (C restatement of the reference trace) and its own optic
+    builder: the CPU legs never load the product package or its library."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as ora
-    import batoid_gb300 as bt
-    from batoid_gb300 import workloads as W
-    build_optic, make_rays, nsurf = W.WORKLOADS[workload]
-    opt = build_optic(bt)
+    import optics as OO
+    return ora, OO
+
+
+def cpu_workload(workload):
+    ora, OO = _oracle()
+    build_optic, make_rays, nsurf = OO.workloads().WORKLOADS[workload]
+    return ora, build_optic(OO), make_rays, nsurf
+
+
+def time_cpu(workload, nrays, threads=None):
+    ora, opt, make_rays, nsurf = cpu_workload(workload)
     threads = threads or ora.threads()
     rays = ora.Rays(*make_rays(nrays, seed=1000))
     t1 = time.perf_counter()
@@ -151,140 +162,274 @@ def cpu_baseline(workload, target_s=12.0):
 
 
 def run_reference(args):
+    """The reference's trace algorithm on the host cores (the oracle's C
+    restatement, OpenMP over all threads) on the same configuration as the
+    GPU arm: the full ray batch of each rank-0 step, same seeds, traced in
+    place from a fresh copy of the inputs (copy outside the timed region)."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
-    from batoid_gb300 import workloads as W
-    _, _, nsurf = W.WORKLOADS[args.workload]
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as ora
-    # bounded per-step sample sized to ~1-2 s of CPU work
-    n = 1 << 16
-    rate, dt, threads = time_cpu(args.workload, n)
-    while dt < 0.8 and n < (1 << 23):
-        n *= 2
-        rate, dt, threads = time_cpu(args.workload, n)
-    for _ in range(args.warmup):
-        time_cpu(args.workload, n, threads)
+    ora, opt, make_rays, nsurf = cpu_workload(args.workload)
+    threads = ora.threads()
+    n = args.nrays
+    pristine = ora.Rays(*make_rays(n, seed=4242))
+    rays = pristine.copy()
     total = 0.0
-    for _ in range(args.steps):
-        _, d, _ = time_cpu(args.workload, n, threads)
-        total += d
+    for it in range(args.warmup + args.steps):
+        np.copyto(rays.d, pristine.d)
+        np.copyto(rays.b, pristine.b)
+        rays.origin, rays.rot = pristine.origin.copy(), pristine.rot.copy()
+        t1 = time.perf_counter()
+        ora.trace(opt, rays, nthreads=threads)
+        dt = time.perf_counter() - t1
+        if it >= args.warmup:
+            total += dt
     value = n * nsurf * args.steps / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{args.workload} (sample of {n} rays per step; full batch {args.nrays})",
-                   "surfaces": nsurf, "l2": "inputs > L2 (host)"},
+        "config": {"workload": f"{args.workload}: {nsurf}-surface trace of {n} rays per step (seed 4242, as "
+                               "the GPU arm's rank 0), 6 wavelengths 350-1000 nm, Sellmeier silica",
+                   "rays_per_step": n, "surfaces": nsurf, "l2": "host arrays, 1.2 GB per step"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{n} rays per step, oracle C restatement of the reference trace"},
+                         "sample": f"the full {n}-ray batch per step, oracle C restatement of the reference "
+                                   f"trace, OpenMP {threads} threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def load_traffic(workload):
-    """Per-ray DRAM traffic of the trace kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "trace_kernel_traffic.json")
+def load_counters(key):
+    """Per-unit counters of one kernel on one workload from the committed ncu
+    summaries (profiles/kernel_counters.json): DRAM bytes and executed FP64
+    instructions per ray, measured on a case larger than L2."""
+    path = os.path.join(ROOT, "profiles", "kernel_counters.json")
     try:
         with open(path) as f:
-            d = json.load(f)
-        return d[workload]["dram_bytes_per_ray"]
-    except (OSError, KeyError, ValueError):
+            return json.load(f).get(key)
+    except (OSError, ValueError):
         return None
+
+
+def executed_fp64_flops(c):
+    """Executed FP64 flops per unit from an ncu census: DADD + DMUL + 2 DFMA."""
+    if not c or "fp64_dfma_per_ray" not in c:
+        return None
+    return c["fp64_dadd_per_ray"] + c["fp64_dmul_per_ray"] + 2 * c["fp64_dfma_per_ray"]
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def host_trace_e2e(L, _lib, prog, arrs, n, niter, steps, sp, chunk=1 << 21):
+    """The trace through the C-ABI host-buffer entry point (bt_optic_trace_host):
+    pinned host arrays in, results back in them; host clock around each call.
+    Returns (ms per call, h2d bytes, d2h bytes)."""
+    import torch
+    host = [torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).pin_memory() for x in arrs[:9]]
+    hflags = [torch.from_numpy(np.ascontiguousarray(x, dtype=np.uint8)).pin_memory() for x in arrs[9:]]
+    pristine = [h.clone() for h in host] + [f.clone() for f in hflags]
+    hrv = _lib.BtRayVector(*[h.data_ptr() for h in host], *[f.data_ptr() for f in hflags], n)
+    total = 0.0
+    for it in range(1 + steps):
+        for dst, src in zip(host + hflags, pristine):
+            dst.copy_(src)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        _lib.check(L.bt_optic_trace_host(prog._optic.ptr, ctypes.byref(hrv), niter, chunk, sp))
+        dt = (time.perf_counter() - t1) * 1e3
+        if it > 0:
+            total += dt
+    return total / max(steps, 1), n * (9 * 8 + 2), n * (8 * 8 + 2)
+
+
+def bench_paraboloid(bt, fp64_peak, n=1_000_000, reps=20, cpu=True):
+    """The f/4 paraboloid mirror onto a flat detector, 1e6 rays (2 surfaces):
+    device-timed out-of-place trace with L2 flushed between steps (the
+    148 MB of rays are about L2's size), e2e through the host-buffer entry
+    point, and the oracle on the host cores on the same 1e6 rays."""
+    import torch
+    from batoid_gb300 import _lib, _device as D, workloads as W, workcount as WC
+    opt = W.paraboloid_optic(bt)
+    arrs = W.paraboloid_rays(n, seed=57721)
+    rv_in = bt.RayVector(*arrs)
+    rv_out = bt.RayVector._empty(n)
+    prog = opt._program(rv_in.coordSys)
+    L = _lib.lib()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    niter = bt.global_vars._batoid_niter
+    a, b = rv_in._rv, rv_out._rv
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=D.device())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    times = []
+    for it in range(3 + reps):
+        flush.fill_(it & 0xff)
+        e0.record(stream)
+        _lib.check(L.bt_optic_trace_into(prog._optic.ptr, a, b, niter, sp))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if it >= 3:
+            times.append(e0.elapsed_time(e1))
+    ms = statistics.median(times)
+    nsurf = 2
+    bpr = WC.READ_BYTES_PER_RAY + WC.WRITE_BYTES_PER_RAY
+    gbs = bpr * n / (ms * 1e-3) / 1e9
+    hbm_peak = measured_peaks().get("hbm_gbs", 6800.0)
+    c = load_counters("k_trace/paraboloid")
+    out = {"workload": f"paraboloid: f/4 mirror (R 8 m, annulus 0.2-0.5 m) + flat detector, {n} rays, "
+                       "field +-0.5 deg, 500 nm, vacuum",
+           "value": n * nsurf / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "steps": reps,
+           "l2": "flushed between steps (256 MB write)",
+           "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                        "bytes_per_ray": bpr, "peak_source": "MEASURED_PEAKS.json hbm_gbs",
+                        "traffic": (c["dram_bytes_per_ray"] * n if c else None)}}
+    fpr = executed_fp64_flops(c)
+    if fpr and fp64_peak:
+        ach = fpr * n / (ms * 1e-3) / 1e12
+        out["fp64"] = {"executed_flops_per_ray": fpr, "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
+                       "frac": ach / fp64_peak}
+    e2e_ms, h2d, d2h = host_trace_e2e(L, _lib, prog, arrs, n, niter, 5, sp, chunk=1 << 19)
+    out["e2e"] = {"value": n * nsurf / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                  "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+                  "path": "bt_optic_trace_host, pinned host arrays, 2-stream chunks"}
+    if cpu:
+        ora, copt, make_rays, _ = cpu_workload("paraboloid")
+        pristine = ora.Rays(*make_rays(n, seed=57721))
+        rates = []
+        spent = 0.0
+        while spent < 5.0 or len(rates) < 3:
+            rays = pristine.copy()
+            t1 = time.perf_counter()
+            ora.trace(copt, rays)
+            d = time.perf_counter() - t1
+            spent += d
+            rates.append(n * nsurf / d)
+        out["cpu_baseline"] = {"value": statistics.median(rates), "unit": UNIT, "cores": ora.threads(),
+                               "kind": "port", "sample": f"the full {n}-ray batch x {len(rates)} repeats, "
+                                                          "oracle C restatement of the reference trace"}
+        out["speedup_vs_cpu"] = out["value"] / out["cpu_baseline"]["value"]
+        out["e2e_speedup_vs_cpu"] = out["e2e"]["value"] / out["cpu_baseline"]["value"]
+    return out
 
 
 HUYGENS_FIELDS = [(fx, fy) for fy in (-1.2, 0.0, 1.2) for fx in (-1.2, 0.0, 1.2)]  # degrees
 
 
-def bench_huygens(bt, opt, nx=256, npix=128, pitch=2e-6, wavelength=620e-9, check_pixels=48, cpu=True):
+def bench_huygens(bt, opt, nx=256, npix=128, pitch=2e-6, wavelength=620e-9, check_pixels=48, cpu=True,
+                  fp32_peak=None, reps=5):
     """Huygens PSF of the 12-surface system: 9 field points (3x3 grid over
-    +-1.2 deg), 256x256 pupil grid, 128x128 pixels at 2 um around the chief
-    ray.  Device-timed: trace + phasor sums for all fields.  Error: PSF on
-    sampled pixels vs the FP64 per-pixel sum (device sumAmplitude kernel,
-    the reference's algorithm), relative to the PSF peak."""
+    +-1.2 deg), 256x256 pupil grid each, 128x128 pixels at 2 um around each
+    field's chief ray.  Device-timed: one trace launch for all fields, and
+    one launch set of the phasor sums for all fields
+    (bt_huygens_amplitudes_fields).  Error: PSF on sampled pixels vs the
+    FP64 per-pixel sum (device sumAmplitude kernel, the reference's
+    algorithm), relative to each field's PSF peak."""
     import torch
-    from batoid_gb300 import analysis as A
-    lat = np.array([[pitch, 0.0], [0.0, pitch]])
-    rng = np.random.default_rng(5)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    sums = {"ms_trace_and_psf": 0.0, "ms_psf_kernels": 0.0}
-    max_err = 0.0
-    pairs = 0
-    kept = []
-    for fx, fy in HUYGENS_FIELDS:
-        rays = bt.RayVector.asGrid(optic=opt, wavelength=wavelength, theta_x=np.deg2rad(fx),
-                                   theta_y=np.deg2rad(fy), nx=nx)
-        torch.cuda.synchronize()
-        e0.record()
-        opt.trace(rays)
-        e1.record()
-        torch.cuda.synchronize()
-        sums["ms_trace_and_psf"] += e0.elapsed_time(e1)
-        point = rays.r[(nx // 2) * nx + nx // 2]
-        t0 = float(rays.t[0])
-        e0.record()
-        re, im = A.huygens_amplitudes(rays, (point[0], point[1], 0.0), lat, npix, npix, t0)
-        e1.record()
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)   # includes the two device-to-host copies of the result
-        sums["ms_psf_kernels"] += ms
-        sums["ms_trace_and_psf"] += ms
-        valid = int((~rays.failed & ~rays.vignetted).sum())
-        pairs += valid * npix * npix
-        psf = re * re + im * im
-        peak = psf.max()
-        idx = rng.integers(0, npix, (check_pixels, 2))
-        for a, b in idx:
-            P = (point[0] + (b - npix // 2) * pitch, point[1] + (a - npix // 2) * pitch, 0.0)
-            ref = rays.sumAmplitude(P, t0)
-            err = abs(abs(ref) ** 2 - psf[a, b]) / peak
-            max_err = max(max_err, err)
-        kept.append((rays, point, t0, psf))
-    # all fields in one call (analysis.huygensPSFs: one trace launch, one
-    # copy of the amplitudes to the host), same lattice and pixels
+    from batoid_gb300 import _lib, _device as D, analysis as A
+    from batoid_gb300.rayVector import concatenateRayVectors
+    L = _lib.lib()
+    F = len(HUYGENS_FIELDS)
     thx = np.deg2rad([f[0] for f in HUYGENS_FIELDS])
     thy = np.deg2rad([f[1] for f in HUYGENS_FIELDS])
+    n = nx * nx
+    rays = concatenateRayVectors([bt.RayVector.asGrid(optic=opt, wavelength=wavelength, theta_x=thx[f],
+                                                      theta_y=thy[f], nx=nx) for f in range(F)])
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    opt.trace(rays)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_trace = e0.elapsed_time(e1)
+    cidx = (nx // 2) * nx + nx // 2
+    pts = np.ascontiguousarray([[rays.x[f * n + cidx], rays.y[f * n + cidx], 0.0] for f in range(F)])
+    t0 = np.ascontiguousarray([float(rays.t[f * n]) for f in range(F)])
+    lat = np.ascontiguousarray(np.tile([pitch, 0.0, 0.0, pitch], (F, 1)))
+    re = D.empty(F * npix * npix)
+    im = D.empty(F * npix * npix)
+    dp = _lib.c_double_p
+
+    def sums():
+        _lib.check(L.bt_huygens_amplitudes_fields(rays._rv, F, pts.ctypes.data_as(dp), lat.ctypes.data_as(dp),
+                                                  t0.ctypes.data_as(dp), npix, npix, 1, D.ptr(re), D.ptr(im),
+                                                  D.stream_ptr()))
+
+    sums()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        sums()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_psf = e0.elapsed_time(e1) / reps
+    psf = (D.to_host(re) ** 2 + D.to_host(im) ** 2).reshape(F, npix, npix)
+    valid = (~rays.failed & ~rays.vignetted)
+    pairs = int(valid.sum()) * npix * npix
+    rng = np.random.default_rng(5)
+    max_err = 0.0
+    for f in range(F):
+        view = bt.RayVector._fromBuffers(rays._d[:, f * n:(f + 1) * n], rays._b[:, f * n:(f + 1) * n],
+                                         rays.coordSys)
+        peak = psf[f].max()
+        for a, b in rng.integers(0, npix, (check_pixels // 4, 2)):
+            P = (pts[f][0] + (b - npix // 2) * pitch, pts[f][1] + (a - npix // 2) * pitch, 0.0)
+            ref = view.sumAmplitude(P, t0[f])
+            max_err = max(max_err, abs(abs(ref) ** 2 - psf[f, a, b]) / peak)
+    # through the public API: one huygensPSFs call vs nine huygensPSF calls
+    # (host clock around ray generation, trace, sums and the copy back)
     A.huygensPSFs(opt, thx, thy, wavelength, nx=nx, dx=pitch, nxOut=npix)  # warm-up
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     multi = A.huygensPSFs(opt, thx, thy, wavelength, nx=nx, dx=pitch, nxOut=npix)
     ms_multi = (time.perf_counter() - t1) * 1e3
-    # the same through the public per-field call, timed the same way (host
-    # clock around ray generation, trace, sums and the copy back)
     t1 = time.perf_counter()
-    for f in range(len(thx)):
-        A.huygensPSF(opt, thx[f], thy[f], wavelength, nx=nx, dx=pitch, nxOut=npix)
+    single = [A.huygensPSF(opt, thx[f], thy[f], wavelength, nx=nx, dx=pitch, nxOut=npix) for f in range(F)]
     ms_per_field_api = (time.perf_counter() - t1) * 1e3
     out = {
-        "workload": f"{len(HUYGENS_FIELDS)} fields x {nx}x{nx} pupil rays x {npix}x{npix} px at {pitch*1e6:.0f} um, "
+        "workload": f"{F} fields x {nx}x{nx} pupil rays x {npix}x{npix} px at {pitch*1e6:.0f} um, "
                     f"{wavelength*1e9:.0f} nm, tma_corrector",
-        "api_wall_ms": {"huygensPSF_per_field": ms_per_field_api, "huygensPSFs_one_call": ms_multi},
-        "fields_per_s_one_call": len(HUYGENS_FIELDS) / (ms_multi * 1e-3),
-        "one_call_max_diff_rel_peak": max(float(np.abs(m.array - (k[3])).max() / k[3].max()) for m, k in zip(multi, kept)),
-        "fields_per_s": len(HUYGENS_FIELDS) / (sums["ms_trace_and_psf"] * 1e-3),
-        "ray_pixel_pairs_per_s": pairs / (sums["ms_psf_kernels"] * 1e-3),
-        "ms_total": sums["ms_trace_and_psf"], "ms_psf": sums["ms_psf_kernels"],
+        "fields_per_s": F / ((ms_trace + ms_psf) * 1e-3),
+        "ray_pixel_pairs_per_s": pairs / (ms_psf * 1e-3),
+        "ms_trace": ms_trace, "ms_psf": ms_psf, "ms_total": ms_trace + ms_psf,
+        "gpu_launches": {"trace": 1, "psf": 3},
         "psf_max_err_rel_peak": max_err,
-        "err_reference": "FP64 per-pixel phasor sum (bt_rv_sum_amplitude) on sampled pixels",
+        "err_reference": "FP64 per-pixel phasor sum (bt_rv_sum_amplitude) on sampled pixels of every field",
+        "api_wall_ms": {"huygensPSF_per_field": ms_per_field_api, "huygensPSFs_one_call": ms_multi},
+        "fields_per_s_one_call": F / (ms_multi * 1e-3),
+        "one_call_vs_per_field_max_abs_diff": max(float(np.abs(m.array - o.array).max()) for m, o in zip(multi, single)),
     }
+    if fp32_peak:
+        ach = 10.0 * pairs / (ms_psf * 1e-3) / 1e12
+        out["roofline"] = {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
+                           "frac": ach / fp32_peak, "flops_per_pair": 10,
+                           "peak_source": "FFMA loop measured in this run (bt_measure_fp32_peak)",
+                           "note": "prep + phasor sums + reduce of all fields over their event time"}
     if cpu:
         # oracle (C, all threads): per-pixel sumAmplitude on a pixel sample, extrapolated
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as ora
-        rays, point, t0, _ = kept[4]
-        host = ora.Rays(*[getattr(rays, k) for k in ora.Rays.FIELDS], rays.vignetted, rays.failed)
+        f = 4
+        sl = slice(f * n, (f + 1) * n)
+        host = ora.Rays(*[getattr(rays, k)[sl] for k in ora.Rays.FIELDS], rays.vignetted[sl], rays.failed[sl])
         npx = 64
         t1 = time.perf_counter()
         for k in range(npx):
-            ora.sum_amplitude(host, (point[0] + k * pitch, point[1], 0.0), t0)
+            ora.sum_amplitude(host, (pts[f][0] + k * pitch, pts[f][1], 0.0), t0[f])
         per_px = (time.perf_counter() - t1) / npx
-        out["cpu_baseline"] = {"s_per_pixel": per_px, "cores": ora.threads(),
-                               "extrapolated_s_total": per_px * npix * npix * len(HUYGENS_FIELDS),
+        out["cpu_baseline"] = {"s_per_pixel": per_px, "cores": ora.threads(), "kind": "port",
+                               "extrapolated_s_total": per_px * npix * npix * F,
                                "sample": f"{npx} pixels of one field, oracle sumAmplitude (reference algorithm)"}
-        out["speedup_vs_cpu"] = out["cpu_baseline"]["extrapolated_s_total"] / (sums["ms_psf_kernels"] * 1e-3)
+        out["speedup_vs_cpu"] = out["cpu_baseline"]["extrapolated_s_total"] / (ms_psf * 1e-3)
     return out
 
 
@@ -595,50 +740,37 @@ def run_gpu(args):
     # sanity: the benchmark traced real rays
     vig = float(rv_out.field("vignetted").float().mean().item())
 
-    # FP64 roofline of the fused trace kernel (one launch per step)
+    # FP64 roofline of the fused trace kernel (one launch per step).  The
+    # numerator is the FP64 work the kernel executes (DADD + DMUL + 2 DFMA per
+    # ray, from the committed ncu census of the same kernel and workload);
+    # the reference-expression flop count is reported beside it.
     fpeak = ctypes.c_double(0.0)
     _lib.check(L.bt_measure_fp64_peak(1 << 14, ctypes.byref(fpeak), sp))
-    flops_per_ray = WC.optic_flops_per_ray(opt, niter)
-    achieved_tflops = flops_per_ray * n / (ms_per_step * 1e-3) / 1e12
+    ref_flops_per_ray = WC.optic_flops_per_ray(opt, niter)
+    ref_tflops = ref_flops_per_ray * n / (ms_per_step * 1e-3) / 1e12
+    counters = load_counters(f"k_trace/{args.workload}")
+    exec_fpr = executed_fp64_flops(counters)
+    exec_tflops = exec_fpr * n / (ms_per_step * 1e-3) / 1e12 if exec_fpr else None
     bytes_per_ray = WC.READ_BYTES_PER_RAY + WC.WRITE_BYTES_PER_RAY
     hbm_gbs = bytes_per_ray * n / (ms_per_step * 1e-3) / 1e9
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except (OSError, ValueError):
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    traffic_per_ray = load_traffic(args.workload)
+    hbm_peak = measured_peaks().get("hbm_gbs", 6800.0)
 
     # end to end through the C-ABI with pinned host buffers
-    host = [torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).pin_memory() for x in arrs[:9]]
-    hflags = [torch.from_numpy(np.ascontiguousarray(x, dtype=np.uint8)).pin_memory() for x in arrs[9:]]
-    pristine = [h.clone() for h in host] + [f.clone() for f in hflags]
-    hrv = _lib.BtRayVector(*[h.data_ptr() for h in host], *[f.data_ptr() for f in hflags], n)
-    chunk = 1 << 21
-    e2e_ms = 0.0
-    for it in range(1 + args.e2e_steps):
-        for dst, src in zip(host + hflags, pristine):
-            dst.copy_(src)
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        _lib.check(L.bt_optic_trace_host(prog._optic.ptr, ctypes.byref(hrv), niter, chunk, sp))
-        dt = (time.perf_counter() - t1) * 1e3
-        if it > 0:
-            e2e_ms += dt
-    e2e_ms /= max(args.e2e_steps, 1)
+    e2e_ms, h2d, d2h = host_trace_e2e(L, _lib, prog, arrs, n, niter, args.e2e_steps, sp)
     e2e_value = total_rays * nsurf / (e2e_ms * 1e-3)
-    h2d = n * (9 * 8 + 2)
-    d2h = n * (8 * 8 + 2)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.workload)
+    paraboloid = None
+    if rank == 0 and not args.no_paraboloid:
+        paraboloid = bench_paraboloid(bt, fpeak.value, cpu=not args.no_cpu_baseline)
     huygens = None
     if rank == 0 and not args.no_huygens:
         del rv_in, rv_out
-        huygens = bench_huygens(bt, opt, cpu=not args.no_cpu_baseline)
+        fp32 = ctypes.c_double(0.0)
+        _lib.check(L.bt_measure_fp32_peak(1 << 14, ctypes.byref(fp32), sp))
+        huygens = bench_huygens(bt, opt, cpu=not args.no_cpu_baseline, fp32_peak=fp32.value)
     batched = None
     if rank == 0 and not args.no_batch:
         batched = bench_batched(bt, nstates=args.batch_states, cpu=not args.no_cpu_baseline,
@@ -657,11 +789,18 @@ def run_gpu(args):
                        "rays_per_gpu": n, "surfaces": nsurf, "niter": niter,
                        "l2": "inputs larger than L2 (1.2 GB per step), no flush",
                        "vignetted_fraction": vig},
-            "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": fpeak.value, "unit": "TFLOP/s",
-                         "frac": achieved_tflops / fpeak.value if fpeak.value else None,
-                         "traffic": (traffic_per_ray * n if traffic_per_ray else None),
+            "roofline": {"bound": "fp64", "achieved": exec_tflops, "peak": fpeak.value, "unit": "TFLOP/s",
+                         "frac": exec_tflops / fpeak.value if (exec_tflops and fpeak.value) else None,
+                         "traffic": (counters["dram_bytes_per_ray"] * n if counters else None),
                          "peak_source": "DFMA loop measured in this run (bt_measure_fp64_peak)",
-                         "flops_per_ray": flops_per_ray,
+                         "executed_flops_per_ray": exec_fpr,
+                         "counters": counters,
+                         "fp64_pipe_busy": (counters or {}).get("fp64_pipe_busy_pct"),
+                         "reference_flops": {"flops_per_ray": ref_flops_per_ray, "tflops": ref_tflops,
+                                             "ratio_to_peak": ref_tflops / fpeak.value if fpeak.value else None,
+                                             "convention": "FP64 operations of the reference's own expressions "
+                                                           "(batoid_gb300/workcount.py); the kernel executes "
+                                                           "fewer (FP32 derivatives, float-float polynomials)"},
                          "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s",
                                  "frac": hbm_gbs / hbm_peak, "bytes_per_ray": bytes_per_ray,
                                  "peak_source": "MEASURED_PEAKS.json hbm_gbs"}},
@@ -670,6 +809,7 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": args.steps,
+            "paraboloid": paraboloid,
             "huygens_psf": huygens,
             "batched_wavefronts": batched,
             "surrogate": surrogate,

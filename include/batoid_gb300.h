@@ -256,6 +256,16 @@ int bt_huygens_amplitudes(const bt_rayvector* rv, double px, double py, double p
                           const double lat[4], int na, int nb, double t0, int ignore_vignetted,
                           double* out_re, double* out_im, void* stream);
 
+/* bt_huygens_amplitudes for many fields in one launch set (what huygensPSF
+ * computes per field, batoid/analysis.py:181-305, for a list of fields).
+ * Field f's rays are rows [f*n/nfields, (f+1)*n/nfields) of rv (n must be a
+ * multiple of nfields); its point is points[3f..3f+2], its lattice
+ * lat[4f..4f+3] and its reference time t0[f] (host arrays).  Outputs:
+ * device arrays of nfields*na*nb doubles, [f][a][b]. */
+int bt_huygens_amplitudes_fields(const bt_rayvector* rv, int nfields, const double* points, const double* lat,
+                                 const double* t0, int na, int nb, int ignore_vignetted, double* out_re,
+                                 double* out_im, void* stream);
+
 /* Allocation-free bt_huygens_amplitudes (no counterpart in the reference).
  * For callers that may not allocate device memory -- e.g. a host framework
  * that owns all device memory under a fixed budget, or a latency-critical
@@ -264,8 +274,10 @@ int bt_huygens_amplitudes(const bt_rayvector* rv, double px, double py, double p
  * the library until exit.  Limit: 32 bytes per ray + 16 bytes per pixel must
  * fit in 8 MiB (e.g. 245,760 rays with a 128x128 lattice); larger problems
  * return BT_ERR_ARG with the size needed.  The first call on a device sets
- * up the scratch address (make it before any stream capture).  All calls
- * share the array: calls that overlap on the GPU race. */
+ * up the scratch address (make it before any stream capture); that address
+ * is cached and not refreshed after cudaDeviceReset, so do not call this
+ * again on a device that was reset.  All calls share the array: calls that
+ * overlap on the GPU race. */
 int bt_huygens_amplitudes_noalloc(const bt_rayvector* rv, double px, double py, double pz,
                                   const double lat[4], int na, int nb, double t0, int ignore_vignetted,
                                   double* out_re, double* out_im, void* stream);
@@ -418,6 +430,10 @@ int bt_surrogate_combine(const float* feat, int nfeat, int nlin, const int* grp,
  * with independent DFMA chains; `iters` FMAs per chain (e.g. 1 << 14).
  * The denominator of the tracer's FP64 roofline.  Synchronous. */
 int bt_measure_fp64_peak(int iters, double* tflops, void* stream);
+
+/* The same for the FP32 pipe (independent FFMA chains, 2 flops per FMA):
+ * the denominator of the Huygens phasor sums' roofline.  Synchronous. */
+int bt_measure_fp32_peak(int iters, double* tflops, void* stream);
 
 /* Reads and clears the device status word of the blob-staging kernels:
  * BT_ERR_TIMEOUT if a kernel's bounded wait for its descriptor copy expired

@@ -46,7 +46,9 @@ def import_reference(ref_root=None):
     """Return the reference ``batoid`` module, or raise ImportError."""
     if "batoid" in sys.modules and getattr(sys.modules["batoid"], "_is_ref", False):
         return sys.modules["batoid"]
-    ref_root = ref_root or os.environ.get("BATOID_REF", "/root/reference")
+    ref_root = ref_root or os.environ.get("BATOID_REF")
+    if not ref_root:
+        raise ImportError("reference root not given: pass it or set BATOID_REF")
     pkg = os.path.join(ref_root, "batoid")
     if not os.path.isdir(pkg):
         raise ImportError(f"reference sources not found at {pkg}")

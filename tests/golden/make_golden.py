@@ -3,8 +3,8 @@
 Run in a container that has the reference sources and its compiled module
 (oracle/Makefile.ref builds oracle/_ref/_batoid*.so from them):
 
-    make -f oracle/Makefile.ref -j8
-    python tests/golden/make_golden.py [/path/to/reference]
+    make -f oracle/Makefile.ref REF=/path/to/reference -j8
+    python tests/golden/make_golden.py /path/to/reference   (or BATOID_REF)
 
 Every fixture stores seeded inputs and the reference's outputs for them.
 The inputs are regenerated from the same seeds by the tests, so only the
@@ -291,6 +291,123 @@ def zemax_fixture(batoid, ref_root):
     return out
 
 
+def _utf16_rows(path, skip, nrows, cols):
+    with open(path, encoding='utf-16-le') as f:
+        return np.genfromtxt(f, skip_header=skip, max_rows=nrows, usecols=cols)
+
+
+def zemax_more_fixture(batoid, ref_root):
+    """More Zemax goldens of the reference's tests (tests/test_zemax.py):
+    LSST wavefronts (:224-270, 1e-11 m), the HSC Zernike decomposition
+    (:189-221), DECam traces and exit pupil (:466-534), CBP traces
+    (:536-612) and ComCam traces (:614-700).  Each optic is stored as its
+    parsed YAML configuration; the reference's own outputs for the same
+    calls are stored beside the Zemax data."""
+    import copy
+    import json
+    from batoid_gb300.parse import yaml_load
+    out = {}
+    data = os.path.join(ref_root, "batoid", "data")
+    testdata = os.path.join(ref_root, "tests", "testdata")
+
+    def load(rel, key):
+        cfg = yaml_load(open(os.path.join(data, rel)).read())
+        out[f"{key}_config"] = np.array(json.dumps(cfg))
+        return batoid.parse.parse_optic(copy.deepcopy(cfg["opticalSystem"]))
+
+    # LSST wavefronts, nx 32, chief reference, zemax projection
+    tel = load("LSST/LSST_g_500.yaml", "lsst")
+    for k, (thx, thy, fn) in enumerate([(0.0, 0.0, "LSST_wf_0.0_0.0.txt"), (0.0, 1.225, "LSST_wf_0.0_1.225.txt"),
+                                        (0.0, 1.75, "LSST_wf_0.0_1.75.txt"),
+                                        (1.176, 1.176, "LSST_wf_1.176_1.176.txt")]):
+        with open(os.path.join(testdata, fn), encoding='utf-16-le') as f:
+            Zwf = np.loadtxt(f, skiprows=16)[::-1]
+        out[f"lsstwf{k}_field_deg"] = np.array([thx, thy])
+        out[f"lsstwf{k}_zemax"] = Zwf
+        bwf = batoid.wavefront(tel, np.deg2rad(thx), np.deg2rad(thy), 500e-9, nx=32, reference='chief',
+                               projection='zemax')
+        out[f"lsstwf{k}_ref"] = np.asarray(bwf.array.data)
+        out[f"lsstwf{k}_ref_mask"] = np.asarray(bwf.array.mask)
+    # HSC Zernike decomposition by Zemax: jmax 37 at 0.75 deg, 750 nm, nx 256
+    tel = load("HSC/HSC_no_obsc.yaml", "hsc_no_obsc")
+    zz = [0.0]
+    with open(os.path.join(testdata, "HSC_Zernike.txt")) as f:
+        for i, line in enumerate(f):
+            if i > 38:
+                zz.append(float(line[9:20]))
+    out["hsc_zernike_zemax"] = np.array(zz)
+    # the reference's wavefront that the reference's zernike fits (GalSim-free part)
+    bwf = batoid.wavefront(tel, 0.0, np.deg2rad(0.75), 750e-9, nx=64, reference='chief', projection='zemax')
+    out["hsc_wf64_ref"] = np.asarray(bwf.array.data)
+    out["hsc_wf64_ref_mask"] = np.asarray(bwf.array.mask)
+    # DECam
+    tel = load("DECam/DECam.yaml", "decam")
+    for k in range(3):
+        fn = os.path.join(testdata, f"DECam_raytrace_{k}.txt")
+        out[f"decam{k}_hp"] = _utf16_rows(fn, 13, 4, (6,))
+        out[f"decam{k}_zemax"] = _utf16_rows(fn, 22, 40, list(range(1, 12)))
+        Hx, Hy, Px, Py = out[f"decam{k}_hp"]
+        ray = batoid.RayVector.fromStop(Px * 2.005, Py * 2.005, optic=tel, stopSurface=tel['PM'],
+                                        wavelength=700e-9, theta_x=np.deg2rad(Hx * 1.1),
+                                        theta_y=np.deg2rad(Hy * 1.1), projection='zemax')
+        out.update(rv_to_dict(ray, f"decam{k}_in"))
+        tf = tel.traceFull(ray)
+        out[f"decam{k}_names"] = np.array(list(tf.keys()))
+        for name, v in tf.items():
+            out.update(rv_to_dict(v["out"].toCoordSys(batoid.CoordSys()), f"decam{k}_{name}"))
+    tel.stopSurface = tel['PM']
+    out["decam_epp_ref"] = np.asarray(batoid.exitPupilPos(tel, wavelength=700e-9))
+    out["decam_D_z"] = np.array(tel['D'].coordSys.origin[2])
+    # CBP
+    tel = load("LSST/CBP.yaml", "cbp")
+    for i in range(1, 5):
+        fn = os.path.join(testdata, f"CBP_SRT{i}.txt")
+        out[f"cbp{i}_wavelength_um"] = np.atleast_1d(_utf16_rows(fn, 8, 1, (2,)))
+        out[f"cbp{i}_hp"] = _utf16_rows(fn, 13, 4, (6,))
+        out[f"cbp{i}_rows"] = _utf16_rows(fn, 22, 18, list(range(0, 12)))
+    # ComCam, six bands
+    for band in "ugrizy":
+        load(f"LSST/ComCam_{band}.yaml", f"comcam_{band}")
+        for i in (1, 2):
+            fn = os.path.join(testdata, f"ComCam_SRT{i}_{band.upper()}.txt")
+            out[f"comcam_{band}{i}_wavelength_um"] = np.atleast_1d(_utf16_rows(fn, 8, 1, (2,)))
+            out[f"comcam_{band}{i}_hp"] = _utf16_rows(fn, 13, 4, (6,))
+            out[f"comcam_{band}{i}_rows"] = _utf16_rows(fn, 22, 18, list(range(0, 12)))
+    return out
+
+
+def wavefront_fixture(batoid):
+    """The reference's own batoid.wavefront (batoid/analysis.py:308-388),
+    huygensPSF (:181-305) and dkdu (:17-56) on the 12-surface system: three
+    fields, an even and an odd pupil grid, both reference points, and both
+    lattice paths of huygensPSF (dx given; dx None, from dkdu)."""
+    opt = W.tma_optic(batoid, zernike_factory=ref_zernike_factory(batoid))
+    A = batoid.analysis
+    out = {}
+    fields = [(0.0, 0.0), (np.deg2rad(0.8), np.deg2rad(-0.5)), (np.deg2rad(-1.2), np.deg2rad(0.9))]
+    out["fields"] = np.array(fields)
+    for f, (tx, ty) in enumerate(fields):
+        for nx in (32, 33):
+            for ref in ("chief", "mean"):
+                wf = A.wavefront(opt, tx, ty, 620e-9, nx=nx, reference=ref)
+                out[f"wf_{f}_{nx}_{ref}"] = np.asarray(wf.array.data)
+                out[f"wf_{f}_{nx}_{ref}_mask"] = np.asarray(wf.array.mask)
+                out[f"wf_{f}_{nx}_{ref}_prim"] = np.asarray(wf.primitiveVectors)
+        out[f"dkdu_{f}"] = np.asarray(A.dkdu(opt, tx, ty, 620e-9))
+    # huygensPSF: field 1 and 2, both lattice paths
+    for f in (1, 2):
+        tx, ty = fields[f]
+        for nx in (32, 33):
+            for ref in ("chief", "mean"):
+                p = A.huygensPSF(opt, tx, ty, 620e-9, nx=nx, dx=1.5e-6, nxOut=20, reference=ref)
+                out[f"hpsf_{f}_{nx}_{ref}_dx"] = np.asarray(p.array)
+                out[f"hpsf_{f}_{nx}_{ref}_dx_prim"] = np.asarray(p.primitiveVectors)
+        p = A.huygensPSF(opt, tx, ty, 620e-9, nx=24, reference="chief")
+        out[f"hpsf_{f}_24_chief_dkdu"] = np.asarray(p.array)
+        out[f"hpsf_{f}_24_chief_dkdu_prim"] = np.asarray(p.primitiveVectors)
+    return out
+
+
 def split_fixture(batoid):
     """rSplit on single surfaces (incl. TIR, misses, failed inputs) and
     traceSplit through a two-singlet system with 2 % reflecting coatings."""
@@ -347,7 +464,9 @@ def factories_fixture(batoid):
 
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    ref_root = args[0] if args else "/root/reference"
+    ref_root = args[0] if args else os.environ.get("BATOID_REF")
+    if not ref_root:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT [--only-...]  (or set BATOID_REF)")
     os.environ["BATOID_REF"] = ref_root
     batoid = import_reference(ref_root)
     batoid.global_vars._batoid_max_threads = 1
@@ -356,6 +475,12 @@ def main():
         return
     if "--only-factories" in sys.argv:
         np.savez_compressed(os.path.join(HERE, "factories.npz"), **factories_fixture(batoid))
+        return
+    if "--only-zemax-more" in sys.argv:
+        np.savez_compressed(os.path.join(HERE, "zemax_more.npz"), **zemax_more_fixture(batoid, ref_root))
+        return
+    if "--only-wavefront" in sys.argv:
+        np.savez_compressed(os.path.join(HERE, "wavefront.npz"), **wavefront_fixture(batoid))
         return
     if "--only-analysis" in sys.argv:
         np.savez_compressed(os.path.join(HERE, "analysis.npz"), **analysis_fixture(batoid))
@@ -368,6 +493,8 @@ def main():
     np.savez_compressed(os.path.join(HERE, "split.npz"), **split_fixture(batoid))
     np.savez_compressed(os.path.join(HERE, "analysis.npz"), **analysis_fixture(batoid))
     np.savez_compressed(os.path.join(HERE, "factories.npz"), **factories_fixture(batoid))
+    np.savez_compressed(os.path.join(HERE, "zemax_more.npz"), **zemax_more_fixture(batoid, ref_root))
+    np.savez_compressed(os.path.join(HERE, "wavefront.npz"), **wavefront_fixture(batoid))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

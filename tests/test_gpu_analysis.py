@@ -76,8 +76,8 @@ def test_doubleZernike_reproduces_field_dependence(optic):
 
 @pytest.mark.parametrize("dx,reference", [(2e-6, "chief"), (None, "chief"), (2e-6, "mean")])
 def test_huygens_psfs_match_per_field_calls(optic, dx, reference):
-    """Many fields in one trace launch and one copy back: each PSF equals
-    the single-field call's."""
+    """Many fields in one trace launch, one launch set of the phasor sums
+    and one copy back: each PSF equals the single-field call's bit for bit."""
     thx = np.deg2rad([0.0, 0.6, -1.1])
     thy = np.deg2rad([0.0, -0.4, 0.9])
     kw = dict(nx=48, dx=dx, nxOut=24, reference=reference)
@@ -87,4 +87,41 @@ def test_huygens_psfs_match_per_field_calls(optic, dx, reference):
         one = bt.huygensPSF(optic, thx[f], thy[f], WL, **kw)
         assert many[f].array.shape == one.array.shape
         np.testing.assert_allclose(many[f].primitiveVectors, one.primitiveVectors, rtol=1e-12, atol=0)
-        np.testing.assert_allclose(many[f].array, one.array, rtol=0, atol=1e-9 * one.array.max())
+        np.testing.assert_array_equal(many[f].array, one.array)
+
+
+def test_huygens_fields_entry_point_matches_single_field_calls(optic):
+    """bt_huygens_amplitudes_fields over 70 fields (two launch sets of at
+    most 64 fields) equals bt_huygens_amplitudes per field bit for bit; a
+    ray count that is not a multiple of the field count is an argument
+    error."""
+    import ctypes
+    from batoid_gb300 import _lib, _device as D
+    from batoid_gb300.rayVector import concatenateRayVectors
+    L = _lib.lib()
+    F, nx, npix = 70, 6, 5
+    rng = np.random.default_rng(3)
+    thx = np.deg2rad(rng.uniform(-1, 1, F))
+    thy = np.deg2rad(rng.uniform(-1, 1, F))
+    rays = concatenateRayVectors([bt.RayVector.asGrid(optic=optic, wavelength=WL, theta_x=thx[f], theta_y=thy[f],
+                                                      nx=nx) for f in range(F)])
+    optic.trace(rays)
+    n = nx * nx
+    pts = np.ascontiguousarray([[rays.x[f * n + 21], rays.y[f * n + 21], 0.0] for f in range(F)])
+    lat = np.ascontiguousarray(rng.uniform(1e-6, 3e-6, (F, 4)) * [1, 0.1, 0.1, 1])
+    t0 = np.ascontiguousarray([float(rays.t[f * n]) for f in range(F)])
+    re = D.empty(F * npix * npix)
+    im = D.empty(F * npix * npix)
+    dp = _lib.c_double_p
+    _lib.check(L.bt_huygens_amplitudes_fields(rays._rv, F, pts.ctypes.data_as(dp), lat.ctypes.data_as(dp),
+                                              t0.ctypes.data_as(dp), npix, npix, 1, D.ptr(re), D.ptr(im),
+                                              D.stream_ptr()))
+    got = (D.to_host(re) + 1j * D.to_host(im)).reshape(F, npix, npix)
+    for f in range(F):
+        view = bt.RayVector._fromBuffers(rays._d[:, f * n:(f + 1) * n], rays._b[:, f * n:(f + 1) * n],
+                                         rays.coordSys)
+        a, b = bt.analysis.huygens_amplitudes(view, pts[f], lat[f].reshape(2, 2), npix, npix, t0[f])
+        np.testing.assert_array_equal(got[f], a + 1j * b)
+    rc = L.bt_huygens_amplitudes_fields(rays._rv, F + 1, pts.ctypes.data_as(dp), lat.ctypes.data_as(dp),
+                                        t0.ctypes.data_as(dp), npix, npix, 1, D.ptr(re), D.ptr(im), D.stream_ptr())
+    assert rc != 0

@@ -155,17 +155,3 @@ def test_training_reduces_loss():
     pred = D.to_host(net.predict(x))
     assert np.sqrt(np.mean((pred - ts) ** 2)) < 0.1
 
-
-def test_gemm_cta_pair_path():
-    """The epilogue and many-tile tests again with CTA pairs (B multicast)
-    forced for every shape, incl. an odd number of row tiles (M = 384), in a
-    fresh process (the launcher reads the switch once)."""
-    import os
-    import subprocess
-    import sys
-    here = os.path.dirname(os.path.abspath(__file__))
-    env = dict(os.environ, BATOID_GB300_GEMM_CLUSTER="1")
-    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-p", "no:cacheprovider", os.path.abspath(__file__),
-                        "-k", "epilogues or many_tiles or gradients"],
-                       cwd=os.path.dirname(here), env=env, capture_output=True, text=True, timeout=600)
-    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]

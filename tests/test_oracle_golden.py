@@ -121,3 +121,18 @@ def test_oracle_sellmeier_known_answers():
                                 97.93400253792099)
     got = np.array([ora.getN(silica, w * 1e-6) for w in g["csv_wmicron"]])
     np.testing.assert_allclose(got, g["csv_n"], atol=0, rtol=1e-13)
+
+
+@pytest.mark.parametrize("workload", ["paraboloid", "tma_corrector"])
+def test_oracle_optics_builder_matches_package(workload):
+    """oracle/optics.py builds the workloads without the product package (the
+    reference arm of bench.py uses it); its trace equals the trace of the
+    package-built optic bit for bit."""
+    import optics as OO
+    Wo = OO.workloads()
+    build, make_rays, _ = Wo.WORKLOADS[workload]
+    arrs = make_rays(3000, seed=11)
+    a = ora.trace(build(OO), ora.Rays(*arrs))
+    b = ora.trace(W.WORKLOADS[workload][0](bt), ora.Rays(*arrs))
+    np.testing.assert_array_equal(a.d, b.d)
+    np.testing.assert_array_equal(a.b, b.b)

@@ -7,7 +7,8 @@ import batoid_gb300 as bt
 from batoid_gb300.parse import yaml_load, parse_optic
 import oracle as ora
 from _helpers import golden, assert_rays_match, FIELDS
-from _zemax import optic, check_lsst, check_hsc, HSC_NAMES
+from _zemax import (optic, check_lsst, check_hsc, check_decam, check_cbp, check_comcam, cbp_start, comcam_start,
+                    HSC_NAMES)
 
 DOC = """
 top:
@@ -87,3 +88,44 @@ def test_oracle_hsc_zemax(k):
         pos, vel = _global(r)
         by_name[name] = (pos[0, 0], pos[0, 1], pos[0, 2], vel[0, 0], vel[0, 1], vel[0, 2])
     check_hsc(by_name, g[f"hsc{k}_zemax"])
+
+
+def _by_name(outs):
+    by_name = {}
+    for name, r in outs:
+        pos, vel = _global(r)
+        by_name[name] = (pos[0, 0], pos[0, 1], pos[0, 2], vel[0, 0], vel[0, 1], vel[0, 2])
+    return by_name
+
+
+def _one_ray(x, y, z, vx, vy, vz, t, wl):
+    return ora.Rays([x], [y], [z], [vx], [vy], [vz], [t], [wl], [1.0], [False], [False])
+
+
+@pytest.mark.parametrize("k", [0, 1, 2])
+def test_oracle_decam_zemax(k):
+    g = golden("zemax_more")
+    tel = optic("decam", "zemax_more")
+    rays = ora.Rays(*[g[f"decam{k}_in_{f}"] for f in FIELDS])
+    outs = ora.trace(tel, rays, full=True)
+    assert [n for n, _ in outs] == list(g[f"decam{k}_names"])
+    for name, r in outs:
+        pos, _ = _global(r)
+        np.testing.assert_allclose(pos[0], [g[f"decam{k}_{name}_{c}"][0] for c in "xyz"], rtol=0, atol=1e-12)
+    by_name = _by_name(outs)
+    check_decam([by_name[n] for n, _ in outs], g[f"decam{k}_zemax"])
+
+
+@pytest.mark.parametrize("i", [1, 2, 3, 4])
+def test_oracle_cbp_zemax(i):
+    g = golden("zemax_more")
+    check_cbp(_by_name(ora.trace(optic("cbp", "zemax_more"), _one_ray(*cbp_start(g, i)), full=True)), g, i)
+
+
+@pytest.mark.parametrize("band", list("ugrizy"))
+def test_oracle_comcam_zemax(band):
+    g = golden("zemax_more")
+    tel = optic(f"comcam_{band}", "zemax_more")
+    for i in (1, 2):
+        by_name = _by_name(ora.trace(tel, _one_ray(*comcam_start(g, band, i)), full=True))
+        check_comcam({k: v[:3] for k, v in by_name.items()}, g, band, i)
