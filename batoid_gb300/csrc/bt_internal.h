@@ -31,6 +31,7 @@ struct SnapSet {
 // Status word written by kernels whose bounded waits expire (0 = fine).
 // Read and cleared by bt_check_device_status().
 cudaError_t bt_read_device_status(int* status, cudaStream_t stream);
+cudaError_t bt_read_split_device_status(int* status, cudaStream_t stream);
 
 // trace.cu
 cudaError_t bt_launch_trace(const unsigned char* d_blob, int blob_bytes, const RV& in, const RV& out,
@@ -89,4 +90,5 @@ cudaError_t bt_launch_zk_normal(const double* x, const double* y, const double* 
                                 cudaStream_t stream);
 
 int bt_sm_count();
+int bt_grid_for(long long n, int threads, int per_sm);  // ceil(n / threads), at most per_sm per SM
 void bt_keep_pool();  // keep the default pool's freed scratch cached (once per process)

@@ -1286,8 +1286,10 @@ extern "C" int bt_measure_fp32_peak(int iters, double* tflops, void* stream) {
 // Test hook: reads and clears the device status word of the trace kernels
 // (BT_ERR_TIMEOUT if a bounded wait expired).  Synchronous.
 extern "C" int bt_check_device_status(void* stream) {
-    int st = 0, sb = 0, sm = 0;
+    int st = 0, sb = 0, sm = 0, ss = 0;
     CUDA_TRY(bt_read_device_status(&st, (cudaStream_t)stream), "device status");
+    CUDA_TRY(bt_read_split_device_status(&ss, (cudaStream_t)stream), "device status");
+    if (st == 0) st = ss;
     CUDA_TRY(bt_read_batch_device_status(&sb, (cudaStream_t)stream), "device status");
     CUDA_TRY(bt_read_mlp_device_status(&sm, (cudaStream_t)stream), "device status");
     const int any = st ? st : (sb ? sb : sm);

@@ -26,11 +26,11 @@ cudaError_t bt_read_device_status(int* status, cudaStream_t stream) {
 }
 
 #define TRACE_THREADS 256
-#define BT_TRACE_MINB_DEFAULT 2
+#define BT_TRACE_MINB 2
 
 // MINB = resident blocks per SM the register budget is sized for: 2 gives
-// 128 registers (16 warps per SM, a few spills), 1 gives the compiler's
-// choice (no spills, fewer warps per SM).
+// 128 registers (16 warps per SM).  (1, the compiler's choice of registers
+// and 8 warps per SM, measured slower.)
 //
 // Stage-synchronous: the block's rays advance one stage at a time with a
 // barrier between stages, so all warps of the block run the same stage's
@@ -112,7 +112,7 @@ int bt_sm_count() {
     return g_sm_count;
 }
 
-static int grid_for(long long n, int threads, int per_sm) {
+int bt_grid_for(long long n, int threads, int per_sm) {
     long long need = (n + threads - 1) / threads;
     long long cap = (long long)bt_sm_count() * per_sm;
     if (need > cap) need = cap;
@@ -125,117 +125,15 @@ cudaError_t bt_launch_trace(const unsigned char* d_blob, int blob_bytes, const R
     if (in.n <= 0) return cudaSuccess;
     static SnapSet empty;
     const SnapSet& ss = snaps ? *snaps : empty;
-    // register budget variant; BATOID_GB300_TRACE_MINB=1 or 2 overrides
-    static int minb = 0;
-    if (minb == 0) {
-        const char* env = getenv("BATOID_GB300_TRACE_MINB");
-        minb = (env && atoi(env) == 1) ? 1 : (env && atoi(env) == 2) ? 2 : BT_TRACE_MINB_DEFAULT;
-    }
-    auto kern = (minb == 1) ? k_trace<1> : k_trace<2>;
+    auto kern = k_trace<BT_TRACE_MINB>;
     if (blob_bytes > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, blob_bytes);
         if (e != cudaSuccess) return e;
     }
     // Persistent grid (2 blocks per SM): the blob is staged once per block
     // and amortised over the grid-stride loop.
-    const int grid = grid_for(in.n, TRACE_THREADS, 2);
+    const int grid = bt_grid_for(in.n, TRACE_THREADS, 2);
     kern<<<grid, TRACE_THREADS, blob_bytes, stream>>>(d_blob, blob_bytes, in, out, ss, nsnaps, niter);
-    return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------
-// Split at one surface (src/batoid.cpp:509-674): the refracted ray replaces
-// the input ray, the reflected ray goes to `sp` (which holds a copy of the
-// input on entry); fluxes take the coating's transmit / reflect factors.
-// Stage 0 of the program: the surface, its transform, the outgoing medium
-// and the coating factors.
-// ---------------------------------------------------------------------------
-
-__global__ void __launch_bounds__(TRACE_THREADS)
-k_rsplit(const unsigned char* __restrict__ gblob, int blob_bytes, RV rv, RV sp, int niter) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bar;
-    if (!bt_stage_blob(smem, gblob, blob_bytes, &bar)) return;
-    const Prog P = prog_from_blob(smem);
-    const bt_stage& st = P.stages[0];
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < rv.n; i += stride) {
-        if (rv.fail[i]) continue;
-        const double dx = rv.x[i] - st.dr[0], dy = rv.y[i] - st.dr[1], dz = rv.z[i] - st.dr[2];
-        double x = dx * st.drot[0] + dy * st.drot[3] + dz * st.drot[6];
-        double y = dx * st.drot[1] + dy * st.drot[4] + dz * st.drot[7];
-        double z = dx * st.drot[2] + dy * st.drot[5] + dz * st.drot[8];
-        const double vx = rv.vx[i] * st.drot[0] + rv.vy[i] * st.drot[3] + rv.vz[i] * st.drot[6];
-        const double vy = rv.vx[i] * st.drot[1] + rv.vy[i] * st.drot[4] + rv.vz[i] * st.drot[7];
-        const double vz = rv.vx[i] * st.drot[2] + rv.vy[i] * st.drot[5] + rv.vz[i] * st.drot[8];
-        double dt = 0.0;
-        if (!bt_surf_tti_fast(P, st.surf, x, y, z, vx, vy, vz, dt, niter)) {
-            rv.vig[i] = 1;
-            rv.fail[i] = 1;
-            sp.vig[i] = 1;
-            sp.fail[i] = 1;
-            continue;
-        }
-        x += vx * dt;
-        y += vy * dt;
-        z += vz * dt;
-        const double t = rv.t[i] + dt;
-        const double n1 = 1.0 / sqrt(vx * vx + vy * vy + vz * vz);
-        const double nvx = vx * n1, nvy = vy * n1, nvz = vz * n1;
-        double nx, ny, nz;
-        bt_normal_precise(P, st.surf, x, y, &nx, &ny, &nz);
-        double alpha = nvx * nx + nvy * ny + nvz * nz;
-        if (alpha > 0.) {
-            nx = -nx; ny = -ny; nz = -nz;
-            alpha = -alpha;
-        }
-        const double w = rv.w[i];
-        const double f = rv.f[i];
-        // reflection
-        sp.x[i] = x;
-        sp.y[i] = y;
-        sp.z[i] = z;
-        sp.vx[i] = vx - 2 * alpha * nx / n1;
-        sp.vy[i] = vy - 2 * alpha * ny / n1;
-        sp.vz[i] = vz - 2 * alpha * nz / n1;
-        sp.t[i] = t;
-        sp.w[i] = w;
-        sp.f[i] = f * st.coat_r;
-        sp.vig[i] = rv.vig[i];
-        sp.fail[i] = 0;
-        // refraction
-        const double n2 = bt_getN(P, st.medium, w);
-        const double eta = n1 / n2;
-        const double sinsqr = eta * eta * (1 - alpha * alpha);
-        rv.x[i] = x;
-        rv.y[i] = y;
-        rv.z[i] = z;
-        rv.t[i] = t;
-        if (sinsqr > 1.0) {
-            rv.vx[i] = NAN;
-            rv.vy[i] = NAN;
-            rv.vz[i] = NAN;
-            rv.fail[i] = 1;
-            rv.vig[i] = 1;
-        } else {
-            const double nfactor = eta * alpha + sqrt(1 - sinsqr);
-            rv.vx[i] = (eta * nvx - nfactor * nx) / n2;
-            rv.vy[i] = (eta * nvy - nfactor * ny) / n2;
-            rv.vz[i] = (eta * nvz - nfactor * nz) / n2;
-        }
-        rv.f[i] = f * st.coat_t;
-    }
-}
-
-cudaError_t bt_launch_rsplit(const unsigned char* d_blob, int blob_bytes, const RV& rv, const RV& sp, int niter,
-                             cudaStream_t stream) {
-    if (rv.n <= 0) return cudaSuccess;
-    if (blob_bytes > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_rsplit, cudaFuncAttributeMaxDynamicSharedMemorySize, blob_bytes);
-        if (e != cudaSuccess) return e;
-    }
-    k_rsplit<<<grid_for(rv.n, TRACE_THREADS, 16), TRACE_THREADS, blob_bytes, stream>>>(d_blob, blob_bytes, rv, sp,
-                                                                                       niter);
     return cudaGetLastError();
 }
 
@@ -277,7 +175,7 @@ cudaError_t bt_launch_surface_eval(const unsigned char* d_blob, int blob_bytes, 
         cudaError_t e = cudaFuncSetAttribute(k_surface_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, blob_bytes);
         if (e != cudaSuccess) return e;
     }
-    k_surface_eval<<<grid_for(n, 256, 8), 256, blob_bytes, stream>>>(d_blob, blob_bytes, x, y, sag, normal, n);
+    k_surface_eval<<<bt_grid_for(n, 256, 8), 256, blob_bytes, stream>>>(d_blob, blob_bytes, x, y, sag, normal, n);
     return cudaGetLastError();
 }
 
@@ -295,7 +193,7 @@ __global__ void k_getN(const unsigned char* __restrict__ gblob, int blob_bytes, 
 cudaError_t bt_launch_getN(const unsigned char* d_blob, int blob_bytes, const double* w, double* out,
                            long long n, cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
-    k_getN<<<grid_for(n, 256, 8), 256, blob_bytes, stream>>>(d_blob, blob_bytes, w, out, n);
+    k_getN<<<bt_grid_for(n, 256, 8), 256, blob_bytes, stream>>>(d_blob, blob_bytes, w, out, n);
     return cudaGetLastError();
 }
 
@@ -322,7 +220,7 @@ cudaError_t bt_launch_obsc(const unsigned char* d_blob, int blob_bytes, const do
                            uint8_t* out, const RV* rv, long long n, cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
     RV dummy = {};
-    k_obsc<<<grid_for(n, 256, 8), 256, blob_bytes, stream>>>(d_blob, blob_bytes, x, y, out, rv ? *rv : dummy,
+    k_obsc<<<bt_grid_for(n, 256, 8), 256, blob_bytes, stream>>>(d_blob, blob_bytes, x, y, out, rv ? *rv : dummy,
                                                              rv ? 1 : 0, n);
     return cudaGetLastError();
 }
