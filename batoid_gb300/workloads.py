@@ -80,12 +80,21 @@ def _reconic(R, k_design, k_used):
     return list((_conic_series(R, k_design) - _conic_series(R, k_used))[1:])
 
 
-def _mirror_terms(rng, design):
+def _mirror_terms(rng, design, first_seeded):
     """Asphere coefficients r^4..r^20: the design's leading terms plus seeded
-    terms |a| < 1e-18 on r^6..r^20."""
+    terms |a| < 1e-18 on r^6..r^20.  The terms from r^(2 first_seeded + 2) up
+    are drawn first (in the order the earlier versions of this workload drew
+    them, so those coefficients are unchanged), then the ones below."""
     c = np.zeros(9)
     c[:len(design)] = design
-    c[1:] += rng.uniform(-1e-18, 1e-18, 8)
+    c[first_seeded:] += rng.uniform(-1e-18, 1e-18, 9 - first_seeded)
+    return c
+
+
+def _low_terms(rng, c, first_seeded):
+    """The seeded terms on r^6 .. r^(2 first_seeded) (index 1 .. first_seeded-1)."""
+    c = np.array(c)
+    c[1:first_seeded] += rng.uniform(-1e-18, 1e-18, first_seeded - 1)
     return list(c)
 
 
@@ -104,8 +113,11 @@ def tma_optic(bt, zernike_factory=None, seed=20231):
     silica = bt.SellmeierMedium(*SILICA)
     vac = bt.ConstMedium(1.0)
     zfac = zernike_factory or (lambda c, ro, ri: bt.Zernike(c, R_outer=ro, R_inner=ri))
-    m1_surf = bt.Sum(bt.Asphere(19.835, -1.215, _mirror_terms(rng, [0.0, -1.381e-9])),
-                     zfac(tma_zernike_coefs(seed), 4.18, 2.558))
+    c1 = _mirror_terms(rng, [0.0, -1.381e-9], 2)
+    c2 = _mirror_terms(rng, [0.0, 1.274e-5, 9.68e-7], 3)
+    c3 = _mirror_terms(rng, np.add(_reconic(8.3445, 0.155, 0.1), [0.0, 4.5e-7, 8.15e-9, 0, 0, 0, 0, 0, 0]), 3)
+    c1, c2, c3 = _low_terms(rng, c1, 2), _low_terms(rng, c2, 3), _low_terms(rng, c3, 3)
+    m1_surf = bt.Sum(bt.Asphere(19.835, -1.215, c1), zfac(tma_zernike_coefs(seed), 4.18, 2.558))
     z0 = np.zeros(3)
 
     def cs(z):
@@ -114,11 +126,10 @@ def tma_optic(bt, zernike_factory=None, seed=20231):
     items = [
         bt.Mirror(m1_surf, obscuration=bt.ObscNegation(bt.ObscAnnulus(2.558, 4.18)), name="M1", coordSys=cs(0.0),
                   inMedium=vac, outMedium=vac),
-        bt.Mirror(bt.Asphere(6.788, -0.222, _mirror_terms(rng, [0.0, 1.274e-5, 9.68e-7])),
+        bt.Mirror(bt.Asphere(6.788, -0.222, c2),
                   obscuration=bt.ObscNegation(bt.ObscAnnulus(0.9, 1.71)), name="M2", coordSys=cs(6.1562006),
                   inMedium=vac, outMedium=vac),
-        bt.Mirror(bt.Asphere(8.3445, 0.1, _mirror_terms(
-            rng, np.add(_reconic(8.3445, 0.155, 0.1), [0.0, 4.5e-7, 8.15e-9, 0, 0, 0, 0, 0, 0]))),
+        bt.Mirror(bt.Asphere(8.3445, 0.1, c3),
                   obscuration=bt.ObscNegation(bt.ObscAnnulus(0.55, 2.508)), name="M3", coordSys=cs(-0.2338),
                   inMedium=vac, outMedium=vac),
     ]
