@@ -798,6 +798,10 @@ def run_gpu(args):
                          "traffic": (counters["dram_bytes_per_ray"] * n if counters else None),
                          "peak_source": "DFMA loop measured in this run (bt_measure_fp64_peak)",
                          "executed_flops_per_ray": exec_fpr,
+                         "fp64_pipe": ({"slots_per_ray": counters["fp64_pipe_thread_inst_per_ray"],
+                                        "frac_of_dfma_loop": counters["fp64_pipe_thread_inst_per_ray"] * n
+                                        / (ms_per_step * 1e-3) / (fpeak.value * 1e12 / 2)}
+                                       if counters and fpeak.value else None),
                          "counters": counters,
                          "fp64_pipe_busy": (counters or {}).get("fp64_pipe_busy_pct"),
                          "reference_flops": {"flops_per_ray": ref_flops_per_ray, "tflops": ref_tflops,
