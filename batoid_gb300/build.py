@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libbatoid_gb300.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["capi.cu", "trace.cu", "split.cu", "rayvec.cu", "huygens.cu", "fit.cu", "batch.cu", "mlp.cu"]
+SOURCES = ["capi.cu", "trace.cu", "trace_ff.cu", "split.cu", "rayvec.cu", "huygens.cu", "fit.cu", "batch.cu", "mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
 

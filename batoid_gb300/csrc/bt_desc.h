@@ -59,8 +59,16 @@ typedef struct bt_surf {
     int32_t off;
     double p[12];
     const double* tab;
-    double pad_;
+    int32_t ffc;   // pool index of the float-float constants (see below), -1 if none
+    int32_t pad_;
 } bt_surf;  // 128 bytes
+
+// Float-float constants (one (hi, lo) float pair per double slot of the
+// pool, at index ffc) used by the trace kernel's float-float path:
+//  SPHERE:     R, R^2, 1/R, 1/R^2
+//  PARABOLOID: R, 1/R, 1/(2R)
+//  QUADRIC/ASPHERE: R, 1/(1+k), R/(1+k), R^2/(1+k)^2, (1+k)/R^2, 1/R
+//  POLY:       xorigin, yorigin
 
 enum bt_medium_kind {
     BT_M_CONST = 0,
@@ -70,7 +78,8 @@ enum bt_medium_kind {
     BT_M_AIR = 4
 };
 
-// CONST: p0=n.  TABLE: n entries, args at pool[off], vals at pool[off+n].
+// CONST: p0=n p1=1/n p2=(n as a float-float pair) p3=(1/n as a pair).
+// TABLE: n entries, args at pool[off], vals at pool[off+n].
 // SELLMEIER: B1 B2 B3 C1 C2 C3.  SUMITA: A0..A5.
 // AIR: p0=P(mmHg) p1=T(C) p2=W(mmHg)
 typedef struct bt_medium {

@@ -32,6 +32,11 @@ struct SnapSet {
 // Read and cleared by bt_check_device_status().
 cudaError_t bt_read_device_status(int* status, cudaStream_t stream);
 cudaError_t bt_read_split_device_status(int* status, cudaStream_t stream);
+cudaError_t bt_read_trace_ff_device_status(int* status, cudaStream_t stream);
+
+// trace_ff.cu: the float-float form of the fused trace
+cudaError_t bt_launch_trace_ff(const unsigned char* d_blob, int blob_bytes, const RV& in, const RV& out,
+                               const SnapSet* snaps, int nsnaps, int niter, cudaStream_t stream);
 
 // trace.cu
 cudaError_t bt_launch_trace(const unsigned char* d_blob, int blob_bytes, const RV& in, const RV& out,

@@ -1,0 +1,677 @@
+// Float-float path of the fused trace.
+//
+// The fused trace is bound by the FP64 pipe: on GB300 each FP64-pipe
+// instruction (DFMA, DADD, DMUL, compares, double<->float conversions)
+// occupies the pipe for the same time, and a stage of the FP64 form costs
+// 60-450 of them per ray.  The FP32 pipe issues ~64 lanes for each FP64
+// lane.  This path keeps each ray in float-float (pairs of floats, ~48
+// significant bits) between stages and evaluates the geometry there, and
+// keeps FP64 where the result's stability needs it:
+//  * the Newton intersection solve of aspheres, polynomial surfaces and
+//    sums: iterated in float-float to ~1e-13 m, then its residual
+//    sag(x + v dt) - (z + vz dt) is evaluated in FP64 at the FP64 point and
+//    the last correction applied in FP64 (src/surface.cpp:22-49: success is
+//    |residual| < 1e-12 at the final point);
+//  * the optical path: t accumulates in FP64.
+// Analytic intersections (plane, sphere, paraboloid, quadric), normals,
+// reflection, refraction, the media and the annulus / circle obscuration
+// tests run in float-float; a circle test whose h^2 - r^2 is within 1e-13
+// relative falls back to the reference's FP64 hypot.  Results agree with the
+// reference within its parity tolerances (positions 1e-12 m, path 1e-11 m).
+//
+// Stages whose surface kind has no float-float form here (Tilted, Bicubic,
+// the batched kernel's modal tables, Sum over those) and obscurations other
+// than circles and annuli run the FP64 form on a double copy of the ray.
+#pragma once
+#include "bt_trace_core.cuh"
+
+struct RayF {
+    ff x, y, z, vx, vy, vz;
+    double t, w, f;
+    bool vig, fail;
+};
+
+// Index of the medium whose index is cached and the cached (n, 1/n).
+struct MediumCacheF {
+    int idx;
+    ff n, inv_n;
+};
+
+__device__ __forceinline__ RayF rayf_from(const RayState& r) {
+    RayF o;
+    o.x = d_to_ff(r.x); o.y = d_to_ff(r.y); o.z = d_to_ff(r.z);
+    o.vx = d_to_ff(r.vx); o.vy = d_to_ff(r.vy); o.vz = d_to_ff(r.vz);
+    o.t = r.t; o.w = r.w; o.f = r.f;
+    o.vig = r.vig; o.fail = r.fail;
+    return o;
+}
+
+__device__ __forceinline__ RayState rayf_to(const RayF& r) {
+    RayState o;
+    o.x = ff_to_d(r.x); o.y = ff_to_d(r.y); o.z = ff_to_d(r.z);
+    o.vx = ff_to_d(r.vx); o.vy = ff_to_d(r.vy); o.vz = ff_to_d(r.vz);
+    o.t = r.t; o.w = r.w; o.f = r.f;
+    o.vig = r.vig; o.fail = r.fail;
+    return o;
+}
+
+// |a| < c for finite c > 0 on the integer pipe (false for NaN, as the
+// floating-point comparison).
+__device__ __forceinline__ bool d_abs_lt(double a, double c) {
+    const unsigned long long ua = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
+    return ua < (unsigned long long)__double_as_longlong(c);
+}
+
+__device__ __forceinline__ ff ff_one() { return ff{1.f, 0.f}; }
+
+// ---------------------------------------------------------------------------
+// Which surfaces have a float-float form
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ bool ffs_leaf_ok(const bt_surf& s) {
+    switch (s.kind) {
+    case BT_S_PLANE:
+        return true;
+    case BT_S_SPHERE:
+    case BT_S_PARABOLOID:
+    case BT_S_QUADRIC:
+    case BT_S_ASPHERE:
+        return s.ffc >= 0 && s.p[0] != 0.0;
+    case BT_S_POLY:
+        return s.ffc >= 0;
+    default:
+        return false;
+    }
+}
+
+__device__ __forceinline__ bool ffs_ok(const Prog& P, int si) {
+    const bt_surf& s = P.surfs[si];
+    if (s.kind != BT_S_SUM) return ffs_leaf_ok(s);
+    for (int c = 0; c < s.n; c++)
+        if (!ffs_leaf_ok(P.surfs[s.m + c])) return false;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Sags (float-float value as conic part + polynomial part, FP32 slope)
+// ---------------------------------------------------------------------------
+
+// r^2 = x^2 + y^2
+__device__ __forceinline__ ff ff_r2(ff x, ff y) { return ff_add(ff_sqr(x), ff_sqr(y)); }
+
+// Conic sag of a QUADRIC / ASPHERE record: (1 - q) R/(1+k) or r^2/(R (1+q)),
+// q = sqrt(1 - r^2 (1+k)/R^2), as the FP64 form (bt_conic).
+__device__ __forceinline__ ff ffs_conic(const bt_surf& s, const double* C, ff r2, ff* w_out) {
+    const ff w = ff_sub(ff_one(), ff_mul(r2, ff_slot(C + 4)));
+    *w_out = w;
+    const ff q = ff_sqrt(w);
+    if (s.p[10] != 0.0) return ff_mul(ff_sub(ff_one(), q), ff_slot(C + 2));
+    return ff_div(r2, ff_mul(ff_slot(C + 0), ff_add(ff_one(), q)));
+}
+
+// Leaf sag at (x, y): *zc the conic part (recomputed in FP64 by
+// ffs_conic64), *zp the polynomial part, (ux, uy) the FP32 slope
+// (-dz/dx, -dz/dy) for the Newton derivative.
+__device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* pool, ff x, ff y, ff* zc, ff* zp,
+                                              float* ux, float* uy) {
+    const double* C = pool + s.ffc;
+    *zp = ff{0.f, 0.f};
+    switch (s.kind) {
+    case BT_S_SPHERE: {
+        const ff r2 = ff_r2(x, y);
+        const ff w = ff_sub(ff_one(), ff_mul(r2, ff_slot(C + 3)));
+        *zc = ff_mul(ff_slot(C + 0), ff_sub(ff_one(), ff_sqrt(w)));
+        const float k = rsqrtf(w.hi) * ff_slot(C + 2).hi;
+        *ux = -x.hi * k;
+        *uy = -y.hi * k;
+        return;
+    }
+    case BT_S_PARABOLOID: {
+        *zc = ff_mul(ff_r2(x, y), ff_slot(C + 2));
+        const float k = ff_slot(C + 1).hi;
+        *ux = -x.hi * k;
+        *uy = -y.hi * k;
+        return;
+    }
+    case BT_S_QUADRIC:
+    case BT_S_ASPHERE: {
+        const ff r2 = ff_r2(x, y);
+        ff w;
+        *zc = ffs_conic(s, C, r2, &w);
+        float kf = rsqrtf(w.hi) * ff_slot(C + 5).hi;
+        if (s.kind == BT_S_ASPHERE && s.n > 0) {
+            const ff* c = ff_ptr(pool, s.off + 2 * s.n);
+            const ff* dc = c + s.n;
+            *zp = ff_mul(ff_horner(r2, c, s.n), r2);
+            float da = 0.f;
+            for (int i = s.n - 1; i >= 0; i--) da = fmaf(da, r2.hi, dc[i].hi);
+            kf += da;
+        }
+        *ux = -x.hi * kf;
+        *uy = -y.hi * kf;
+        return;
+    }
+    case BT_S_POLY: {
+        const ff xx = ff_sub(x, ff_slot(C + 0)), yy = ff_sub(y, ff_slot(C + 1));
+        const int nx = s.n, ny = s.m;
+        const int g = (nx - 1) * (ny - 1);
+        const ff* c = ff_ptr(pool, s.off + nx * ny + 2 * g);
+        *zc = ff{0.f, 0.f};
+        *zp = ff_horner2d(xx, yy, c, nx, ny);
+        *ux = -f_horner2d(xx.hi, yy.hi, c + nx * ny, nx - 1, ny - 1);
+        *uy = -f_horner2d(xx.hi, yy.hi, c + nx * ny + g, nx - 1, ny - 1);
+        return;
+    }
+    default:  // plane
+        *zc = ff{0.f, 0.f};
+        *ux = 0.f;
+        *uy = 0.f;
+        return;
+    }
+}
+
+__device__ __forceinline__ void ffs_eval(const Prog& P, int si, ff x, ff y, ff* zc, ff* zp, float* ux, float* uy) {
+    const bt_surf& s = P.surfs[si];
+    if (s.kind != BT_S_SUM) {
+        ffs_leaf_eval(s, P.pool, x, y, zc, zp, ux, uy);
+        return;
+    }
+    ff c_acc{0.f, 0.f}, p_acc{0.f, 0.f};
+    float gx = 0.f, gy = 0.f;
+    for (int c = 0; c < s.n; c++) {
+        ff cz, pz;
+        float cx, cy;
+        ffs_leaf_eval(P.surfs[s.m + c], P.pool, x, y, &cz, &pz, &cx, &cy);
+        c_acc = ff_add(c_acc, cz);
+        p_acc = ff_add(p_acc, pz);
+        gx += cx;
+        gy += cy;
+    }
+    *zc = c_acc;
+    *zp = p_acc;
+    *ux = gx;
+    *uy = gy;
+}
+
+// FP64 conic part of the sag (the reference's expressions, src/sphere.cpp,
+// src/paraboloid.cpp, src/quadric.cpp) at an FP64 point.
+__device__ __forceinline__ double ffs_conic64_leaf(const bt_surf& s, double x, double y) {
+    double z, k;
+    switch (s.kind) {
+    case BT_S_SPHERE:
+        bt_sphere_conic(s, x * x + y * y, &z, &k);
+        return z;
+    case BT_S_PARABOLOID:
+        return (x * x + y * y) * s.p[2];
+    case BT_S_QUADRIC:
+    case BT_S_ASPHERE:
+        bt_conic(s, x * x + y * y, &z, &k);
+        return z;
+    default:
+        return 0.0;
+    }
+}
+
+__device__ __forceinline__ double ffs_conic64(const Prog& P, int si, double x, double y) {
+    const bt_surf& s = P.surfs[si];
+    if (s.kind != BT_S_SUM) return ffs_conic64_leaf(s, x, y);
+    double z = 0.0;
+    for (int c = 0; c < s.n; c++) z += ffs_conic64_leaf(P.surfs[s.m + c], x, y);
+    return z;
+}
+
+// ---------------------------------------------------------------------------
+// Intersections
+// ---------------------------------------------------------------------------
+
+// One root of a t^2 + b t + c = 0 as bt_one_root (the reference's dt1 / dt2
+// pair, src/sphere.cpp:51-58): `plus` selects (-b + sqrt(D)) / 2a.
+__device__ __forceinline__ bool ff_one_root(ff a, ff b, ff c, bool plus, ff* t) {
+    const ff disc = ff_sub(ff_sqr(b), ff_mul_f(ff_mul(a, c), 4.f));
+    if (disc.hi < 0.f) return false;
+    const ff s = ff_sqrt(disc);
+    const ff mb = ff_neg(b);
+    if (b.hi > 0.f) *t = plus ? ff_div(ff_mul_f(c, 2.f), ff_sub(mb, s)) : ff_div(ff_sub(mb, s), ff_mul_f(a, 2.f));
+    else *t = plus ? ff_div(ff_add(mb, s), ff_mul_f(a, 2.f)) : ff_div(ff_mul_f(c, 2.f), ff_add(mb, s));
+    return true;
+}
+
+// Conic root with the smaller |z| (src/quadric.cpp:41-71).
+__device__ __forceinline__ bool ff_quadric_root(const double* C, ff x, ff y, ff z, ff vx, ff vy, ff vz, ff* dt) {
+    const ff icp1 = ff_slot(C + 1);
+    const ff z0 = ff_sub(z, ff_slot(C + 2));
+    const ff vrr0 = ff_add(ff_mul(vx, x), ff_mul(vy, y));
+    const ff a = ff_add(ff_sqr(vz), ff_mul(ff_r2(vx, vy), icp1));
+    const ff b = ff_mul_f(ff_add(ff_mul(vz, z0), ff_mul(vrr0, icp1)), 2.f);
+    const ff c = ff_add(ff_sub(ff_sqr(z0), ff_slot(C + 3)), ff_mul(ff_r2(x, y), icp1));
+    const ff disc = ff_sub(ff_sqr(b), ff_mul_f(ff_mul(a, c), 4.f));
+    if (disc.hi < 0.f) return false;
+    const ff s = ff_sqrt(disc);
+    const ff mb = ff_neg(b);
+    const ff r1 = (b.hi > 0.f) ? ff_div(ff_sub(mb, s), ff_mul_f(a, 2.f)) : ff_div(ff_mul_f(c, 2.f), ff_add(mb, s));
+    const ff r2 = ff_div(c, ff_mul(a, r1));
+    const ff z1 = ff_mad(vz, r1, z), z2 = ff_mad(vz, r2, z);
+    *dt = ff_lt(ff_abs(z1), ff_abs(z2)) ? r1 : r2;
+    return true;
+}
+
+// Analytic time to intersect of PLANE / SPHERE / PARABOLOID / QUADRIC.
+__device__ __forceinline__ bool ff_analytic(const bt_surf& s, const double* pool, ff x, ff y, ff z, ff vx, ff vy,
+                                            ff vz, ff* dt) {
+    const double* C = pool + s.ffc;
+    switch (s.kind) {
+    case BT_S_PLANE:
+        // src/plane.cpp:23-30
+        if (vz.hi == 0.f) return false;
+        *dt = ff_div(ff_neg(z), vz);
+        return true;
+    case BT_S_SPHERE: {
+        // src/sphere.cpp:36-67
+        const ff R = ff_slot(C + 0);
+        const ff z0 = ff_sub(z, R);
+        const ff a = ff_add(ff_sqr(vz), ff_r2(vx, vy));
+        const ff b = ff_mul_f(ff_add(ff_mul(vz, z0), ff_add(ff_mul(vx, x), ff_mul(vy, y))), 2.f);
+        const ff c = ff_add(ff_sub(ff_sqr(z0), ff_slot(C + 1)), ff_r2(x, y));
+        const bool want_max = (vz.hi * R.hi < 0.f);
+        return ff_one_root(a, b, c, want_max == (a.hi > 0.f), dt);
+    }
+    case BT_S_PARABOLOID: {
+        // src/paraboloid.cpp:38-71
+        const ff a = ff_mul(ff_r2(vx, vy), ff_slot(C + 2));
+        const ff b = ff_sub(ff_mul(ff_add(ff_mul(x, vx), ff_mul(y, vy)), ff_slot(C + 1)), vz);
+        const ff c = ff_sub(ff_mul(ff_r2(x, y), ff_slot(C + 2)), z);
+        if (a.hi == 0.f) {
+            *dt = ff_div(ff_neg(c), b);
+            return true;
+        }
+        const bool want_max = (vz.hi * ff_slot(C + 0).hi < 0.f);
+        return ff_one_root(a, b, c, want_max == (a.hi > 0.f), dt);
+    }
+    default:  // QUADRIC
+        return ff_quadric_root(C, x, y, z, vx, vy, vz, dt);
+    }
+}
+
+// Newton's tangent-plane iteration in float-float from dt, at most niter
+// corrections, stopping once a correction is below 1e-12 m.  Returns whether
+// it stopped that way; *zp and *inv_den hold the polynomial part of the sag
+// and 1/F' at the last evaluation (the point before the last correction).
+__device__ __forceinline__ bool ff_newton_iter(const Prog& P, int si, ff x, ff y, ff z, ff vx, ff vy, ff vz, ff* dt,
+                                               int niter, ff* zp, float* inv_den) {
+    const float fvx = vx.hi, fvy = vy.hi, fvz = vz.hi;
+    for (int it = 0; it < niter; it++) {
+        const ff px = ff_mad(vx, *dt, x), py = ff_mad(vy, *dt, y), pz = ff_mad(vz, *dt, z);
+        ff zc;
+        float ux, uy;
+        ffs_eval(P, si, px, py, &zc, zp, &ux, &uy);
+        const ff res = ff_sub(ff_add(zc, *zp), pz);
+        *inv_den = 1.f / fmaf(ux, fvx, fmaf(uy, fvy, fvz));
+        const ff ddt = ff_mul_f(res, *inv_den);
+        *dt = ff_add(*dt, ddt);
+        if (fabsf(ddt.hi) < 1e-12f) return true;
+    }
+    return false;
+}
+
+// Residual of surface si at dt in float-float (for a first child's success
+// test, as the reference's |sag - z| < 1e-12 at its final point).
+__device__ __forceinline__ bool ff_residual_ok(const Prog& P, int si, ff x, ff y, ff z, ff vx, ff vy, ff vz, ff dt) {
+    const ff px = ff_mad(vx, dt, x), py = ff_mad(vy, dt, y), pz = ff_mad(vz, dt, z);
+    ff zc, zp;
+    float ux, uy;
+    ffs_eval(P, si, px, py, &zc, &zp, &ux, &uy);
+    const ff res = ff_sub(ff_add(zc, zp), pz);
+    return fabsf(res.hi) < 1e-12f;
+}
+
+// Iterative intersection of an ASPHERE / POLY / SUM: start (the conic root,
+// dt = 0, or the first child's own solve: src/asphere.cpp:76-85,
+// src/sum.cpp:47-56), float-float Newton, then the FP64 residual at the FP64
+// point and the final correction in FP64.  On success the FP64 dt and the
+// FP64 intersection point are returned.
+__device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, ff x, ff y, ff z, ff vx, ff vy, ff vz, int niter,
+                                           double* dt_out, double* rx, double* ry, double* rz) {
+    const bt_surf& s = P.surfs[si];
+    ff dt{0.f, 0.f};
+    ff zp;
+    float inv_den = 0.f;
+    if (s.kind == BT_S_SUM) {
+        const int c0 = s.m;
+        const bt_surf& first = P.surfs[c0];
+        if (first.kind == BT_S_ASPHERE || first.kind == BT_S_POLY) {
+            if (first.kind == BT_S_ASPHERE && !ff_quadric_root(P.pool + first.ffc, x, y, z, vx, vy, vz, &dt))
+                return false;
+            if (!ff_newton_iter(P, c0, x, y, z, vx, vy, vz, &dt, niter, &zp, &inv_den) &&
+                !ff_residual_ok(P, c0, x, y, z, vx, vy, vz, dt))
+                return false;
+        } else if (!ff_analytic(first, P.pool, x, y, z, vx, vy, vz, &dt)) {
+            return false;
+        }
+    } else if (s.kind == BT_S_ASPHERE) {
+        if (!ff_quadric_root(P.pool + s.ffc, x, y, z, vx, vy, vz, &dt)) return false;
+    }
+    const bool conv = ff_newton_iter(P, si, x, y, z, vx, vy, vz, &dt, niter, &zp, &inv_den);
+    // FP64 residual at the FP64 point x + v dt
+    const double xd = ff_to_d(x), yd = ff_to_d(y), zd = ff_to_d(z);
+    const double vxd = ff_to_d(vx), vyd = ff_to_d(vy), vzd = ff_to_d(vz);
+    double dtd = ff_to_d(dt);
+    if (conv) {
+        const double px = fma(vxd, dtd, xd), py = fma(vyd, dtd, yd), pz = fma(vzd, dtd, zd);
+        // the polynomial part was evaluated before the last correction
+        // (< 1e-12 m earlier along the ray; its slope is small): the error is
+        // far below the FP64 conic part's rounding
+        const double res = ffs_conic64(P, si, px, py) + ff_to_d(zp) - pz;
+        if (d_abs_lt(res, 1e-12)) {
+            // the residual after this correction is ~1e-7 of |res|
+            dtd += res * f2d_bits(inv_den);
+            *dt_out = dtd;
+            *rx = fma(vxd, dtd, xd);
+            *ry = fma(vyd, dtd, yd);
+            *rz = fma(vzd, dtd, zd);
+            return true;
+        }
+    }
+    // not converged in float-float: the FP64 mixed-precision Newton from here
+    const bool ok = bt_newton_mixed(P, si, xd, yd, zd, vxd, vyd, vzd, dtd, niter);
+    *dt_out = dtd;
+    *rx = fma(vxd, dtd, xd);
+    *ry = fma(vyd, dtd, yd);
+    *rz = fma(vzd, dtd, zd);
+    return ok;
+}
+
+// ---------------------------------------------------------------------------
+// Normals, reflection, refraction
+// ---------------------------------------------------------------------------
+
+// Slope (ux, uy) = (nx/nz, ny/nz) of a leaf at (x, y), float-float.
+__device__ __forceinline__ void ffs_leaf_slope(const bt_surf& s, const double* pool, ff x, ff y, ff* ux, ff* uy) {
+    const double* C = pool + s.ffc;
+    switch (s.kind) {
+    case BT_S_SPHERE: {
+        const ff w = ff_sub(ff_one(), ff_mul(ff_r2(x, y), ff_slot(C + 3)));
+        const ff k = ff_mul(ff_slot(C + 2), ff_rsqrt(w));
+        *ux = ff_neg(ff_mul(x, k));
+        *uy = ff_neg(ff_mul(y, k));
+        return;
+    }
+    case BT_S_PARABOLOID: {
+        const ff k = ff_slot(C + 1);
+        *ux = ff_neg(ff_mul(x, k));
+        *uy = ff_neg(ff_mul(y, k));
+        return;
+    }
+    case BT_S_QUADRIC:
+    case BT_S_ASPHERE: {
+        const ff r2 = ff_r2(x, y);
+        const ff w = ff_sub(ff_one(), ff_mul(r2, ff_slot(C + 4)));
+        ff k = ff_mul(ff_slot(C + 5), ff_rsqrt(w));
+        if (s.kind == BT_S_ASPHERE && s.n > 0) k = ff_add(k, ff_horner(r2, ff_ptr(pool, s.off + 3 * s.n), s.n));
+        *ux = ff_neg(ff_mul(x, k));
+        *uy = ff_neg(ff_mul(y, k));
+        return;
+    }
+    case BT_S_POLY: {
+        const int nx = s.n, ny = s.m;
+        const int g = (nx - 1) * (ny - 1);
+        const ff* c = ff_ptr(pool, s.off + nx * ny + 2 * g);
+        const ff xx = ff_sub(x, ff_slot(C + 0)), yy = ff_sub(y, ff_slot(C + 1));
+        *ux = ff_neg(ff_horner2d(xx, yy, c + nx * ny, nx - 1, ny - 1));
+        *uy = ff_neg(ff_horner2d(xx, yy, c + nx * ny + g, nx - 1, ny - 1));
+        return;
+    }
+    default:
+        *ux = ff{0.f, 0.f};
+        *uy = ff{0.f, 0.f};
+        return;
+    }
+}
+
+// Unit normal at (x, y) with the reference's conventions (bt_normal_precise).
+__device__ __forceinline__ void ffs_normal(const Prog& P, int si, ff x, ff y, ff* nx, ff* ny, ff* nz) {
+    const bt_surf& s = P.surfs[si];
+    if (s.kind == BT_S_PLANE) {
+        *nx = ff{0.f, 0.f}; *ny = ff{0.f, 0.f}; *nz = ff_one();
+        return;
+    }
+    if (s.kind == BT_S_SPHERE) {
+        // (-x/R, -y/R, sqrt(1 - r^2/R^2))
+        const double* C = P.pool + s.ffc;
+        const ff iR = ff_slot(C + 2);
+        *nx = ff_neg(ff_mul(x, iR));
+        *ny = ff_neg(ff_mul(y, iR));
+        *nz = ff_sqrt(ff_sub(ff_one(), ff_mul(ff_r2(x, y), ff_slot(C + 3))));
+        return;
+    }
+    ff ux{0.f, 0.f}, uy{0.f, 0.f};
+    if (s.kind != BT_S_SUM) {
+        ffs_leaf_slope(s, P.pool, x, y, &ux, &uy);
+    } else {
+        for (int c = 0; c < s.n; c++) {
+            ff cx, cy;
+            ffs_leaf_slope(P.surfs[s.m + c], P.pool, x, y, &cx, &cy);
+            ux = ff_add(ux, cx);
+            uy = ff_add(uy, cy);
+        }
+    }
+    const ff k = ff_rsqrt(ff_add_f(ff_r2(ux, uy), 1.f));
+    *nx = ff_mul(ux, k);
+    *ny = ff_mul(uy, k);
+    *nz = k;
+}
+
+__device__ __forceinline__ ff ff_dot3(ff ax, ff ay, ff az, ff bx, ff by, ff bz) {
+    return ff_add(ff_add(ff_mul(ax, bx), ff_mul(ay, by)), ff_mul(az, bz));
+}
+
+// Refractive index and its reciprocal in float-float (src/medium.cpp).
+__device__ __forceinline__ void ff_medium(const Prog& P, int mi, double w, ff* n, ff* inv_n) {
+    const bt_medium& m = P.media[mi];
+    if (m.kind == BT_M_CONST) {
+        *n = ff_slot(&m.p[2]);
+        *inv_n = ff_slot(&m.p[3]);
+        return;
+    }
+    if (m.kind == BT_M_SELLMEIER) {
+        // src/medium.cpp:145-149: n^2 = 1 + sum B_i x / (x - C_i), x = (w / 1 um)^2
+        const ff wf = d_to_ff(w);
+        const ff x = ff_mul_f(ff_sqr(wf), 1e12f);
+        ff n2 = ff_one();
+        for (int i = 0; i < 3; i++) {
+            const ff B = d_to_ff(m.p[i]), Cc = d_to_ff(m.p[3 + i]);
+            n2 = ff_add(n2, ff_div(ff_mul(B, x), ff_sub(x, Cc)));
+        }
+        *n = ff_sqrt(n2);
+        *inv_n = ff_div(ff_one(), *n);
+        return;
+    }
+    const double nd = bt_getN(P, mi, w);
+    *n = d_to_ff(nd);
+    *inv_n = d_to_ff(1.0 / nd);
+}
+
+// ---------------------------------------------------------------------------
+// Obscurations: circles and annuli in float-float, the rest in FP64
+// ---------------------------------------------------------------------------
+
+// hypot(dx, dy) < r decided from h^2 - r^2 in float-float unless within
+// 1e-13 relative of r^2; then *undecided.
+__device__ __forceinline__ bool ff_radius_less(ff dx, ff dy, double r, bool* undecided) {
+    const ff rf = d_to_ff(r);
+    const ff r2 = ff_sqr(rf);
+    const ff d = ff_sub(ff_r2(dx, dy), r2);
+    const float thr = 1e-13f * r2.hi;
+    if (d.hi < -thr) return r > 0.0;
+    if (d.hi > thr) return false;
+    *undecided = true;
+    return false;
+}
+
+__device__ __forceinline__ bool ff_obsc_run(const Prog& P, int begin, int end, ff x, ff y) {
+    uint32_t stack = 0;
+    int sp = 0;
+    bool have_d = false;
+    double xd = 0.0, yd = 0.0;
+    for (int k = begin; k < end; k++) {
+        const bt_obsc& o = P.obsc[k];
+        bool v = false;
+        if (o.op == BT_O_CIRCLE || o.op == BT_O_ANNULUS) {
+            const int c = (o.op == BT_O_CIRCLE) ? 1 : 2;  // index of the centre x in p[]
+            const ff dx = ff_sub(x, d_to_ff(o.p[c])), dy = ff_sub(y, d_to_ff(o.p[c + 1]));
+            bool und = false;
+            if (o.op == BT_O_CIRCLE) {
+                v = ff_radius_less(dx, dy, o.p[0], &und);
+            } else {
+                const bool in_inner = ff_radius_less(dx, dy, o.p[0], &und);
+                const bool in_outer = ff_radius_less(dx, dy, o.p[1], &und);
+                v = !in_inner && in_outer;
+            }
+            if (und) {
+                if (!have_d) { xd = ff_to_d(x); yd = ff_to_d(y); have_d = true; }
+                v = bt_obsc_run(P, k, k + 1, xd, yd);
+            }
+        } else if (o.op == BT_O_NEGATION || o.op == BT_O_UNION || o.op == BT_O_INTERSECTION) {
+            if (o.op == BT_O_NEGATION) {
+                sp--;
+                v = !((stack >> sp) & 1u);
+            } else if (o.op == BT_O_UNION) {
+                bool acc = false;
+                for (int j = 0; j < o.n; j++) { sp--; acc |= (bool)((stack >> sp) & 1u); }
+                v = acc;
+            } else {
+                bool acc = true;
+                for (int j = 0; j < o.n; j++) { sp--; acc &= (bool)((stack >> sp) & 1u); }
+                v = acc;
+            }
+        } else {
+            if (!have_d) { xd = ff_to_d(x); yd = ff_to_d(y); have_d = true; }
+            v = bt_obsc_run(P, k, k + 1, xd, yd);
+        }
+        stack = (stack & ~(1u << sp)) | ((uint32_t)v << sp);
+        sp++;
+    }
+    return sp > 0 ? (bool)((stack >> (sp - 1)) & 1u) : false;
+}
+
+// ---------------------------------------------------------------------------
+// One stage (semantics of run_stage, src/batoid.cpp:175-506)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void ff_translate(const bt_stage& st, ff* x, ff* y, ff* z) {
+    if (st.dr[0] != 0.0) *x = ff_sub(*x, d_to_ff(st.dr[0]));
+    if (st.dr[1] != 0.0) *y = ff_sub(*y, d_to_ff(st.dr[1]));
+    if (st.dr[2] != 0.0) *z = ff_sub(*z, d_to_ff(st.dr[2]));
+}
+
+// x' = R^T (x - dr) with the column-major rotation of the stage.
+__device__ __forceinline__ void ff_rotate(const bt_stage& st, ff* x, ff* y, ff* z) {
+    const ff a = *x, b = *y, c = *z;
+    ff m[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) m[i] = d_to_ff(st.drot[i]);
+    *x = ff_add(ff_add(ff_mul(a, m[0]), ff_mul(b, m[3])), ff_mul(c, m[6]));
+    *y = ff_add(ff_add(ff_mul(a, m[1]), ff_mul(b, m[4])), ff_mul(c, m[7]));
+    *z = ff_add(ff_add(ff_mul(a, m[2]), ff_mul(b, m[5])), ff_mul(c, m[8]));
+}
+
+// A stage on the FP64 form, for the surface kinds without a float-float form.
+__device__ __noinline__ void ff_stage_fp64(const Prog& P, const bt_stage& st, RayF& r, int niter) {
+    RayState d = rayf_to(r);
+    int cm = -1;
+    double cn = 0.0, cin = 0.0;
+    run_stage<false>(P, st, d, niter, cm, cn, cin);
+    r = rayf_from(d);
+}
+
+__device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, RayF& r, int niter,
+                                             MediumCacheF& mc) {
+    if (st.kind == BT_ST_SCREEN || (st.kind != BT_ST_OBSCURE && !r.fail && !ffs_ok(P, st.surf))) {
+        ff_stage_fp64(P, st, r, niter);
+        return;
+    }
+    if (st.kind != BT_ST_OBSCURE && !r.fail) {
+        ff x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
+        if (st.identity != 1) {
+            ff_translate(st, &x, &y, &z);
+            if (st.identity == 0) {
+                ff_rotate(st, &x, &y, &z);
+                ff_rotate(st, &vx, &vy, &vz);
+            }
+        }
+        const bt_surf& s = P.surfs[st.surf];
+        bool ok;
+        ff nx_, ny_, nz_;
+        if (s.kind == BT_S_ASPHERE || s.kind == BT_S_POLY || s.kind == BT_S_SUM) {
+            double dtd, px, py, pz;
+            ok = ff_newton_tti(P, st.surf, x, y, z, vx, vy, vz, niter, &dtd, &px, &py, &pz);
+            if (ok) {
+                x = d_to_ff(px);
+                y = d_to_ff(py);
+                z = d_to_ff(pz);
+                r.t += dtd;
+            }
+        } else {
+            ff dt;
+            ok = ff_analytic(s, P.pool, x, y, z, vx, vy, vz, &dt);
+            if (ok) {
+                x = ff_mad(vx, dt, x);
+                y = ff_mad(vy, dt, y);
+                z = ff_mad(vz, dt, z);
+                r.t += ff_to_d(dt);
+            }
+        }
+        if (ok) {
+            if (st.kind == BT_ST_INTERSECT) {
+                if (st.coated) r.f *= st.coat_t;
+            } else {
+                ffs_normal(P, st.surf, x, y, &nx_, &ny_, &nz_);
+                if (st.kind == BT_ST_REFLECT) {
+                    // src/batoid.cpp:343-353
+                    const ff a2 = ff_mul_f(ff_dot3(vx, vy, vz, nx_, ny_, nz_), 2.f);
+                    vx = ff_sub(vx, ff_mul(a2, nx_));
+                    vy = ff_sub(vy, ff_mul(a2, ny_));
+                    vz = ff_sub(vz, ff_mul(a2, nz_));
+                    if (st.coated) r.f *= st.coat_r;
+                } else {
+                    // src/batoid.cpp:453-499
+                    const ff n1 = ff_rsqrt(ff_add(ff_sqr(vz), ff_r2(vx, vy)));
+                    const ff nvx = ff_mul(vx, n1), nvy = ff_mul(vy, n1), nvz = ff_mul(vz, n1);
+                    ff alpha = ff_dot3(nvx, nvy, nvz, nx_, ny_, nz_);
+                    if (alpha.hi > 0.f) {
+                        nx_ = ff_neg(nx_); ny_ = ff_neg(ny_); nz_ = ff_neg(nz_);
+                        alpha = ff_neg(alpha);
+                    }
+                    const int mi = st.medium;
+                    if (mi != mc.idx) {
+                        ff_medium(P, mi, r.w, &mc.n, &mc.inv_n);
+                        mc.idx = mi;
+                    }
+                    const ff eta = ff_mul(n1, mc.inv_n);
+                    const ff sinsqr = ff_mul(ff_sqr(eta), ff_sub(ff_one(), ff_sqr(alpha)));
+                    if (sinsqr.hi > 1.f || (sinsqr.hi == 1.f && sinsqr.lo > 0.f)) {
+                        const float qnan = __int_as_float(0x7fc00000);
+                        vx = ff{qnan, 0.f}; vy = ff{qnan, 0.f}; vz = ff{qnan, 0.f};
+                        r.fail = true;
+                        r.vig = true;
+                    } else {
+                        const ff cosr = ff_sqrt(ff_sub(ff_one(), sinsqr));
+                        const ff nfactor = ff_add(ff_mul(eta, alpha), cosr);
+                        vx = ff_mul(ff_sub(ff_mul(eta, nvx), ff_mul(nfactor, nx_)), mc.inv_n);
+                        vy = ff_mul(ff_sub(ff_mul(eta, nvy), ff_mul(nfactor, ny_)), mc.inv_n);
+                        vz = ff_mul(ff_sub(ff_mul(eta, nvz), ff_mul(nfactor, nz_)), mc.inv_n);
+                    }
+                    if (st.coated) r.f *= st.coat_t;
+                }
+            }
+            r.x = x; r.y = y; r.z = z;
+            r.vx = vx; r.vy = vy; r.vz = vz;
+        } else {
+            r.fail = true;
+            r.vig = true;
+        }
+    }
+    if (st.obsc_end > st.obsc_begin) {
+        // src/batoid.cpp:169-171: vignetted |= contains(x, y), for every ray
+        if (ff_obsc_run(P, st.obsc_begin, st.obsc_end, r.x, r.y)) r.vig = true;
+    }
+}

@@ -99,7 +99,29 @@ static bt_surf blank_surf(int kind) {
     bt_surf s;
     memset(&s, 0, sizeof(s));
     s.kind = kind;
+    s.ffc = -1;
     return s;
+}
+
+// A double's float-float split (hi, lo) stored in one double slot.
+static double ff_slot(double v) {
+    float pair[2];
+    pair[0] = (float)v;
+    pair[1] = (float)(v - (double)pair[0]);
+    double out;
+    memcpy(&out, pair, sizeof(out));
+    return out;
+}
+
+static void append_ff(std::vector<double>& pool, size_t begin, size_t n) {
+    for (size_t i = 0; i < n; i++) pool.push_back(ff_slot(pool[begin + i]));
+}
+
+// Appends the float-float constants of a record to its surface's pool and
+// points the record's ffc at them.
+static void push_ffc(bt_surface* s, bt_surf& r, std::initializer_list<double> vals) {
+    r.ffc = (int32_t)s->pool.size();
+    for (double v : vals) s->pool.push_back(ff_slot(v));
 }
 
 static void push_rec(bt_surface* s, const bt_surf& r, bt_table* t = nullptr) {
@@ -141,6 +163,7 @@ extern "C" int bt_sphere_create(double R, bt_surface** out) {
     r.p[1] = R * R;
     r.p[2] = 1. / R;
     r.p[3] = 1. / R / R;
+    push_ffc(s, r, {R, R * R, 1. / R, 1. / R / R});
     push_rec(s, r);
     return make_out(out, s);
 }
@@ -152,23 +175,11 @@ extern "C" int bt_paraboloid_create(double R, bt_surface** out) {
     r.p[0] = R;
     r.p[1] = 1. / R;
     r.p[2] = 1. / 2 / R;
+    push_ffc(s, r, {R, 1. / R, 1. / 2 / R});
     push_rec(s, r);
     return make_out(out, s);
 }
 
-// A double's float-float split (hi, lo) stored in one double slot.
-static double ff_slot(double v) {
-    float pair[2];
-    pair[0] = (float)v;
-    pair[1] = (float)(v - (double)pair[0]);
-    double out;
-    memcpy(&out, pair, sizeof(out));
-    return out;
-}
-
-static void append_ff(std::vector<double>& pool, size_t begin, size_t n) {
-    for (size_t i = 0; i < n; i++) pool.push_back(ff_slot(pool[begin + i]));
-}
 
 static void fill_quadric(bt_surf& r, double R, double conic) {
     // src/quadric.cpp:9-14
@@ -197,6 +208,7 @@ extern "C" int bt_quadric_create(double R, double conic, bt_surface** out) {
     bt_surface* s = new bt_surface;
     bt_surf r = blank_surf(BT_S_QUADRIC);
     fill_quadric(r, R, conic);
+    push_ffc(s, r, {r.p[0], r.p[5], r.p[6], r.p[7], r.p[8], r.p[9]});
     push_rec(s, r);
     return make_out(out, s);
 }
@@ -213,6 +225,7 @@ extern "C" int bt_asphere_create(double R, double conic, const double* coefs, si
     // (src/asphere.cpp:10-16)
     for (size_t j = 0; j < n; j++) s->pool.push_back(coefs[j] * (double)(2 * (j + 1)));
     append_ff(s->pool, 0, 2 * n);
+    push_ffc(s, r, {r.p[0], r.p[5], r.p[6], r.p[7], r.p[8], r.p[9]});
     push_rec(s, r);
     return make_out(out, s);
 }
@@ -236,6 +249,7 @@ extern "C" int bt_polynomial_create(const double* coefs, const double* gradx, co
         s->pool.insert(s->pool.end(), grady, grady + gsz);
     }
     append_ff(s->pool, 0, xsize * ysize + 2 * gsz);
+    push_ffc(s, r, {xorigin, yorigin});
     push_rec(s, r);
     return make_out(out, s);
 }
@@ -288,6 +302,7 @@ extern "C" int bt_sum_create(const bt_surface* const* surfaces, size_t n, bt_sur
     push_rec(s, root);
     for (size_t i = 0; i < n; i++) {
         bt_surf c = surfaces[i]->recs[0];
+        if (c.ffc >= 0) c.ffc += (int32_t)s->pool.size();
         c.off += (int32_t)s->pool.size();
         s->pool.insert(s->pool.end(), surfaces[i]->pool.begin(), surfaces[i]->pool.end());
         push_rec(s, c, surfaces[i]->tables[0]);
@@ -310,6 +325,8 @@ extern "C" int bt_const_medium_create(double n, bt_medium_h** out) {
     bt_medium_h* m = new_medium(BT_M_CONST);
     m->rec.p[0] = n;
     m->rec.p[1] = 1.0 / n;  // reciprocal used by the refraction kernels
+    m->rec.p[2] = ff_slot(n);
+    m->rec.p[3] = ff_slot(1.0 / n);
     return make_out(out, m);
 }
 
@@ -487,6 +504,7 @@ struct ProgBuilder {
         for (size_t i = 0; i < s->recs.size(); i++) {
             bt_surf r = s->recs[i];
             r.off += base_pool;
+            if (r.ffc >= 0) r.ffc += base_pool;
             if (r.kind == BT_S_SUM) r.m += base_rec;
             if (r.kind == BT_S_BICUBIC) {
                 cudaError_t e = table_device(s->tables[i], &r.tab);
@@ -1290,6 +1308,8 @@ extern "C" int bt_check_device_status(void* stream) {
     CUDA_TRY(bt_read_device_status(&st, (cudaStream_t)stream), "device status");
     CUDA_TRY(bt_read_split_device_status(&ss, (cudaStream_t)stream), "device status");
     if (st == 0) st = ss;
+    CUDA_TRY(bt_read_trace_ff_device_status(&ss, (cudaStream_t)stream), "device status");
+    if (st == 0) st = ss;
     CUDA_TRY(bt_read_batch_device_status(&sb, (cudaStream_t)stream), "device status");
     CUDA_TRY(bt_read_mlp_device_status(&sm, (cudaStream_t)stream), "device status");
     const int any = st ? st : (sb ? sb : sm);
@@ -1478,9 +1498,7 @@ extern "C" int bt_batch_create(const bt_batch_desc* d, bt_batch** out) {
             return BT_ERR_CUDA;
         }
         if (modal && (int)k == d->modal_stage) {
-            bt_surf m;
-            memset(&m, 0, sizeof(m));
-            m.kind = BT_S_MODAL;
+            bt_surf m = blank_surf(BT_S_MODAL);
             m.n = d->modal_nx;
             m.m = d->modal_ny;
             for (int i = 0; i < 4; i++) m.p[i] = d->modal_grid[i];

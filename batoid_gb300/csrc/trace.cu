@@ -5,6 +5,7 @@
 // per ray once per surface, each ray is loaded once and stored once.
 #include <cuda_runtime.h>
 #include <stdlib.h>
+#include <string.h>
 #include "bt_internal.h"
 #include "bt_device.cuh"
 #include "bt_stage_smem.cuh"
@@ -123,6 +124,16 @@ int bt_grid_for(long long n, int threads, int per_sm) {
 cudaError_t bt_launch_trace(const unsigned char* d_blob, int blob_bytes, const RV& in, const RV& out,
                             const SnapSet* snaps, int nsnaps, int niter, cudaStream_t stream) {
     if (in.n <= 0) return cudaSuccess;
+    // The float-float form (trace_ff.cu) unless Newton is capped below 3
+    // iterations (its float-float iterations then cannot stand for the
+    // reference's FP64 ones) or BATOID_GB300_TRACE_FORM=fp64 asks for the
+    // FP64 form (a diagnostic: both forms meet the same tolerances).
+    static int form = -1;
+    if (form < 0) {
+        const char* env = getenv("BATOID_GB300_TRACE_FORM");
+        form = (env && strcmp(env, "fp64") == 0) ? 0 : 1;
+    }
+    if (form == 1 && niter >= 3) return bt_launch_trace_ff(d_blob, blob_bytes, in, out, snaps, nsnaps, niter, stream);
     static SnapSet empty;
     const SnapSet& ss = snaps ? *snaps : empty;
     auto kern = k_trace<BT_TRACE_MINB>;
