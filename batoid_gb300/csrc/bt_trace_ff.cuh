@@ -64,6 +64,11 @@ __device__ __forceinline__ bool d_abs_lt(double a, double c) {
 
 __device__ __forceinline__ ff ff_one() { return ff{1.f, 0.f}; }
 
+// a != 0 (either sign of zero) on the integer pipe.
+__device__ __forceinline__ bool d_nonzero(double a) {
+    return ((unsigned long long)__double_as_longlong(a) << 1) != 0ull;
+}
+
 // ---------------------------------------------------------------------------
 // Which surfaces have a float-float form
 // ---------------------------------------------------------------------------
@@ -76,7 +81,7 @@ __device__ __forceinline__ bool ffs_leaf_ok(const bt_surf& s) {
     case BT_S_PARABOLOID:
     case BT_S_QUADRIC:
     case BT_S_ASPHERE:
-        return s.ffc >= 0 && s.p[0] != 0.0;
+        return s.ffc >= 0 && d_nonzero(s.p[0]);
     case BT_S_POLY:
         return s.ffc >= 0;
     default:
@@ -105,7 +110,7 @@ __device__ __forceinline__ ff ffs_conic(const bt_surf& s, const double* C, ff r2
     const ff w = ff_sub(ff_one(), ff_mul(r2, ff_slot(C + 4)));
     *w_out = w;
     const ff q = ff_sqrt(w);
-    if (s.p[10] != 0.0) return ff_mul(ff_sub(ff_one(), q), ff_slot(C + 2));
+    if (d_nonzero(s.p[10])) return ff_mul(ff_sub(ff_one(), q), ff_slot(C + 2));
     return ff_div(r2, ff_mul(ff_slot(C + 0), ff_add(ff_one(), q)));
 }
 
@@ -371,13 +376,49 @@ __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, ff x, ff y, ff
             return true;
         }
     }
-    // not converged in float-float: the FP64 mixed-precision Newton from here
-    const bool ok = bt_newton_mixed(P, si, xd, yd, zd, vxd, vyd, vzd, dtd, niter);
+    // No correction below 1e-12 within niter: as the reference after its
+    // niter iterations, success is |residual| < 1e-12 at the final point
+    // (FP64 conic part, polynomial part evaluated at this dt).
+    const double px = fma(vxd, dtd, xd), py = fma(vyd, dtd, yd), pz = fma(vzd, dtd, zd);
+    ff zc;
+    float ux, uy;
+    ffs_eval(P, si, ff_mad(vx, dt, x), ff_mad(vy, dt, y), &zc, &zp, &ux, &uy);
+    const double res = ffs_conic64(P, si, px, py) + ff_to_d(zp) - pz;
+    *dt_out = dtd;
+    *rx = px;
+    *ry = py;
+    *rz = pz;
+    return d_abs_lt(res, 1e-12);
+}
+
+// Analytic roots whose float-float rounding can approach the position
+// tolerance (|R| above 50 m for spheres and paraboloids, every quadric: the
+// quadric form subtracts squares of R/(1+k), thousands of metres for
+// near-parabolic mirrors) are corrected by one FP64 Newton step on the
+// surface's FP64 sag.  Success stays the analytic root's (a finite
+// discriminant), as in the reference; the step is applied only when the
+// residual is finite and below 1e-9 m.
+__device__ __noinline__ void ff_refine64(const Prog& P, int si, ff x, ff y, ff z, ff vx, ff vy, ff vz, ff dt,
+                                         double* dt_out, double* rx, double* ry, double* rz) {
+    const double xd = ff_to_d(x), yd = ff_to_d(y), zd = ff_to_d(z);
+    const double vxd = ff_to_d(vx), vyd = ff_to_d(vy), vzd = ff_to_d(vz);
+    double dtd = ff_to_d(dt);
+    const double px = fma(vxd, dtd, xd), py = fma(vyd, dtd, yd), pz = fma(vzd, dtd, zd);
+    ff zc, zp;
+    float ux, uy;
+    ffs_eval(P, si, ff_mad(vx, dt, x), ff_mad(vy, dt, y), &zc, &zp, &ux, &uy);
+    const double res = ffs_conic64(P, si, px, py) - pz;
+    if (d_abs_lt(res, 1e-9)) dtd += res * f2d_bits(1.f / fmaf(ux, vx.hi, fmaf(uy, vy.hi, vz.hi)));
     *dt_out = dtd;
     *rx = fma(vxd, dtd, xd);
     *ry = fma(vyd, dtd, yd);
     *rz = fma(vzd, dtd, zd);
-    return ok;
+}
+
+__device__ __forceinline__ bool ffs_needs_refine(const bt_surf& s) {
+    if (s.kind == BT_S_QUADRIC) return true;
+    if (s.kind == BT_S_SPHERE || s.kind == BT_S_PARABOLOID) return !d_abs_lt(s.p[0], 50.0);
+    return false;
 }
 
 // ---------------------------------------------------------------------------
@@ -475,7 +516,8 @@ __device__ __forceinline__ void ff_medium(const Prog& P, int mi, double w, ff* n
     if (m.kind == BT_M_SELLMEIER) {
         // src/medium.cpp:145-149: n^2 = 1 + sum B_i x / (x - C_i), x = (w / 1 um)^2
         const ff wf = d_to_ff(w);
-        const ff x = ff_mul_f(ff_sqr(wf), 1e12f);
+        // 1e12 = 999999995904 + 4096, both exact floats
+        const ff x = ff_mul(ff_sqr(wf), ff{999999995904.f, 4096.f});
         ff n2 = ff_one();
         for (int i = 0; i < 3; i++) {
             const ff B = d_to_ff(m.p[i]), Cc = d_to_ff(m.p[3 + i]);
@@ -501,7 +543,7 @@ __device__ __forceinline__ bool ff_radius_less(ff dx, ff dy, double r, bool* und
     const ff r2 = ff_sqr(rf);
     const ff d = ff_sub(ff_r2(dx, dy), r2);
     const float thr = 1e-13f * r2.hi;
-    if (d.hi < -thr) return r > 0.0;
+    if (d.hi < -thr) return __double_as_longlong(r) > 0;  // r > 0 (a finite radius)
     if (d.hi > thr) return false;
     *undecided = true;
     return false;
@@ -558,9 +600,9 @@ __device__ __forceinline__ bool ff_obsc_run(const Prog& P, int begin, int end, f
 // ---------------------------------------------------------------------------
 
 __device__ __forceinline__ void ff_translate(const bt_stage& st, ff* x, ff* y, ff* z) {
-    if (st.dr[0] != 0.0) *x = ff_sub(*x, d_to_ff(st.dr[0]));
-    if (st.dr[1] != 0.0) *y = ff_sub(*y, d_to_ff(st.dr[1]));
-    if (st.dr[2] != 0.0) *z = ff_sub(*z, d_to_ff(st.dr[2]));
+    if (d_nonzero(st.dr[0])) *x = ff_sub(*x, d_to_ff(st.dr[0]));
+    if (d_nonzero(st.dr[1])) *y = ff_sub(*y, d_to_ff(st.dr[1]));
+    if (d_nonzero(st.dr[2])) *z = ff_sub(*z, d_to_ff(st.dr[2]));
 }
 
 // x' = R^T (x - dr) with the column-major rotation of the stage.
@@ -614,10 +656,19 @@ __device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, 
             ff dt;
             ok = ff_analytic(s, P.pool, x, y, z, vx, vy, vz, &dt);
             if (ok) {
-                x = ff_mad(vx, dt, x);
-                y = ff_mad(vy, dt, y);
-                z = ff_mad(vz, dt, z);
-                r.t += ff_to_d(dt);
+                if (ffs_needs_refine(s)) {
+                    double dtd, px, py, pz;
+                    ff_refine64(P, st.surf, x, y, z, vx, vy, vz, dt, &dtd, &px, &py, &pz);
+                    x = d_to_ff(px);
+                    y = d_to_ff(py);
+                    z = d_to_ff(pz);
+                    r.t += dtd;
+                } else {
+                    x = ff_mad(vx, dt, x);
+                    y = ff_mad(vy, dt, y);
+                    z = ff_mad(vz, dt, z);
+                    r.t += ff_to_d(dt);
+                }
             }
         }
         if (ok) {
