@@ -4,56 +4,38 @@
 // instruction (DFMA, DADD, DMUL, compares, double<->float conversions)
 // occupies the pipe for the same time, and a stage of the FP64 form costs
 // 60-450 of them per ray.  The FP32 pipe issues ~64 lanes for each FP64
-// lane.  This path keeps each ray in float-float (pairs of floats, ~48
-// significant bits) between stages and evaluates the geometry there, and
-// keeps FP64 where the result's stability needs it:
+// lane.  This path evaluates each stage's geometry in float-float (pairs of
+// floats, ~48 significant bits) on float-float copies of the ray, converted
+// with integer instructions, and keeps FP64 where the result's stability
+// needs it:
+//  * the ray's state: positions and directions stay FP64 between stages;
+//    the position update x + v dt is an FP64 FMA, so a ray whose direction
+//    component is zero keeps that coordinate exactly, as in the reference;
 //  * the Newton intersection solve of aspheres, polynomial surfaces and
 //    sums: iterated in float-float to ~1e-13 m, then its residual
 //    sag(x + v dt) - (z + vz dt) is evaluated in FP64 at the FP64 point and
 //    the last correction applied in FP64 (src/surface.cpp:22-49: success is
 //    |residual| < 1e-12 at the final point);
 //  * the optical path: t accumulates in FP64.
-// Analytic intersections (plane, sphere, paraboloid, quadric), normals,
+// Analytic intersections (plane, sphere, paraboloid, quadric; quadrics and
+// large spheres then corrected by one FP64 Newton step), normals,
 // reflection, refraction, the media and the annulus / circle obscuration
-// tests run in float-float; a circle test whose h^2 - r^2 is within 1e-13
-// relative falls back to the reference's FP64 hypot.  Results agree with the
-// reference within its parity tolerances (positions 1e-12 m, path 1e-11 m).
+// tests run in float-float; an obscuration test within 1e-13 relative of
+// its edge falls back to the reference's FP64 test on the FP64 position.
+// Results agree with the reference within its parity tolerances
+// (positions 1e-12 m, path 1e-11 m).
 //
 // Stages whose surface kind has no float-float form here (Tilted, Bicubic,
 // the batched kernel's modal tables, Sum over those) and obscurations other
-// than circles and annuli run the FP64 form on a double copy of the ray.
+// than circles and annuli run the FP64 form.
 #pragma once
 #include "bt_trace_core.cuh"
-
-struct RayF {
-    ff x, y, z, vx, vy, vz;
-    double t, w, f;
-    bool vig, fail;
-};
 
 // Index of the medium whose index is cached and the cached (n, 1/n).
 struct MediumCacheF {
     int idx;
     ff n, inv_n;
 };
-
-__device__ __forceinline__ RayF rayf_from(const RayState& r) {
-    RayF o;
-    o.x = d_to_ff(r.x); o.y = d_to_ff(r.y); o.z = d_to_ff(r.z);
-    o.vx = d_to_ff(r.vx); o.vy = d_to_ff(r.vy); o.vz = d_to_ff(r.vz);
-    o.t = r.t; o.w = r.w; o.f = r.f;
-    o.vig = r.vig; o.fail = r.fail;
-    return o;
-}
-
-__device__ __forceinline__ RayState rayf_to(const RayF& r) {
-    RayState o;
-    o.x = ff_to_d(r.x); o.y = ff_to_d(r.y); o.z = ff_to_d(r.z);
-    o.vx = ff_to_d(r.vx); o.vy = ff_to_d(r.vy); o.vz = ff_to_d(r.vz);
-    o.t = r.t; o.w = r.w; o.f = r.f;
-    o.vig = r.vig; o.fail = r.fail;
-    return o;
-}
 
 // |a| < c for finite c > 0 on the integer pipe (false for NaN, as the
 // floating-point comparison).
@@ -329,14 +311,19 @@ __device__ __forceinline__ bool ff_residual_ok(const Prog& P, int si, ff x, ff y
     return fabsf(res.hi) < 1e-12f;
 }
 
+// FP64 state of a ray in a surface's frame, with its float-float copy.
+struct RayLocal {
+    double xd, yd, zd, vxd, vyd, vzd;
+    ff x, y, z, vx, vy, vz;
+};
+
 // Iterative intersection of an ASPHERE / POLY / SUM: start (the conic root,
 // dt = 0, or the first child's own solve: src/asphere.cpp:76-85,
 // src/sum.cpp:47-56), float-float Newton, then the FP64 residual at the FP64
-// point and the final correction in FP64.  On success the FP64 dt and the
-// FP64 intersection point are returned.
-__device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, ff x, ff y, ff z, ff vx, ff vy, ff vz, int niter,
-                                           double* dt_out, double* rx, double* ry, double* rz) {
+// point and the final correction in FP64.  On success *dt_out is the FP64 dt.
+__device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const RayLocal& L, int niter, double* dt_out) {
     const bt_surf& s = P.surfs[si];
+    const ff x = L.x, y = L.y, z = L.z, vx = L.vx, vy = L.vy, vz = L.vz;
     ff dt{0.f, 0.f};
     ff zp;
     float inv_den = 0.f;
@@ -357,38 +344,26 @@ __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, ff x, ff y, ff
     }
     const bool conv = ff_newton_iter(P, si, x, y, z, vx, vy, vz, &dt, niter, &zp, &inv_den);
     // FP64 residual at the FP64 point x + v dt
-    const double xd = ff_to_d(x), yd = ff_to_d(y), zd = ff_to_d(z);
-    const double vxd = ff_to_d(vx), vyd = ff_to_d(vy), vzd = ff_to_d(vz);
     double dtd = ff_to_d(dt);
-    if (conv) {
-        const double px = fma(vxd, dtd, xd), py = fma(vyd, dtd, yd), pz = fma(vzd, dtd, zd);
-        // the polynomial part was evaluated before the last correction
-        // (< 1e-12 m earlier along the ray; its slope is small): the error is
-        // far below the FP64 conic part's rounding
-        const double res = ffs_conic64(P, si, px, py) + ff_to_d(zp) - pz;
-        if (d_abs_lt(res, 1e-12)) {
-            // the residual after this correction is ~1e-7 of |res|
-            dtd += res * f2d_bits(inv_den);
-            *dt_out = dtd;
-            *rx = fma(vxd, dtd, xd);
-            *ry = fma(vyd, dtd, yd);
-            *rz = fma(vzd, dtd, zd);
-            return true;
-        }
+    const double px = fma(L.vxd, dtd, L.xd), py = fma(L.vyd, dtd, L.yd), pz = fma(L.vzd, dtd, L.zd);
+    if (!conv) {
+        // no correction below 1e-12 within niter: the polynomial part at
+        // this dt for the final test below
+        ff zc;
+        float ux, uy;
+        ffs_eval(P, si, ff_mad(vx, dt, x), ff_mad(vy, dt, y), &zc, &zp, &ux, &uy);
     }
-    // No correction below 1e-12 within niter: as the reference after its
-    // niter iterations, success is |residual| < 1e-12 at the final point
-    // (FP64 conic part, polynomial part evaluated at this dt).
-    const double px = fma(vxd, dtd, xd), py = fma(vyd, dtd, yd), pz = fma(vzd, dtd, zd);
-    ff zc;
-    float ux, uy;
-    ffs_eval(P, si, ff_mad(vx, dt, x), ff_mad(vy, dt, y), &zc, &zp, &ux, &uy);
+    // (after a converged iteration the polynomial part was evaluated before
+    // the last correction, < 1e-12 m earlier along the ray; its slope is
+    // small, so the difference is far below the FP64 conic part's rounding)
     const double res = ffs_conic64(P, si, px, py) + ff_to_d(zp) - pz;
+    const bool ok = d_abs_lt(res, 1e-12);
+    // converged: the residual after this last correction is ~1e-7 of |res|;
+    // otherwise, as the reference after its niter iterations, success is
+    // |residual| < 1e-12 at the final point
+    if (conv && ok) dtd += res * f2d_bits(inv_den);
     *dt_out = dtd;
-    *rx = px;
-    *ry = py;
-    *rz = pz;
-    return d_abs_lt(res, 1e-12);
+    return ok;
 }
 
 // Analytic roots whose float-float rounding can approach the position
@@ -398,21 +373,15 @@ __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, ff x, ff y, ff
 // surface's FP64 sag.  Success stays the analytic root's (a finite
 // discriminant), as in the reference; the step is applied only when the
 // residual is finite and below 1e-9 m.
-__device__ __noinline__ void ff_refine64(const Prog& P, int si, ff x, ff y, ff z, ff vx, ff vy, ff vz, ff dt,
-                                         double* dt_out, double* rx, double* ry, double* rz) {
-    const double xd = ff_to_d(x), yd = ff_to_d(y), zd = ff_to_d(z);
-    const double vxd = ff_to_d(vx), vyd = ff_to_d(vy), vzd = ff_to_d(vz);
+__device__ __noinline__ double ff_refine64(const Prog& P, int si, const RayLocal& L, ff dt) {
     double dtd = ff_to_d(dt);
-    const double px = fma(vxd, dtd, xd), py = fma(vyd, dtd, yd), pz = fma(vzd, dtd, zd);
+    const double px = fma(L.vxd, dtd, L.xd), py = fma(L.vyd, dtd, L.yd), pz = fma(L.vzd, dtd, L.zd);
     ff zc, zp;
     float ux, uy;
-    ffs_eval(P, si, ff_mad(vx, dt, x), ff_mad(vy, dt, y), &zc, &zp, &ux, &uy);
+    ffs_eval(P, si, ff_mad(L.vx, dt, L.x), ff_mad(L.vy, dt, L.y), &zc, &zp, &ux, &uy);
     const double res = ffs_conic64(P, si, px, py) - pz;
-    if (d_abs_lt(res, 1e-9)) dtd += res * f2d_bits(1.f / fmaf(ux, vx.hi, fmaf(uy, vy.hi, vz.hi)));
-    *dt_out = dtd;
-    *rx = fma(vxd, dtd, xd);
-    *ry = fma(vyd, dtd, yd);
-    *rz = fma(vzd, dtd, zd);
+    if (d_abs_lt(res, 1e-9)) dtd += res * f2d_bits(1.f / fmaf(ux, L.vx.hi, fmaf(uy, L.vy.hi, L.vz.hi)));
+    return dtd;
 }
 
 __device__ __forceinline__ bool ffs_needs_refine(const bt_surf& s) {
@@ -549,11 +518,10 @@ __device__ __forceinline__ bool ff_radius_less(ff dx, ff dy, double r, bool* und
     return false;
 }
 
-__device__ __forceinline__ bool ff_obsc_run(const Prog& P, int begin, int end, ff x, ff y) {
+__device__ __forceinline__ bool ff_obsc_run(const Prog& P, int begin, int end, ff x, ff y, double xd,
+                                            double yd) {
     uint32_t stack = 0;
     int sp = 0;
-    bool have_d = false;
-    double xd = 0.0, yd = 0.0;
     for (int k = begin; k < end; k++) {
         const bt_obsc& o = P.obsc[k];
         bool v = false;
@@ -568,10 +536,7 @@ __device__ __forceinline__ bool ff_obsc_run(const Prog& P, int begin, int end, f
                 const bool in_outer = ff_radius_less(dx, dy, o.p[1], &und);
                 v = !in_inner && in_outer;
             }
-            if (und) {
-                if (!have_d) { xd = ff_to_d(x); yd = ff_to_d(y); have_d = true; }
-                v = bt_obsc_run(P, k, k + 1, xd, yd);
-            }
+            if (und) v = bt_obsc_run(P, k, k + 1, xd, yd);
         } else if (o.op == BT_O_NEGATION || o.op == BT_O_UNION || o.op == BT_O_INTERSECTION) {
             if (o.op == BT_O_NEGATION) {
                 sp--;
@@ -586,7 +551,6 @@ __device__ __forceinline__ bool ff_obsc_run(const Prog& P, int begin, int end, f
                 v = acc;
             }
         } else {
-            if (!have_d) { xd = ff_to_d(x); yd = ff_to_d(y); have_d = true; }
             v = bt_obsc_run(P, k, k + 1, xd, yd);
         }
         stack = (stack & ~(1u << sp)) | ((uint32_t)v << sp);
@@ -599,94 +563,76 @@ __device__ __forceinline__ bool ff_obsc_run(const Prog& P, int begin, int end, f
 // One stage (semantics of run_stage, src/batoid.cpp:175-506)
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ void ff_translate(const bt_stage& st, ff* x, ff* y, ff* z) {
-    if (d_nonzero(st.dr[0])) *x = ff_sub(*x, d_to_ff(st.dr[0]));
-    if (d_nonzero(st.dr[1])) *y = ff_sub(*y, d_to_ff(st.dr[1]));
-    if (d_nonzero(st.dr[2])) *z = ff_sub(*z, d_to_ff(st.dr[2]));
-}
-
-// x' = R^T (x - dr) with the column-major rotation of the stage.
-__device__ __forceinline__ void ff_rotate(const bt_stage& st, ff* x, ff* y, ff* z) {
-    const ff a = *x, b = *y, c = *z;
-    ff m[9];
-#pragma unroll
-    for (int i = 0; i < 9; i++) m[i] = d_to_ff(st.drot[i]);
-    *x = ff_add(ff_add(ff_mul(a, m[0]), ff_mul(b, m[3])), ff_mul(c, m[6]));
-    *y = ff_add(ff_add(ff_mul(a, m[1]), ff_mul(b, m[4])), ff_mul(c, m[7]));
-    *z = ff_add(ff_add(ff_mul(a, m[2]), ff_mul(b, m[5])), ff_mul(c, m[8]));
-}
-
-// A stage on the FP64 form, for the surface kinds without a float-float form.
-__device__ __noinline__ void ff_stage_fp64(const Prog& P, const bt_stage& st, RayF& r, int niter) {
-    RayState d = rayf_to(r);
+// A stage on the FP64 form, for the surface kinds without a float-float
+// form (out of line: rare, and large).
+__device__ __noinline__ void ff_stage_fp64(const Prog& P, const bt_stage& st, RayState& r, int niter) {
     int cm = -1;
     double cn = 0.0, cin = 0.0;
-    run_stage<false>(P, st, d, niter, cm, cn, cin);
-    r = rayf_from(d);
+    run_stage<false>(P, st, r, niter, cm, cn, cin);
 }
 
-__device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, RayF& r, int niter,
+__device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, RayState& r, int niter,
                                              MediumCacheF& mc) {
     if (st.kind == BT_ST_SCREEN || (st.kind != BT_ST_OBSCURE && !r.fail && !ffs_ok(P, st.surf))) {
         ff_stage_fp64(P, st, r, niter);
         return;
     }
+    ff fx, fy;  // float-float copy of the final (x, y), for the obscuration
+    bool have_f = false;
     if (st.kind != BT_ST_OBSCURE && !r.fail) {
-        ff x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
-        if (st.identity != 1) {
-            ff_translate(st, &x, &y, &z);
-            if (st.identity == 0) {
-                ff_rotate(st, &x, &y, &z);
-                ff_rotate(st, &vx, &vy, &vz);
-            }
+        RayLocal L;
+        // the transform in FP64, as the reference (src/batoid.cpp:225-233)
+        if (st.identity == 1) {
+            L.xd = r.x; L.yd = r.y; L.zd = r.z; L.vxd = r.vx; L.vyd = r.vy; L.vzd = r.vz;
+        } else if (st.identity == 2) {
+            L.xd = r.x - st.dr[0]; L.yd = r.y - st.dr[1]; L.zd = r.z - st.dr[2];
+            L.vxd = r.vx; L.vyd = r.vy; L.vzd = r.vz;
+        } else {
+            const double dx = r.x - st.dr[0], dy = r.y - st.dr[1], dz = r.z - st.dr[2];
+            L.xd = dx * st.drot[0] + dy * st.drot[3] + dz * st.drot[6];
+            L.yd = dx * st.drot[1] + dy * st.drot[4] + dz * st.drot[7];
+            L.zd = dx * st.drot[2] + dy * st.drot[5] + dz * st.drot[8];
+            L.vxd = r.vx * st.drot[0] + r.vy * st.drot[3] + r.vz * st.drot[6];
+            L.vyd = r.vx * st.drot[1] + r.vy * st.drot[4] + r.vz * st.drot[7];
+            L.vzd = r.vx * st.drot[2] + r.vy * st.drot[5] + r.vz * st.drot[8];
         }
+        L.x = d_to_ff(L.xd); L.y = d_to_ff(L.yd); L.z = d_to_ff(L.zd);
+        L.vx = d_to_ff(L.vxd); L.vy = d_to_ff(L.vyd); L.vz = d_to_ff(L.vzd);
         const bt_surf& s = P.surfs[st.surf];
         bool ok;
-        ff nx_, ny_, nz_;
+        double dtd = 0.0;
         if (s.kind == BT_S_ASPHERE || s.kind == BT_S_POLY || s.kind == BT_S_SUM) {
-            double dtd, px, py, pz;
-            ok = ff_newton_tti(P, st.surf, x, y, z, vx, vy, vz, niter, &dtd, &px, &py, &pz);
-            if (ok) {
-                x = d_to_ff(px);
-                y = d_to_ff(py);
-                z = d_to_ff(pz);
-                r.t += dtd;
-            }
+            ok = ff_newton_tti(P, st.surf, L, niter, &dtd);
         } else {
             ff dt;
-            ok = ff_analytic(s, P.pool, x, y, z, vx, vy, vz, &dt);
-            if (ok) {
-                if (ffs_needs_refine(s)) {
-                    double dtd, px, py, pz;
-                    ff_refine64(P, st.surf, x, y, z, vx, vy, vz, dt, &dtd, &px, &py, &pz);
-                    x = d_to_ff(px);
-                    y = d_to_ff(py);
-                    z = d_to_ff(pz);
-                    r.t += dtd;
-                } else {
-                    x = ff_mad(vx, dt, x);
-                    y = ff_mad(vy, dt, y);
-                    z = ff_mad(vz, dt, z);
-                    r.t += ff_to_d(dt);
-                }
-            }
+            ok = ff_analytic(s, P.pool, L.x, L.y, L.z, L.vx, L.vy, L.vz, &dt);
+            if (ok) dtd = ffs_needs_refine(s) ? ff_refine64(P, st.surf, L, dt) : ff_to_d(dt);
         }
         if (ok) {
+            // src/batoid.cpp:236-242: x += v dt, t += dt
+            const double x = fma(L.vxd, dtd, L.xd), y = fma(L.vyd, dtd, L.yd), z = fma(L.vzd, dtd, L.zd);
+            double vx = L.vxd, vy = L.vyd, vz = L.vzd;
+            r.t += dtd;
+            fx = d_to_ff(x);
+            fy = d_to_ff(y);
+            have_f = true;
             if (st.kind == BT_ST_INTERSECT) {
                 if (st.coated) r.f *= st.coat_t;
             } else {
-                ffs_normal(P, st.surf, x, y, &nx_, &ny_, &nz_);
+                ff nx_, ny_, nz_;
+                ffs_normal(P, st.surf, fx, fy, &nx_, &ny_, &nz_);
+                const ff wx = L.vx, wy = L.vy, wz = L.vz;
                 if (st.kind == BT_ST_REFLECT) {
                     // src/batoid.cpp:343-353
-                    const ff a2 = ff_mul_f(ff_dot3(vx, vy, vz, nx_, ny_, nz_), 2.f);
-                    vx = ff_sub(vx, ff_mul(a2, nx_));
-                    vy = ff_sub(vy, ff_mul(a2, ny_));
-                    vz = ff_sub(vz, ff_mul(a2, nz_));
+                    const ff a2 = ff_mul_f(ff_dot3(wx, wy, wz, nx_, ny_, nz_), 2.f);
+                    vx = ff_to_d(ff_sub(wx, ff_mul(a2, nx_)));
+                    vy = ff_to_d(ff_sub(wy, ff_mul(a2, ny_)));
+                    vz = ff_to_d(ff_sub(wz, ff_mul(a2, nz_)));
                     if (st.coated) r.f *= st.coat_r;
                 } else {
                     // src/batoid.cpp:453-499
-                    const ff n1 = ff_rsqrt(ff_add(ff_sqr(vz), ff_r2(vx, vy)));
-                    const ff nvx = ff_mul(vx, n1), nvy = ff_mul(vy, n1), nvz = ff_mul(vz, n1);
+                    const ff n1 = ff_rsqrt(ff_add(ff_sqr(wz), ff_r2(wx, wy)));
+                    const ff nvx = ff_mul(wx, n1), nvy = ff_mul(wy, n1), nvz = ff_mul(wz, n1);
                     ff alpha = ff_dot3(nvx, nvy, nvz, nx_, ny_, nz_);
                     if (alpha.hi > 0.f) {
                         nx_ = ff_neg(nx_); ny_ = ff_neg(ny_); nz_ = ff_neg(nz_);
@@ -700,16 +646,15 @@ __device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, 
                     const ff eta = ff_mul(n1, mc.inv_n);
                     const ff sinsqr = ff_mul(ff_sqr(eta), ff_sub(ff_one(), ff_sqr(alpha)));
                     if (sinsqr.hi > 1.f || (sinsqr.hi == 1.f && sinsqr.lo > 0.f)) {
-                        const float qnan = __int_as_float(0x7fc00000);
-                        vx = ff{qnan, 0.f}; vy = ff{qnan, 0.f}; vz = ff{qnan, 0.f};
+                        vx = NAN; vy = NAN; vz = NAN;
                         r.fail = true;
                         r.vig = true;
                     } else {
                         const ff cosr = ff_sqrt(ff_sub(ff_one(), sinsqr));
                         const ff nfactor = ff_add(ff_mul(eta, alpha), cosr);
-                        vx = ff_mul(ff_sub(ff_mul(eta, nvx), ff_mul(nfactor, nx_)), mc.inv_n);
-                        vy = ff_mul(ff_sub(ff_mul(eta, nvy), ff_mul(nfactor, ny_)), mc.inv_n);
-                        vz = ff_mul(ff_sub(ff_mul(eta, nvz), ff_mul(nfactor, nz_)), mc.inv_n);
+                        vx = ff_to_d(ff_mul(ff_sub(ff_mul(eta, nvx), ff_mul(nfactor, nx_)), mc.inv_n));
+                        vy = ff_to_d(ff_mul(ff_sub(ff_mul(eta, nvy), ff_mul(nfactor, ny_)), mc.inv_n));
+                        vz = ff_to_d(ff_mul(ff_sub(ff_mul(eta, nvz), ff_mul(nfactor, nz_)), mc.inv_n));
                     }
                     if (st.coated) r.f *= st.coat_t;
                 }
@@ -723,6 +668,10 @@ __device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, 
     }
     if (st.obsc_end > st.obsc_begin) {
         // src/batoid.cpp:169-171: vignetted |= contains(x, y), for every ray
-        if (ff_obsc_run(P, st.obsc_begin, st.obsc_end, r.x, r.y)) r.vig = true;
+        if (!have_f) {
+            fx = d_to_ff(r.x);
+            fy = d_to_ff(r.y);
+        }
+        if (ff_obsc_run(P, st.obsc_begin, st.obsc_end, fx, fy, r.x, r.y)) r.vig = true;
     }
 }

@@ -1,6 +1,5 @@
 // Fused sequential trace, float-float form (bt_trace_ff.cuh): one thread
-// carries one ray through every stage, in registers, as in trace.cu; the
-// ray is converted to float-float once on load and back once on store.
+// carries one ray through every stage, in registers, as in trace.cu.
 #include <cuda_runtime.h>
 #include <stdlib.h>
 #include "bt_internal.h"
@@ -42,14 +41,14 @@ k_trace_ff(const unsigned char* __restrict__ gblob, int blob_bytes, RV in, RV ou
     for (long long base = (long long)blockIdx.x * T; base < in.n; base += stride) {
         const long long i = base + threadIdx.x;
         const bool act = i < in.n;
-        RayF r;
+        RayState r;
         if (act) {
-            r.x = d_to_ff(in.x[i]);
-            r.y = d_to_ff(in.y[i]);
-            r.z = d_to_ff(in.z[i]);
-            r.vx = d_to_ff(in.vx[i]);
-            r.vy = d_to_ff(in.vy[i]);
-            r.vz = d_to_ff(in.vz[i]);
+            r.x = in.x[i];
+            r.y = in.y[i];
+            r.z = in.z[i];
+            r.vx = in.vx[i];
+            r.vy = in.vy[i];
+            r.vz = in.vz[i];
             r.t = in.t[i];
             r.w = in.w[i];
             r.f = in.f[i];
@@ -61,11 +60,11 @@ k_trace_ff(const unsigned char* __restrict__ gblob, int blob_bytes, RV in, RV ou
         for (int s = 0; s < P.nstages; s++) {
             if (act) {
                 run_stage_ff(P, P.stages[s], r, niter, mc);
-                if (s < nsnaps) store_ray(snaps.s[s], i, rayf_to(r));
+                if (s < nsnaps) store_ray(snaps.s[s], i, r);
             }
             __syncthreads();
         }
-        if (act && nsnaps == 0) store_ray(out, i, rayf_to(r));
+        if (act && nsnaps == 0) store_ray(out, i, r);
     }
 }
 
