@@ -317,41 +317,57 @@ struct RayLocal {
     ff x, y, z, vx, vy, vz;
 };
 
-// Iterative intersection of an ASPHERE / POLY / SUM: start (the conic root,
-// dt = 0, or the first child's own solve: src/asphere.cpp:76-85,
+// Iterative intersection of an ASPHERE / POLY / SUM: start t0 (the conic
+// root, 0, or the first child's own solve: src/asphere.cpp:76-85,
 // src/sum.cpp:47-56), float-float Newton, then the FP64 residual at the FP64
 // point and the final correction in FP64.  On success *dt_out is the FP64 dt.
+//
+// The float-float iterations run on the ray re-anchored at its FP64 point
+// p0 = x + v t0 (FP64 FMAs), in the offset d = dt - t0: the residual's terms
+// are then of the size of the sag, not of the distance the ray travelled
+// (15 m before the primary of a telescope), so their rounding (~1e-16 m)
+// stays far below the 1e-12 m convergence and success thresholds.
 __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const RayLocal& L, int niter, double* dt_out) {
     const bt_surf& s = P.surfs[si];
-    const ff x = L.x, y = L.y, z = L.z, vx = L.vx, vy = L.vy, vz = L.vz;
-    ff dt{0.f, 0.f};
-    ff zp;
-    float inv_den = 0.f;
+    const ff vx = L.vx, vy = L.vy, vz = L.vz;
+    ff t0{0.f, 0.f};
+    bool child_done = false;
+    int c0 = -1;
     if (s.kind == BT_S_SUM) {
-        const int c0 = s.m;
+        c0 = s.m;
         const bt_surf& first = P.surfs[c0];
-        if (first.kind == BT_S_ASPHERE || first.kind == BT_S_POLY) {
-            if (first.kind == BT_S_ASPHERE && !ff_quadric_root(P.pool + first.ffc, x, y, z, vx, vy, vz, &dt))
-                return false;
-            if (!ff_newton_iter(P, c0, x, y, z, vx, vy, vz, &dt, niter, &zp, &inv_den) &&
-                !ff_residual_ok(P, c0, x, y, z, vx, vy, vz, dt))
-                return false;
-        } else if (!ff_analytic(first, P.pool, x, y, z, vx, vy, vz, &dt)) {
-            return false;
+        if (first.kind == BT_S_ASPHERE) {
+            if (!ff_quadric_root(P.pool + first.ffc, L.x, L.y, L.z, vx, vy, vz, &t0)) return false;
+        } else if (first.kind != BT_S_POLY) {
+            if (!ff_analytic(first, P.pool, L.x, L.y, L.z, vx, vy, vz, &t0)) return false;
+            child_done = true;
         }
     } else if (s.kind == BT_S_ASPHERE) {
-        if (!ff_quadric_root(P.pool + s.ffc, x, y, z, vx, vy, vz, &dt)) return false;
+        if (!ff_quadric_root(P.pool + s.ffc, L.x, L.y, L.z, vx, vy, vz, &t0)) return false;
     }
-    const bool conv = ff_newton_iter(P, si, x, y, z, vx, vy, vz, &dt, niter, &zp, &inv_den);
+    // anchor
+    const double t0d = ff_to_d(t0);
+    const double p0x = fma(L.vxd, t0d, L.xd), p0y = fma(L.vyd, t0d, L.yd), p0z = fma(L.vzd, t0d, L.zd);
+    const ff ax = d_to_ff(p0x), ay = d_to_ff(p0y), az = d_to_ff(p0z);
+    ff d{0.f, 0.f};
+    ff zp;
+    float inv_den = 0.f;
+    if (c0 >= 0 && !child_done) {
+        // the first child's own Newton; it must succeed (src/sum.cpp:47-56)
+        if (!ff_newton_iter(P, c0, ax, ay, az, vx, vy, vz, &d, niter, &zp, &inv_den) &&
+            !ff_residual_ok(P, c0, ax, ay, az, vx, vy, vz, d))
+            return false;
+    }
+    const bool conv = ff_newton_iter(P, si, ax, ay, az, vx, vy, vz, &d, niter, &zp, &inv_den);
     // FP64 residual at the FP64 point x + v dt
-    double dtd = ff_to_d(dt);
+    double dtd = t0d + ff_to_d(d);
     const double px = fma(L.vxd, dtd, L.xd), py = fma(L.vyd, dtd, L.yd), pz = fma(L.vzd, dtd, L.zd);
     if (!conv) {
         // no correction below 1e-12 within niter: the polynomial part at
         // this dt for the final test below
         ff zc;
         float ux, uy;
-        ffs_eval(P, si, ff_mad(vx, dt, x), ff_mad(vy, dt, y), &zc, &zp, &ux, &uy);
+        ffs_eval(P, si, ff_mad(vx, d, ax), ff_mad(vy, d, ay), &zc, &zp, &ux, &uy);
     }
     // (after a converged iteration the polynomial part was evaluated before
     // the last correction, < 1e-12 m earlier along the ray; its slope is

@@ -28,8 +28,10 @@ def test_reference_analyses(optic):
     sx, sy = bt.spot(optic, *TH, WL, nx=32)
     np.testing.assert_allclose(sx, g["spot_x"], rtol=0, atol=1e-12)
     np.testing.assert_allclose(sy, g["spot_y"], rtol=0, atol=1e-12)
+    # PSF tolerance of the parity contract: 1e-5 of the peak (an OPD error of
+    # 1e-13 m, 1e-6 rad of phase at 620 nm, moves the |FFT|^2 by ~1e-6)
     psf = bt.fftPSF(optic, *TH, WL, nx=32, pad_factor=2)
-    np.testing.assert_allclose(psf.array, g["fft_array"], rtol=0, atol=1e-6 * g["fft_array"].max())
+    np.testing.assert_allclose(psf.array, g["fft_array"], rtol=0, atol=1e-5 * g["fft_array"].max())
     np.testing.assert_allclose(psf.primitiveVectors, g["fft_prim"], rtol=1e-6, atol=0)
     # closest approach of rays 1 arcsec off axis: position noise of 1e-12 m
     # becomes ~2e-7 m along the axis (1 / 5e-6 rad)
