@@ -31,6 +31,7 @@
 #include "bt_device.cuh"
 #include "bt_stage_smem.cuh"
 #include "bt_trace_core.cuh"
+#include "bt_trace_ff.cuh"
 #include "bt_batch.h"
 
 cudaError_t bt_read_batch_device_status(int* status, cudaStream_t stream) {
@@ -244,6 +245,12 @@ __device__ __noinline__ void bt_chol_solve(double* G, const double* bv, int J, i
     }
 }
 
+// The FP64 form of a stage (Newton capped below 3 iterations), out of line.
+static __device__ __noinline__ void bt_batch_stage_fp64(const Prog& P, const bt_stage& st, RayState& r, int niter,
+                                                        int& cm, double& cn, double& cin) {
+    run_stage<true>(P, st, r, niter, cm, cn, cin);
+}
+
 __global__ void __launch_bounds__(BT_BATCH_MAX_THREADS, BT_BATCH_MIN_BLOCKS)
 k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const __grid_constant__ BatchArgs A) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -339,11 +346,18 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
             double gx = 0.0, gy = 0.0;
             int cm = -1;
             double cn = 0.0, cin = 0.0;
+            MediumCacheF mcf_;
+            mcf_.idx = -1;
             if (active) bt_batch_ray(A, F, nx, i, wl, r, &gx, &gy);
             // stage-synchronous: all warps of the block run the same stage's
-            // code together (instruction-cache working set of one stage)
+            // code together (instruction-cache working set of one stage).
+            // The float-float form of the stages (as the fused trace) unless
+            // Newton is capped below 3 iterations.
             for (int k = 0; k < A.ntrace; k++) {
-                if (active) run_stage<true>(P, stages[k], r, A.niter, cm, cn, cin);
+                if (active) {
+                    if (A.niter >= 3) run_stage_ff(P, stages[k], r, A.niter, mcf_);
+                    else bt_batch_stage_fp64(P, stages[k], r, A.niter, cm, cn, cin);
+                }
                 __syncthreads();
             }
             if (active) {

@@ -26,8 +26,9 @@
 // (positions 1e-12 m, path 1e-11 m).
 //
 // Stages whose surface kind has no float-float form here (Tilted, Bicubic,
-// the batched kernel's modal tables, Sum over those) and obscurations other
-// than circles and annuli run the FP64 form.
+// a Sum over those) and obscurations other than circles and annuli run the
+// FP64 form.  The batched kernel's bending-mode tables (a Sum's later
+// child) are evaluated in FP32 on their cached corner values.
 #pragma once
 #include "bt_trace_core.cuh"
 
@@ -74,9 +75,53 @@ __device__ __forceinline__ bool ffs_leaf_ok(const bt_surf& s) {
 __device__ __forceinline__ bool ffs_ok(const Prog& P, int si) {
     const bt_surf& s = P.surfs[si];
     if (s.kind != BT_S_SUM) return ffs_leaf_ok(s);
-    for (int c = 0; c < s.n; c++)
-        if (!ffs_leaf_ok(P.surfs[s.m + c])) return false;
+    for (int c = 0; c < s.n; c++) {
+        const bt_surf& cs = P.surfs[s.m + c];
+        // modal bending tables of the batched kernel (a Sum's later child)
+        if (cs.kind == BT_S_MODAL) {
+            if (c == 0 || P.mc == nullptr) return false;
+        } else if (!ffs_leaf_ok(cs)) {
+            return false;
+        }
+    }
     return true;
+}
+
+// MODAL surface (sum of bending-mode tables, batched kernel only): the cell
+// and fractions from the float-float position, the per-thread cached corner
+// values of the weighted tables (FP32 copies) and the Hermite patch in
+// FP32.  The bending sags are ~1e-7 m, so FP32 carries them to ~1e-14 m.
+// Returns the sag as *zp, the FP32 slope (-dz/dx, -dz/dy).  Outside the grid
+// the reference's fill value (NaN or 0, src/bicubic.cpp:19-40).
+static __device__ __noinline__ void ff_modal_eval(const Prog& P, const bt_surf& s, ff x, ff y, ff* zp, float* ux, float* uy) {
+    const ff u = ff_mul(ff_sub(x, d_to_ff(s.p[0])), d_to_ff(s.p[6]));
+    const ff v = ff_mul(ff_sub(y, d_to_ff(s.p[1])), d_to_ff(s.p[7]));
+    float fu = floorf(u.hi), fv = floorf(v.hi);
+    if (u.hi == fu && u.lo < 0.f) fu -= 1.f;
+    if (v.hi == fv && v.lo < 0.f) fv -= 1.f;
+    if (!(fu >= 0.f) || !(fv >= 0.f) || fu >= (float)(s.n - 1) || fv >= (float)(s.m - 1)) {
+        const float fill = d_nonzero(s.p[4]) ? __int_as_float(0x7fc00000) : 0.f;
+        *zp = ff{fill, 0.f};
+        *ux = fill;
+        *uy = fill;
+        return;
+    }
+    const int ix = (int)fu, iy = (int)fv;
+    const float xf = (u.hi - fu) + u.lo, yf = (v.hi - fv) + v.lo;
+    const int cell = iy * s.n + ix;
+    if (*P.mcell != cell) {
+        bt_modal_fill(P.pool, &s, ix, iy, P.mc, P.mcf, P.mstride);
+        *P.mcell = cell;
+    }
+    float w[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) w[k] = P.mcf[k * P.mstride];
+    float val, gx, gy;
+    bt_hermite<float>(xf, yf, d_to_ff(s.p[2]).hi, d_to_ff(s.p[3]).hi, w, w + 4, w + 8, w + 12, &val, &gx, &gy, true,
+                      true);
+    *zp = ff{val, 0.f};
+    *ux = -gx;
+    *uy = -gy;
 }
 
 // ---------------------------------------------------------------------------
@@ -86,14 +131,14 @@ __device__ __forceinline__ bool ffs_ok(const Prog& P, int si) {
 // r^2 = x^2 + y^2
 __device__ __forceinline__ ff ff_r2(ff x, ff y) { return ff_add(ff_sqr(x), ff_sqr(y)); }
 
-// Conic sag of a QUADRIC / ASPHERE record: (1 - q) R/(1+k) or r^2/(R (1+q)),
-// q = sqrt(1 - r^2 (1+k)/R^2), as the FP64 form (bt_conic).
-__device__ __forceinline__ ff ffs_conic(const bt_surf& s, const double* C, ff r2, ff* w_out) {
+// Conic sag of a QUADRIC / ASPHERE record, r^2 / (R (1 + q)) with
+// q = sqrt(1 - r^2 (1+k)/R^2).  (The equal form (1 - q) R/(1+k), which the
+// FP64 form may use, multiplies the rounding of q by |R/(1+k)|, ~100 m for
+// some mirrors: in float-float that would be ~1e-12 m.)
+__device__ __forceinline__ ff ffs_conic(const double* C, ff r2, ff* w_out) {
     const ff w = ff_sub(ff_one(), ff_mul(r2, ff_slot(C + 4)));
     *w_out = w;
-    const ff q = ff_sqrt(w);
-    if (d_nonzero(s.p[10])) return ff_mul(ff_sub(ff_one(), q), ff_slot(C + 2));
-    return ff_div(r2, ff_mul(ff_slot(C + 0), ff_add(ff_one(), q)));
+    return ff_div(r2, ff_mul(ff_slot(C + 0), ff_add(ff_one(), ff_sqrt(w))));
 }
 
 // Leaf sag at (x, y): *zc the conic part (recomputed in FP64 by
@@ -105,9 +150,11 @@ __device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* po
     *zp = ff{0.f, 0.f};
     switch (s.kind) {
     case BT_S_SPHERE: {
+        // R (1 - q) = r^2 / (R (1 + q)), q = sqrt(1 - r^2/R^2), in the form
+        // without cancellation
         const ff r2 = ff_r2(x, y);
         const ff w = ff_sub(ff_one(), ff_mul(r2, ff_slot(C + 3)));
-        *zc = ff_mul(ff_slot(C + 0), ff_sub(ff_one(), ff_sqrt(w)));
+        *zc = ff_div(r2, ff_mul(ff_slot(C + 0), ff_add(ff_one(), ff_sqrt(w))));
         const float k = rsqrtf(w.hi) * ff_slot(C + 2).hi;
         *ux = -x.hi * k;
         *uy = -y.hi * k;
@@ -124,7 +171,7 @@ __device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* po
     case BT_S_ASPHERE: {
         const ff r2 = ff_r2(x, y);
         ff w;
-        *zc = ffs_conic(s, C, r2, &w);
+        *zc = ffs_conic(C, r2, &w);
         float kf = rsqrtf(w.hi) * ff_slot(C + 5).hi;
         if (s.kind == BT_S_ASPHERE && s.n > 0) {
             const ff* c = ff_ptr(pool, s.off + 2 * s.n);
@@ -166,9 +213,11 @@ __device__ __forceinline__ void ffs_eval(const Prog& P, int si, ff x, ff y, ff* 
     ff c_acc{0.f, 0.f}, p_acc{0.f, 0.f};
     float gx = 0.f, gy = 0.f;
     for (int c = 0; c < s.n; c++) {
-        ff cz, pz;
+        ff cz{0.f, 0.f}, pz;
         float cx, cy;
-        ffs_leaf_eval(P.surfs[s.m + c], P.pool, x, y, &cz, &pz, &cx, &cy);
+        const bt_surf& cs = P.surfs[s.m + c];
+        if (cs.kind == BT_S_MODAL) ff_modal_eval(P, cs, x, y, &pz, &cx, &cy);
+        else ffs_leaf_eval(cs, P.pool, x, y, &cz, &pz, &cx, &cy);
         c_acc = ff_add(c_acc, cz);
         p_acc = ff_add(p_acc, pz);
         gx += cx;
@@ -327,7 +376,7 @@ struct RayLocal {
 // are then of the size of the sag, not of the distance the ray travelled
 // (15 m before the primary of a telescope), so their rounding (~1e-16 m)
 // stays far below the 1e-12 m convergence and success thresholds.
-__device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const RayLocal& L, int niter, double* dt_out) {
+static __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const RayLocal& L, int niter, double* dt_out) {
     const bt_surf& s = P.surfs[si];
     const ff vx = L.vx, vy = L.vy, vz = L.vz;
     ff t0{0.f, 0.f};
@@ -372,12 +421,26 @@ __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const RayLocal
     // (after a converged iteration the polynomial part was evaluated before
     // the last correction, < 1e-12 m earlier along the ray; its slope is
     // small, so the difference is far below the FP64 conic part's rounding)
-    const double res = ffs_conic64(P, si, px, py) + ff_to_d(zp) - pz;
-    const bool ok = d_abs_lt(res, 1e-12);
+    double res = ffs_conic64(P, si, px, py) + ff_to_d(zp) - pz;
+    bool ok = d_abs_lt(res, 1e-12);
     // converged: the residual after this last correction is ~1e-7 of |res|;
     // otherwise, as the reference after its niter iterations, success is
     // |residual| < 1e-12 at the final point
     if (conv && ok) dtd += res * f2d_bits(inv_den);
+    if (conv && !ok) {
+        // converged in float-float but not yet to 1e-12 in FP64 (should not
+        // happen; kept as a safety net): up to two FP64 corrections, the
+        // polynomial part re-evaluated at each point
+        for (int k = 0; k < 2 && !ok; k++) {
+            dtd += res * f2d_bits(inv_den);
+            const double qx = fma(L.vxd, dtd, L.xd), qy = fma(L.vyd, dtd, L.yd), qz = fma(L.vzd, dtd, L.zd);
+            ff zc;
+            float ux, uy;
+            ffs_eval(P, si, d_to_ff(qx), d_to_ff(qy), &zc, &zp, &ux, &uy);
+            res = ffs_conic64(P, si, qx, qy) + ff_to_d(zp) - qz;
+            ok = d_abs_lt(res, 1e-12);
+        }
+    }
     *dt_out = dtd;
     return ok;
 }
@@ -389,7 +452,7 @@ __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const RayLocal
 // surface's FP64 sag.  Success stays the analytic root's (a finite
 // discriminant), as in the reference; the step is applied only when the
 // residual is finite and below 1e-9 m.
-__device__ __noinline__ double ff_refine64(const Prog& P, int si, const RayLocal& L, ff dt) {
+static __device__ __noinline__ double ff_refine64(const Prog& P, int si, const RayLocal& L, ff dt) {
     double dtd = ff_to_d(dt);
     const double px = fma(L.vxd, dtd, L.xd), py = fma(L.vyd, dtd, L.yd), pz = fma(L.vzd, dtd, L.zd);
     ff zc, zp;
@@ -475,7 +538,16 @@ __device__ __forceinline__ void ffs_normal(const Prog& P, int si, ff x, ff y, ff
     } else {
         for (int c = 0; c < s.n; c++) {
             ff cx, cy;
-            ffs_leaf_slope(P.surfs[s.m + c], P.pool, x, y, &cx, &cy);
+            const bt_surf& cs = P.surfs[s.m + c];
+            if (cs.kind == BT_S_MODAL) {
+                ff z;
+                float gx, gy;
+                ff_modal_eval(P, cs, x, y, &z, &gx, &gy);
+                cx = ff{gx, 0.f};
+                cy = ff{gy, 0.f};
+            } else {
+                ffs_leaf_slope(cs, P.pool, x, y, &cx, &cy);
+            }
             ux = ff_add(ux, cx);
             uy = ff_add(uy, cy);
         }
@@ -581,7 +653,7 @@ __device__ __forceinline__ bool ff_obsc_run(const Prog& P, int begin, int end, f
 
 // A stage on the FP64 form, for the surface kinds without a float-float
 // form (out of line: rare, and large).
-__device__ __noinline__ void ff_stage_fp64(const Prog& P, const bt_stage& st, RayState& r, int niter) {
+static __device__ __noinline__ void ff_stage_fp64(const Prog& P, const bt_stage& st, RayState& r, int niter) {
     int cm = -1;
     double cn = 0.0, cin = 0.0;
     run_stage<false>(P, st, r, niter, cm, cn, cin);
