@@ -348,6 +348,8 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
             double cn = 0.0, cin = 0.0;
             MediumCacheF mcf_;
             mcf_.idx = -1;
+            RayCacheF fcache;
+            fcache.ok = false;
             if (active) bt_batch_ray(A, F, nx, i, wl, r, &gx, &gy);
             // stage-synchronous: all warps of the block run the same stage's
             // code together (instruction-cache working set of one stage).
@@ -355,7 +357,7 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
             // Newton is capped below 3 iterations.
             for (int k = 0; k < A.ntrace; k++) {
                 if (active) {
-                    if (A.niter >= 3) run_stage_ff(P, stages[k], r, A.niter, mcf_);
+                    if (A.niter >= 3) run_stage_ff(P, stages[k], r, A.niter, mcf_, fcache);
                     else bt_batch_stage_fp64(P, stages[k], r, A.niter, cm, cn, cin);
                 }
                 __syncthreads();

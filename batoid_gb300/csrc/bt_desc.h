@@ -80,7 +80,8 @@ enum bt_medium_kind {
 
 // CONST: p0=n p1=1/n p2=(n as a float-float pair) p3=(1/n as a pair).
 // TABLE: n entries, args at pool[off], vals at pool[off+n].
-// SELLMEIER: B1 B2 B3 C1 C2 C3.  SUMITA: A0..A5.
+// SELLMEIER: B1 B2 B3 C1 C2 C3 (and as float-float pairs at pool[off]).
+// SUMITA: A0..A5.
 // AIR: p0=P(mmHg) p1=T(C) p2=W(mmHg)
 typedef struct bt_medium {
     int32_t kind;
@@ -91,8 +92,8 @@ typedef struct bt_medium {
 } bt_medium;  // 64 bytes
 
 enum bt_obsc_op {
-    BT_O_CIRCLE = 0,     // p0=r p1=x0 p2=y0
-    BT_O_ANNULUS = 1,    // p0=inner p1=outer p2=x0 p3=y0
+    BT_O_CIRCLE = 0,     // p0=r p1=x0 p2=y0; p3..p5 the same as float-float pairs
+    BT_O_ANNULUS = 1,    // p0=inner p1=outer p2=x0 p3=y0; p4, p5 inner, outer as pairs
     BT_O_RECT = 2,       // p0=w p1=h p2=x0 p3=y0 p4=sin(th) p5=cos(th)
     BT_O_RAY = 3,        // p0=w p1=x0 p2=y0 p3=sin(th) p4=cos(th)
     BT_O_POLYGON = 4,    // n vertices, xs at pool[off], ys at pool[off+n]

@@ -38,6 +38,14 @@ struct MediumCacheF {
     ff n, inv_n;
 };
 
+// Float-float copies of a ray's x, y and direction from the stage that
+// produced them (valid while ok): the next stage reuses those its transform
+// leaves unchanged instead of converting the FP64 values again.
+struct RayCacheF {
+    bool ok;
+    ff x, y, vx, vy, vz;
+};
+
 // |a| < c for finite c > 0 on the integer pipe (false for NaN, as the
 // floating-point comparison).
 __device__ __forceinline__ bool d_abs_lt(double a, double c) {
@@ -145,7 +153,7 @@ __device__ __forceinline__ ff ffs_conic(const double* C, ff r2, ff* w_out) {
 // ffs_conic64), *zp the polynomial part, (ux, uy) the FP32 slope
 // (-dz/dx, -dz/dy) for the Newton derivative.
 __device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* pool, ff x, ff y, ff* zc, ff* zp,
-                                              float* ux, float* uy) {
+                                              float* ux, float* uy, bool fast = false) {
     const double* C = pool + s.ffc;
     *zp = ff{0.f, 0.f};
     switch (s.kind) {
@@ -176,7 +184,13 @@ __device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* po
         if (s.kind == BT_S_ASPHERE && s.n > 0) {
             const ff* c = ff_ptr(pool, s.off + 2 * s.n);
             const ff* dc = c + s.n;
-            *zp = ff_mul(ff_horner(r2, c, s.n), r2);
+            if (fast) {
+                float a = 0.f;
+                for (int i = s.n - 1; i >= 0; i--) a = fmaf(a, r2.hi, c[i].hi);
+                *zp = ff{a * r2.hi, 0.f};
+            } else {
+                *zp = ff_mul(ff_horner(r2, c, s.n), r2);
+            }
             float da = 0.f;
             for (int i = s.n - 1; i >= 0; i--) da = fmaf(da, r2.hi, dc[i].hi);
             kf += da;
@@ -191,7 +205,7 @@ __device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* po
         const int g = (nx - 1) * (ny - 1);
         const ff* c = ff_ptr(pool, s.off + nx * ny + 2 * g);
         *zc = ff{0.f, 0.f};
-        *zp = ff_horner2d(xx, yy, c, nx, ny);
+        *zp = fast ? ff{f_horner2d(xx.hi, yy.hi, c, nx, ny), 0.f} : ff_horner2d(xx, yy, c, nx, ny);
         *ux = -f_horner2d(xx.hi, yy.hi, c + nx * ny, nx - 1, ny - 1);
         *uy = -f_horner2d(xx.hi, yy.hi, c + nx * ny + g, nx - 1, ny - 1);
         return;
@@ -204,10 +218,14 @@ __device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* po
     }
 }
 
-__device__ __forceinline__ void ffs_eval(const Prog& P, int si, ff x, ff y, ff* zc, ff* zp, float* ux, float* uy) {
+// fast: polynomial parts (asphere terms, Zernike / Cartesian polynomials)
+// in FP32 -- ~1e-11 m for the largest asphere terms, enough for the
+// iterations that only bring the root close.
+__device__ __forceinline__ void ffs_eval(const Prog& P, int si, ff x, ff y, ff* zc, ff* zp, float* ux, float* uy,
+                                         bool fast = false) {
     const bt_surf& s = P.surfs[si];
     if (s.kind != BT_S_SUM) {
-        ffs_leaf_eval(s, P.pool, x, y, zc, zp, ux, uy);
+        ffs_leaf_eval(s, P.pool, x, y, zc, zp, ux, uy, fast);
         return;
     }
     ff c_acc{0.f, 0.f}, p_acc{0.f, 0.f};
@@ -217,7 +235,7 @@ __device__ __forceinline__ void ffs_eval(const Prog& P, int si, ff x, ff y, ff* 
         float cx, cy;
         const bt_surf& cs = P.surfs[s.m + c];
         if (cs.kind == BT_S_MODAL) ff_modal_eval(P, cs, x, y, &pz, &cx, &cy);
-        else ffs_leaf_eval(cs, P.pool, x, y, &cz, &pz, &cx, &cy);
+        else ffs_leaf_eval(cs, P.pool, x, y, &cz, &pz, &cx, &cy, fast);
         c_acc = ff_add(c_acc, cz);
         p_acc = ff_add(p_acc, pz);
         gx += cx;
@@ -329,22 +347,32 @@ __device__ __forceinline__ bool ff_analytic(const bt_surf& s, const double* pool
 }
 
 // Newton's tangent-plane iteration in float-float from dt, at most niter
-// corrections, stopping once a correction is below 1e-12 m.  Returns whether
-// it stopped that way; *zp and *inv_den hold the polynomial part of the sag
-// and 1/F' at the last evaluation (the point before the last correction).
+// corrections.  The first ones evaluate the polynomial parts in FP32 (fast)
+// until a correction falls below 1e-9 m; from then on (and always for the
+// last one) in float-float, stopping once a correction is below 1e-12 m.
+// Returns whether it stopped that way; *zp and *inv_den hold the
+// polynomial part of the sag and 1/F' at the last evaluation (the point
+// before the last correction).
 __device__ __forceinline__ bool ff_newton_iter(const Prog& P, int si, ff x, ff y, ff z, ff vx, ff vy, ff vz, ff* dt,
                                                int niter, ff* zp, float* inv_den) {
     const float fvx = vx.hi, fvy = vy.hi, fvz = vz.hi;
+    bool fast = true;
     for (int it = 0; it < niter; it++) {
+        if (it == niter - 1) fast = false;
         const ff px = ff_mad(vx, *dt, x), py = ff_mad(vy, *dt, y), pz = ff_mad(vz, *dt, z);
         ff zc;
         float ux, uy;
-        ffs_eval(P, si, px, py, &zc, zp, &ux, &uy);
+        ffs_eval(P, si, px, py, &zc, zp, &ux, &uy, fast);
         const ff res = ff_sub(ff_add(zc, *zp), pz);
         *inv_den = 1.f / fmaf(ux, fvx, fmaf(uy, fvy, fvz));
         const ff ddt = ff_mul_f(res, *inv_den);
         *dt = ff_add(*dt, ddt);
-        if (fabsf(ddt.hi) < 1e-12f) return true;
+        const float a = fabsf(ddt.hi);
+        if (fast) {
+            if (a < 1e-9f) fast = false;
+        } else if (a < 1e-12f) {
+            return true;
+        }
     }
     return false;
 }
@@ -575,11 +603,9 @@ __device__ __forceinline__ void ff_medium(const Prog& P, int mi, double w, ff* n
         const ff wf = d_to_ff(w);
         // 1e12 = 999999995904 + 4096, both exact floats
         const ff x = ff_mul(ff_sqr(wf), ff{999999995904.f, 4096.f});
+        const double* C = P.pool + m.off;  // B1..B3, C1..C3 as float-float pairs
         ff n2 = ff_one();
-        for (int i = 0; i < 3; i++) {
-            const ff B = d_to_ff(m.p[i]), Cc = d_to_ff(m.p[3 + i]);
-            n2 = ff_add(n2, ff_div(ff_mul(B, x), ff_sub(x, Cc)));
-        }
+        for (int i = 0; i < 3; i++) n2 = ff_add(n2, ff_div(ff_mul(ff_slot(C + i), x), ff_sub(x, ff_slot(C + 3 + i))));
         *n = ff_sqrt(n2);
         *inv_n = ff_div(ff_one(), *n);
         return;
@@ -594,9 +620,8 @@ __device__ __forceinline__ void ff_medium(const Prog& P, int mi, double w, ff* n
 // ---------------------------------------------------------------------------
 
 // hypot(dx, dy) < r decided from h^2 - r^2 in float-float unless within
-// 1e-13 relative of r^2; then *undecided.
-__device__ __forceinline__ bool ff_radius_less(ff dx, ff dy, double r, bool* undecided) {
-    const ff rf = d_to_ff(r);
+// 1e-13 relative of r^2; then *undecided.  rf: r as a float-float pair.
+__device__ __forceinline__ bool ff_radius_less(ff dx, ff dy, ff rf, double r, bool* undecided) {
     const ff r2 = ff_sqr(rf);
     const ff d = ff_sub(ff_r2(dx, dy), r2);
     const float thr = 1e-13f * r2.hi;
@@ -614,14 +639,19 @@ __device__ __forceinline__ bool ff_obsc_run(const Prog& P, int begin, int end, f
         const bt_obsc& o = P.obsc[k];
         bool v = false;
         if (o.op == BT_O_CIRCLE || o.op == BT_O_ANNULUS) {
-            const int c = (o.op == BT_O_CIRCLE) ? 1 : 2;  // index of the centre x in p[]
-            const ff dx = ff_sub(x, d_to_ff(o.p[c])), dy = ff_sub(y, d_to_ff(o.p[c + 1]));
+            // float-float copies packed by the host: CIRCLE p3..p5 = r, x0,
+            // y0; ANNULUS p4, p5 = inner, outer (centre converted if nonzero)
+            ff dx = x, dy = y;
             bool und = false;
             if (o.op == BT_O_CIRCLE) {
-                v = ff_radius_less(dx, dy, o.p[0], &und);
+                dx = ff_sub(x, ff_slot(&o.p[4]));
+                dy = ff_sub(y, ff_slot(&o.p[5]));
+                v = ff_radius_less(dx, dy, ff_slot(&o.p[3]), o.p[0], &und);
             } else {
-                const bool in_inner = ff_radius_less(dx, dy, o.p[0], &und);
-                const bool in_outer = ff_radius_less(dx, dy, o.p[1], &und);
+                if (d_nonzero(o.p[2])) dx = ff_sub(x, d_to_ff(o.p[2]));
+                if (d_nonzero(o.p[3])) dy = ff_sub(y, d_to_ff(o.p[3]));
+                const bool in_inner = ff_radius_less(dx, dy, ff_slot(&o.p[4]), o.p[0], &und);
+                const bool in_outer = ff_radius_less(dx, dy, ff_slot(&o.p[5]), o.p[1], &und);
                 v = !in_inner && in_outer;
             }
             if (und) v = bt_obsc_run(P, k, k + 1, xd, yd);
@@ -660,9 +690,10 @@ static __device__ __noinline__ void ff_stage_fp64(const Prog& P, const bt_stage&
 }
 
 __device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, RayState& r, int niter,
-                                             MediumCacheF& mc) {
+                                             MediumCacheF& mc, RayCacheF& fc) {
     if (st.kind == BT_ST_SCREEN || (st.kind != BT_ST_OBSCURE && !r.fail && !ffs_ok(P, st.surf))) {
         ff_stage_fp64(P, st, r, niter);
+        fc.ok = false;
         return;
     }
     ff fx, fy;  // float-float copy of the final (x, y), for the obscuration
@@ -684,8 +715,17 @@ __device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, 
             L.vyd = r.vx * st.drot[1] + r.vy * st.drot[4] + r.vz * st.drot[7];
             L.vzd = r.vx * st.drot[2] + r.vy * st.drot[5] + r.vz * st.drot[8];
         }
-        L.x = d_to_ff(L.xd); L.y = d_to_ff(L.yd); L.z = d_to_ff(L.zd);
-        L.vx = d_to_ff(L.vxd); L.vy = d_to_ff(L.vyd); L.vz = d_to_ff(L.vzd);
+        // float-float copies; those the transform leaves unchanged come from
+        // the previous stage
+        const bool same_v = fc.ok && st.identity != 0;
+        L.x = (same_v && !d_nonzero(st.dr[0])) ? fc.x : d_to_ff(L.xd);
+        L.y = (same_v && !d_nonzero(st.dr[1])) ? fc.y : d_to_ff(L.yd);
+        L.z = d_to_ff(L.zd);
+        if (same_v) {
+            L.vx = fc.vx; L.vy = fc.vy; L.vz = fc.vz;
+        } else {
+            L.vx = d_to_ff(L.vxd); L.vy = d_to_ff(L.vyd); L.vz = d_to_ff(L.vzd);
+        }
         const bt_surf& s = P.surfs[st.surf];
         bool ok;
         double dtd = 0.0;
@@ -704,6 +744,7 @@ __device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, 
             fx = d_to_ff(x);
             fy = d_to_ff(y);
             have_f = true;
+            fc.vx = L.vx; fc.vy = L.vy; fc.vz = L.vz;
             if (st.kind == BT_ST_INTERSECT) {
                 if (st.coated) r.f *= st.coat_t;
             } else {
@@ -713,9 +754,12 @@ __device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, 
                 if (st.kind == BT_ST_REFLECT) {
                     // src/batoid.cpp:343-353
                     const ff a2 = ff_mul_f(ff_dot3(wx, wy, wz, nx_, ny_, nz_), 2.f);
-                    vx = ff_to_d(ff_sub(wx, ff_mul(a2, nx_)));
-                    vy = ff_to_d(ff_sub(wy, ff_mul(a2, ny_)));
-                    vz = ff_to_d(ff_sub(wz, ff_mul(a2, nz_)));
+                    fc.vx = ff_sub(wx, ff_mul(a2, nx_));
+                    fc.vy = ff_sub(wy, ff_mul(a2, ny_));
+                    fc.vz = ff_sub(wz, ff_mul(a2, nz_));
+                    vx = ff_to_d(fc.vx);
+                    vy = ff_to_d(fc.vy);
+                    vz = ff_to_d(fc.vz);
                     if (st.coated) r.f *= st.coat_r;
                 } else {
                     // src/batoid.cpp:453-499
@@ -738,17 +782,25 @@ __device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, 
                         r.fail = true;
                         r.vig = true;
                     } else {
+                        // (eta v^ - (eta alpha + cos) n) / n2
                         const ff cosr = ff_sqrt(ff_sub(ff_one(), sinsqr));
-                        const ff nfactor = ff_add(ff_mul(eta, alpha), cosr);
-                        vx = ff_to_d(ff_mul(ff_sub(ff_mul(eta, nvx), ff_mul(nfactor, nx_)), mc.inv_n));
-                        vy = ff_to_d(ff_mul(ff_sub(ff_mul(eta, nvy), ff_mul(nfactor, ny_)), mc.inv_n));
-                        vz = ff_to_d(ff_mul(ff_sub(ff_mul(eta, nvz), ff_mul(nfactor, nz_)), mc.inv_n));
+                        const ff a = ff_mul(eta, mc.inv_n);
+                        const ff b = ff_mul(ff_add(ff_mul(eta, alpha), cosr), mc.inv_n);
+                        fc.vx = ff_sub(ff_mul(a, nvx), ff_mul(b, nx_));
+                        fc.vy = ff_sub(ff_mul(a, nvy), ff_mul(b, ny_));
+                        fc.vz = ff_sub(ff_mul(a, nvz), ff_mul(b, nz_));
+                        vx = ff_to_d(fc.vx);
+                        vy = ff_to_d(fc.vy);
+                        vz = ff_to_d(fc.vz);
                     }
                     if (st.coated) r.f *= st.coat_t;
                 }
             }
             r.x = x; r.y = y; r.z = z;
             r.vx = vx; r.vy = vy; r.vz = vz;
+            fc.x = fx;
+            fc.y = fy;
+            fc.ok = true;
         } else {
             r.fail = true;
             r.vig = true;
@@ -757,8 +809,8 @@ __device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, 
     if (st.obsc_end > st.obsc_begin) {
         // src/batoid.cpp:169-171: vignetted |= contains(x, y), for every ray
         if (!have_f) {
-            fx = d_to_ff(r.x);
-            fy = d_to_ff(r.y);
+            fx = fc.ok ? fc.x : d_to_ff(r.x);
+            fy = fc.ok ? fc.y : d_to_ff(r.y);
         }
         if (ff_obsc_run(P, st.obsc_begin, st.obsc_end, fx, fy, r.x, r.y)) r.vig = true;
     }

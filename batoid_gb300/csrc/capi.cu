@@ -344,6 +344,7 @@ extern "C" int bt_sellmeier_medium_create(double B1, double B2, double B3, doubl
     bt_medium_h* m = new_medium(BT_M_SELLMEIER);
     double p[6] = {B1, B2, B3, C1, C2, C3};
     memcpy(m->rec.p, p, sizeof(p));
+    for (double v : p) m->pool.push_back(ff_slot(v));  // float-float copies at pool[off]
     return make_out(out, m);
 }
 
@@ -384,12 +385,14 @@ static bt_obscuration* leaf_obsc(const bt_obsc& o) {
 extern "C" int bt_obsc_circle_create(double radius, double x0, double y0, bt_obscuration** out) {
     bt_obsc o = blank_op(BT_O_CIRCLE);
     o.p[0] = radius; o.p[1] = x0; o.p[2] = y0;
+    o.p[3] = ff_slot(radius); o.p[4] = ff_slot(x0); o.p[5] = ff_slot(y0);  // float-float copies
     return make_out(out, leaf_obsc(o));
 }
 
 extern "C" int bt_obsc_annulus_create(double inner, double outer, double x0, double y0, bt_obscuration** out) {
     bt_obsc o = blank_op(BT_O_ANNULUS);
     o.p[0] = inner; o.p[1] = outer; o.p[2] = x0; o.p[3] = y0;
+    o.p[4] = ff_slot(inner); o.p[5] = ff_slot(outer);  // float-float copies
     return make_out(out, leaf_obsc(o));
 }
 

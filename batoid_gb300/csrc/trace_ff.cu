@@ -59,9 +59,11 @@ k_trace_ff(const unsigned char* __restrict__ gblob, int blob_bytes, RV in, RV ou
         }
         MediumCacheF mc;
         mc.idx = -1;
+        RayCacheF fc;
+        fc.ok = false;
         for (int s = 0; s < P.nstages; s++) {
             if (act) {
-                run_stage_ff(P, P.stages[s], r, niter, mc);
+                run_stage_ff(P, P.stages[s], r, niter, mc, fc);
                 if (s < nsnaps) store_ray(snaps.s[s], i, r);
             }
             __syncthreads();
