@@ -181,6 +181,8 @@ _SIGS = [
     ("bt_mlp_adam", c_int, [_P, c_int, _P, ctypes.c_longlong, _P, _P, _P, ctypes.c_float, ctypes.c_float,
                             ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, c_int, c_int, _P, _P,
                             _P]),
+    ("bt_mlp_adam_dev", c_int, [_P, c_int, _P, ctypes.c_longlong, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float,
+                                ctypes.c_float, c_int, c_int, _P, _P, _P]),
     ("bt_surrogate_combine", c_int, [_P, c_int, c_int, _P, _P, _P, c_int, _P, c_double, c_int, c_int, _P, _P, c_int,
                                      _P]),
     ("bt_measure_fp64_peak", c_int, [c_int, c_double_p, _P]),

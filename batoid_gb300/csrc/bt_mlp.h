@@ -36,7 +36,8 @@ cudaError_t bt_launch_mlp_loss(const float* y, int ldy, const float* t, const fl
 cudaError_t bt_launch_mlp_colsum(const __nv_bfloat16* xt, int rows, int cols, float* out, cudaStream_t stream);
 cudaError_t bt_launch_mlp_adam(const float* partials, int nsplit, const float* grad_direct, long long n, float* w,
                                float* m, float* v, float lr, float b1, float b2, float eps, float bc1, float bc2,
-                               int rows, int cols, __nv_bfloat16* w16, __nv_bfloat16* w16t, cudaStream_t stream);
+                               int rows, int cols, __nv_bfloat16* w16, __nv_bfloat16* w16t, const float* hyper,
+                               cudaStream_t stream);
 cudaError_t bt_launch_surrogate_combine(const float* feat, int nfeat, int nlin, const int* grp, const float* theta,
                                         const float* y, int ldy, const double* wl, double scale, int J, int err_col,
                                         double* out, float* err_nm, int n, cudaStream_t stream);

@@ -1409,7 +1409,18 @@ extern "C" int bt_mlp_adam(const float* partials, int nsplit, const float* grad,
         !(bc2 > 0.f))
         return fail(BT_ERR_ARG, "mlp adam: bad arguments");
     CUDA_TRY(bt_launch_mlp_adam(partials, nsplit, grad, n, w, m, v, lr, b1, b2, eps, bc1, bc2, rows, cols,
-                                (__nv_bfloat16*)w16, (__nv_bfloat16*)w16t, (cudaStream_t)stream), "mlp adam");
+                                (__nv_bfloat16*)w16, (__nv_bfloat16*)w16t, nullptr, (cudaStream_t)stream), "mlp adam");
+    return BT_OK;
+}
+
+extern "C" int bt_mlp_adam_dev(const float* partials, int nsplit, const float* grad, long long n, float* w, float* m,
+                               float* v, const float* hyper, float b1, float b2, float eps, int rows, int cols,
+                               void* w16, void* w16t, void* stream) {
+    if (!w || !m || !v || !hyper || n < 1 || (nsplit > 0 && !partials) || (long long)rows * cols != n)
+        return fail(BT_ERR_ARG, "mlp adam (device schedule): bad arguments");
+    CUDA_TRY(bt_launch_mlp_adam(partials, nsplit, grad, n, w, m, v, 0.f, b1, b2, eps, 1.f, 1.f, rows, cols,
+                                (__nv_bfloat16*)w16, (__nv_bfloat16*)w16t, hyper, (cudaStream_t)stream),
+             "mlp adam (device schedule)");
     return BT_OK;
 }
 

@@ -611,10 +611,19 @@ __global__ void k_mlp_colsum(const __nv_bfloat16* __restrict__ xt, int cols, flo
 // Adam step on FP32 master weights from the sum of split-K partial gradients
 // (or a direct gradient), then the bf16 copies used by the GEMMs:
 // w16 [rows][cols] and, if given, w16t [cols][rows].
+// hyper (may be null): {lr, bc1, bc2} read from device memory instead of
+// the arguments, so that a captured training step follows a schedule
+// computed on the device.
 __global__ void k_mlp_adam(const float* __restrict__ partials, int nsplit, const float* __restrict__ gdir,
                            long long n, float* __restrict__ w, float* __restrict__ m, float* __restrict__ v, float lr,
                            float b1, float b2, float eps, float bc1, float bc2, int rows, int cols,
-                           __nv_bfloat16* __restrict__ w16, __nv_bfloat16* __restrict__ w16t) {
+                           __nv_bfloat16* __restrict__ w16, __nv_bfloat16* __restrict__ w16t,
+                           const float* __restrict__ hyper) {
+    if (hyper) {
+        lr = hyper[0];
+        bc1 = hyper[1];
+        bc2 = hyper[2];
+    }
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         float g = gdir ? gdir[i] : 0.f;
         for (int s = 0; s < nsplit; s++) g += partials[(size_t)s * n + i];
@@ -667,9 +676,10 @@ cudaError_t bt_launch_mlp_colsum(const __nv_bfloat16* xt, int rows, int cols, fl
 
 cudaError_t bt_launch_mlp_adam(const float* partials, int nsplit, const float* grad_direct, long long n, float* w,
                                float* m, float* v, float lr, float b1, float b2, float eps, float bc1, float bc2,
-                               int rows, int cols, __nv_bfloat16* w16, __nv_bfloat16* w16t, cudaStream_t stream) {
+                               int rows, int cols, __nv_bfloat16* w16, __nv_bfloat16* w16t, const float* hyper,
+                               cudaStream_t stream) {
     k_mlp_adam<<<mlp_grid(n), 256, 0, stream>>>(partials, nsplit, grad_direct, n, w, m, v, lr, b1, b2, eps, bc1, bc2,
-                                                rows, cols, w16, w16t);
+                                                rows, cols, w16, w16t, hyper);
     return cudaGetLastError();
 }
 

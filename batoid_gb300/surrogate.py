@@ -143,9 +143,20 @@ class MLP:
                 self._gemm(bf["dz"][l], self.W16t[l], B, i, o, 3, zs=bf["zs"][l - 1], h16=bf["dz"][l - 1],
                            h16t=bf["dzt"][l - 1])
 
-    def adam(self, bf, lr, b1=0.9, b2=0.999, eps=1e-8):
+    def adam(self, bf, lr, b1=0.9, b2=0.999, eps=1e-8, hyper=None):
+        """One Adam step.  hyper: optional device FP32 tensor {lr, bc1, bc2}
+        read by the kernels when they run (a captured step then follows a
+        schedule computed on the device); lr is ignored then."""
         L = _lib.lib()
         s = D.stream_ptr()
+        if hyper is not None:
+            for l, (o, i) in enumerate(self.shapes):
+                _lib.check(L.bt_mlp_adam_dev(_p(bf["ws"][l]), bf["splits"][l], None, o * i, _p(self.W[l]),
+                                             _p(self.mW[l]), _p(self.vW[l]), _p(hyper), b1, b2, eps, o, i,
+                                             _p(self.W16[l]), _p(self.W16t[l]), s))
+                _lib.check(L.bt_mlp_adam_dev(None, 0, _p(bf["db"][l]), o, _p(self.b[l]), _p(self.mb[l]),
+                                             _p(self.vb[l]), _p(hyper), b1, b2, eps, 1, o, None, None, s))
+            return
         self.step_count += 1
         bc1 = 1.0 - b1 ** self.step_count
         bc2 = 1.0 - b2 ** self.step_count
@@ -258,8 +269,14 @@ class WavefrontSurrogate:
         return r
 
     def train(self, feat, grp, w, coefs, epochs=30, batch=8192, lr=1e-3, lr_min=1e-5, err_weight=0.05, seed=0,
-              log=None):
-        """Fits the linear model, then trains the MLP on its residuals."""
+              log=None, graph=True):
+        """Fits the linear model, then trains the MLP on its residuals.
+
+        graph: each training step (minibatch gather, forward, loss,
+        backward, Adam with the cosine learning-rate schedule and bias
+        corrections computed on the device) is captured once in a CUDA
+        graph and replayed; the step's ~30 launches then cost one graph
+        launch.  graph=False issues them one by one (same arithmetic)."""
         self.fit_linear(feat, grp, coefs)
         r = self.residual_targets(feat, grp, w, coefs)
         self.scale = float(np.sqrt(np.mean(r ** 2)))
@@ -269,6 +286,9 @@ class WavefrontSurrogate:
         steps_per_epoch = n // batch
         total = epochs * steps_per_epoch
         rng = np.random.default_rng(seed)
+        if graph and steps_per_epoch > 0:
+            self._train_graph(x_all, t_all, epochs, steps_per_epoch, batch, lr, lr_min, err_weight, rng, log)
+            return
         step = 0
         for ep in range(epochs):
             perm = torch.from_numpy(rng.permutation(n)).to(D.device())
@@ -285,6 +305,62 @@ class WavefrontSurrogate:
             if log is not None:
                 torch.cuda.synchronize()
                 log(ep, float(bf["loss"][0].item()), float(bf["loss"][1].item()))
+        torch.cuda.synchronize()
+
+    def _train_graph(self, x_all, t_all, epochs, steps_per_epoch, batch, lr, lr_min, err_weight, rng, log,
+                     b1=0.9, b2=0.999):
+        net, dev = self.net, D.device()
+        n = x_all.shape[0]
+        total = epochs * steps_per_epoch
+        perm = torch.empty((steps_per_epoch, batch), dtype=torch.int64, device=dev)
+        k_in_epoch = torch.zeros(1, dtype=torch.int64, device=dev)
+        gstep = torch.zeros(1, dtype=torch.float64, device=dev)
+        hyper = torch.empty(3, dtype=torch.float32, device=dev)
+        xb = torch.empty((batch, x_all.shape[1]), dtype=torch.float32, device=dev)
+        tb = torch.empty((batch, t_all.shape[1]), dtype=torch.float32, device=dev)
+        b1t = torch.tensor(b1, dtype=torch.float64, device=dev)
+        b2t = torch.tensor(b2, dtype=torch.float64, device=dev)
+
+        def body():
+            idx = perm.index_select(0, k_in_epoch).view(-1)
+            torch.index_select(x_all, 0, idx, out=xb)
+            torch.index_select(t_all, 0, idx, out=tb)
+            bf = net.pack(xb, batch, True)
+            net.forward(bf, batch, True)
+            net.backward(bf, batch, tb, batch, err_col=self.J, err_weight=err_weight)
+            # cosine schedule and Adam bias corrections of step g (from 0)
+            cur = lr_min + 0.5 * (lr - lr_min) * (1.0 + torch.cos(np.pi * gstep / max(total, 1)))
+            sched = torch.cat([cur, 1.0 - torch.pow(b1t, gstep + 1), 1.0 - torch.pow(b2t, gstep + 1)])
+            hyper.copy_(sched.to(torch.float32))
+            net.adam(bf, 0.0, b1=b1, b2=b2, hyper=hyper)
+            k_in_epoch.add_(1)
+            gstep.add_(1)
+            return bf
+
+        stream = torch.cuda.Stream()
+        stream.wait_stream(torch.cuda.current_stream())
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(stream):
+            done = 0
+            for ep in range(epochs):
+                perm.copy_(torch.from_numpy(rng.permutation(n)[:steps_per_epoch * batch].reshape(steps_per_epoch,
+                                                                                                  batch)))
+                k_in_epoch.zero_()
+                for k in range(steps_per_epoch):
+                    if done == 0:
+                        bf = body()  # eager first step: buffers, kernel attributes
+                        stream.synchronize()
+                        with torch.cuda.graph(g, stream=stream):
+                            body()
+                        # the capture queued no work: undo nothing, count the eager step
+                    else:
+                        g.replay()
+                    done += 1
+                if log is not None:
+                    stream.synchronize()
+                    log(ep, float(bf["loss"][0].item()), float(bf["loss"][1].item()))
+        net.step_count += done
+        torch.cuda.current_stream().wait_stream(stream)
         torch.cuda.synchronize()
 
     # -- inference ------------------------------------------------------------------------

@@ -413,6 +413,12 @@ int bt_mlp_colsum(const void* xt, int rows, int cols, float* out, void* stream);
 int bt_mlp_adam(const float* partials, int nsplit, const float* grad, long long n, float* w, float* m, float* v,
                 float lr, float b1, float b2, float eps, float bc1, float bc2, int rows, int cols, void* w16,
                 void* w16t, void* stream);
+/* bt_mlp_adam with {lr, bc1, bc2} read from the device array hyper[3] when
+ * the kernel runs, so that a training step captured in a CUDA graph follows
+ * a learning-rate schedule and bias corrections computed on the device. */
+int bt_mlp_adam_dev(const float* partials, int nsplit, const float* grad, long long n, float* w, float* m, float* v,
+                    const float* hyper, float b1, float b2, float eps, int rows, int cols, void* w16, void* w16t,
+                    void* stream);
 
 /* Surrogate output assembly: for sample s in group grp[s], Zernike
  * coefficients out[s][0..J] (waves; entry 0 = 0) = linear model

@@ -90,3 +90,31 @@ def test_combine_linear_model_matches_fp64(trained):
     assert np.all(got[:, 0] == 0.0)
     scale = np.abs(want).max()
     np.testing.assert_allclose(got[:, 1:], want, rtol=0, atol=1e-12 * scale)
+
+
+def test_graph_captured_training_matches_launch_by_launch():
+    """A training run whose steps are replayed from one captured CUDA graph
+    (device-side minibatch gather, learning-rate schedule and Adam bias
+    corrections) ends at the weights of the same run issued launch by
+    launch, to float32 rounding."""
+    import torch
+    from batoid_gb300 import _device as D
+    rng = np.random.default_rng(11)
+    n, nd = 4096, 7
+    feat = rng.uniform(-1, 1, (n, nd + 3)).astype(np.float32)
+    grp = np.zeros(n, dtype=np.int32)
+    w = np.full(n, 600e-9)
+
+    class _PT:
+        ndof, nmodes, jmax = nd, 2, 5
+        rigid = [0]
+        fields = np.zeros((1, 2))
+    coefs = np.concatenate([np.zeros((n, 1)), np.sin(feat[:, :5] * 3.0) * 1e-2], axis=1)
+    runs = []
+    for graph in (True, False):
+        sur = WavefrontSurrogate(_PT(), wavelengths=[600e-9], nx=16, hidden=256, layers=2, seed=3)
+        sur.F = 1
+        sur.train(feat, grp, w, coefs, epochs=3, batch=1024, lr=2e-3, seed=5, graph=graph)
+        runs.append([D.to_host(x) for x in sur.net.W])
+    for a, b in zip(*runs):
+        np.testing.assert_allclose(a, b, rtol=1e-4, atol=1e-6 * np.abs(b).max())
