@@ -153,7 +153,7 @@ __device__ __forceinline__ ff ffs_conic(const double* C, ff r2, ff* w_out) {
 // ffs_conic64), *zp the polynomial part, (ux, uy) the FP32 slope
 // (-dz/dx, -dz/dy) for the Newton derivative.
 __device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* pool, ff x, ff y, ff* zc, ff* zp,
-                                              float* ux, float* uy, bool fast = false) {
+                                              float* ux, float* uy) {
     const double* C = pool + s.ffc;
     *zp = ff{0.f, 0.f};
     switch (s.kind) {
@@ -184,13 +184,7 @@ __device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* po
         if (s.kind == BT_S_ASPHERE && s.n > 0) {
             const ff* c = ff_ptr(pool, s.off + 2 * s.n);
             const ff* dc = c + s.n;
-            if (fast) {
-                float a = 0.f;
-                for (int i = s.n - 1; i >= 0; i--) a = fmaf(a, r2.hi, c[i].hi);
-                *zp = ff{a * r2.hi, 0.f};
-            } else {
-                *zp = ff_mul(ff_horner(r2, c, s.n), r2);
-            }
+            *zp = ff_mul(ff_horner(r2, c, s.n), r2);
             float da = 0.f;
             for (int i = s.n - 1; i >= 0; i--) da = fmaf(da, r2.hi, dc[i].hi);
             kf += da;
@@ -205,7 +199,7 @@ __device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* po
         const int g = (nx - 1) * (ny - 1);
         const ff* c = ff_ptr(pool, s.off + nx * ny + 2 * g);
         *zc = ff{0.f, 0.f};
-        *zp = fast ? ff{f_horner2d(xx.hi, yy.hi, c, nx, ny), 0.f} : ff_horner2d(xx, yy, c, nx, ny);
+        *zp = ff_horner2d(xx, yy, c, nx, ny);
         *ux = -f_horner2d(xx.hi, yy.hi, c + nx * ny, nx - 1, ny - 1);
         *uy = -f_horner2d(xx.hi, yy.hi, c + nx * ny + g, nx - 1, ny - 1);
         return;
@@ -218,14 +212,10 @@ __device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* po
     }
 }
 
-// fast: polynomial parts (asphere terms, Zernike / Cartesian polynomials)
-// in FP32 -- ~1e-11 m for the largest asphere terms, enough for the
-// iterations that only bring the root close.
-__device__ __forceinline__ void ffs_eval(const Prog& P, int si, ff x, ff y, ff* zc, ff* zp, float* ux, float* uy,
-                                         bool fast = false) {
+__device__ __forceinline__ void ffs_eval(const Prog& P, int si, ff x, ff y, ff* zc, ff* zp, float* ux, float* uy) {
     const bt_surf& s = P.surfs[si];
     if (s.kind != BT_S_SUM) {
-        ffs_leaf_eval(s, P.pool, x, y, zc, zp, ux, uy, fast);
+        ffs_leaf_eval(s, P.pool, x, y, zc, zp, ux, uy);
         return;
     }
     ff c_acc{0.f, 0.f}, p_acc{0.f, 0.f};
@@ -235,7 +225,7 @@ __device__ __forceinline__ void ffs_eval(const Prog& P, int si, ff x, ff y, ff* 
         float cx, cy;
         const bt_surf& cs = P.surfs[s.m + c];
         if (cs.kind == BT_S_MODAL) ff_modal_eval(P, cs, x, y, &pz, &cx, &cy);
-        else ffs_leaf_eval(cs, P.pool, x, y, &cz, &pz, &cx, &cy, fast);
+        else ffs_leaf_eval(cs, P.pool, x, y, &cz, &pz, &cx, &cy);
         c_acc = ff_add(c_acc, cz);
         p_acc = ff_add(p_acc, pz);
         gx += cx;
@@ -347,32 +337,26 @@ __device__ __forceinline__ bool ff_analytic(const bt_surf& s, const double* pool
 }
 
 // Newton's tangent-plane iteration in float-float from dt, at most niter
-// corrections.  The first ones evaluate the polynomial parts in FP32 (fast)
-// until a correction falls below 1e-9 m; from then on (and always for the
-// last one) in float-float, stopping once a correction is below 1e-12 m.
-// Returns whether it stopped that way; *zp and *inv_den hold the
-// polynomial part of the sag and 1/F' at the last evaluation (the point
-// before the last correction).
+// corrections, stopping once a correction is below 1e-12 m.  Returns whether
+// it stopped that way; *zp and *inv_den hold the polynomial part of the sag
+// and 1/F' at the last evaluation (the point before the last correction).
+// (Evaluating the polynomial terms in FP32 during the first iterations was
+// measured at half the throughput: FP32 rounding of the cancelling terms of
+// the Cartesian Zernike arrays keeps the corrections above any useful
+// switch-over threshold, so the iterations run out.)
 __device__ __forceinline__ bool ff_newton_iter(const Prog& P, int si, ff x, ff y, ff z, ff vx, ff vy, ff vz, ff* dt,
                                                int niter, ff* zp, float* inv_den) {
     const float fvx = vx.hi, fvy = vy.hi, fvz = vz.hi;
-    bool fast = true;
     for (int it = 0; it < niter; it++) {
-        if (it == niter - 1) fast = false;
         const ff px = ff_mad(vx, *dt, x), py = ff_mad(vy, *dt, y), pz = ff_mad(vz, *dt, z);
         ff zc;
         float ux, uy;
-        ffs_eval(P, si, px, py, &zc, zp, &ux, &uy, fast);
+        ffs_eval(P, si, px, py, &zc, zp, &ux, &uy);
         const ff res = ff_sub(ff_add(zc, *zp), pz);
         *inv_den = 1.f / fmaf(ux, fvx, fmaf(uy, fvy, fvz));
         const ff ddt = ff_mul_f(res, *inv_den);
         *dt = ff_add(*dt, ddt);
-        const float a = fabsf(ddt.hi);
-        if (fast) {
-            if (a < 1e-9f) fast = false;
-        } else if (a < 1e-12f) {
-            return true;
-        }
+        if (fabsf(ddt.hi) < 1e-12f) return true;
     }
     return false;
 }
