@@ -152,8 +152,17 @@ __device__ __forceinline__ ff ffs_conic(const double* C, ff r2, ff* w_out) {
 // Leaf sag at (x, y): *zc the conic part (recomputed in FP64 by
 // ffs_conic64), *zp the polynomial part, (ux, uy) the FP32 slope
 // (-dz/dx, -dz/dy) for the Newton derivative.
-__device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* pool, ff x, ff y, ff* zc, ff* zp,
-                                              float* ux, float* uy) {
+struct SagF {
+    ff zc, zp;
+    float ux, uy;
+};
+
+static __device__ __noinline__ SagF ffs_leaf_eval_o(const bt_surf& s, const double* pool, ff x, ff y) {
+    SagF o;
+    ff* zc = &o.zc;
+    ff* zp = &o.zp;
+    float* ux = &o.ux;
+    float* uy = &o.uy;
     const double* C = pool + s.ffc;
     *zp = ff{0.f, 0.f};
     switch (s.kind) {
@@ -166,14 +175,14 @@ __device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* po
         const float k = rsqrtf(w.hi) * ff_slot(C + 2).hi;
         *ux = -x.hi * k;
         *uy = -y.hi * k;
-        return;
+        return o;
     }
     case BT_S_PARABOLOID: {
         *zc = ff_mul(ff_r2(x, y), ff_slot(C + 2));
         const float k = ff_slot(C + 1).hi;
         *ux = -x.hi * k;
         *uy = -y.hi * k;
-        return;
+        return o;
     }
     case BT_S_QUADRIC:
     case BT_S_ASPHERE: {
@@ -191,7 +200,7 @@ __device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* po
         }
         *ux = -x.hi * kf;
         *uy = -y.hi * kf;
-        return;
+        return o;
     }
     case BT_S_POLY: {
         const ff xx = ff_sub(x, ff_slot(C + 0)), yy = ff_sub(y, ff_slot(C + 1));
@@ -202,14 +211,25 @@ __device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* po
         *zp = ff_horner2d(xx, yy, c, nx, ny);
         *ux = -f_horner2d(xx.hi, yy.hi, c + nx * ny, nx - 1, ny - 1);
         *uy = -f_horner2d(xx.hi, yy.hi, c + nx * ny + g, nx - 1, ny - 1);
-        return;
+        return o;
     }
     default:  // plane
         *zc = ff{0.f, 0.f};
         *ux = 0.f;
         *uy = 0.f;
-        return;
+        return o;
     }
+}
+
+// Out of line (one copy of the code for every caller): the fully inlined
+// float-float form missed in the instruction cache on most issues.
+__device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* pool, ff x, ff y, ff* zc, ff* zp,
+                                              float* ux, float* uy) {
+    const SagF o = ffs_leaf_eval_o(s, pool, x, y);
+    *zc = o.zc;
+    *zp = o.zp;
+    *ux = o.ux;
+    *uy = o.uy;
 }
 
 __device__ __forceinline__ void ffs_eval(const Prog& P, int si, ff x, ff y, ff* zc, ff* zp, float* ux, float* uy) {
@@ -281,7 +301,15 @@ __device__ __forceinline__ bool ff_one_root(ff a, ff b, ff c, bool plus, ff* t) 
 }
 
 // Conic root with the smaller |z| (src/quadric.cpp:41-71).
-__device__ __forceinline__ bool ff_quadric_root(const double* C, ff x, ff y, ff z, ff vx, ff vy, ff vz, ff* dt) {
+struct RootF {
+    ff dt;
+    bool ok;
+};
+
+static __device__ __noinline__ RootF ff_quadric_root_o(const double* C, ff x, ff y, ff z, ff vx, ff vy, ff vz) {
+    RootF o;
+    o.ok = false;
+    ff* dt = &o.dt;
     const ff icp1 = ff_slot(C + 1);
     const ff z0 = ff_sub(z, ff_slot(C + 2));
     const ff vrr0 = ff_add(ff_mul(vx, x), ff_mul(vy, y));
@@ -289,19 +317,26 @@ __device__ __forceinline__ bool ff_quadric_root(const double* C, ff x, ff y, ff 
     const ff b = ff_mul_f(ff_add(ff_mul(vz, z0), ff_mul(vrr0, icp1)), 2.f);
     const ff c = ff_add(ff_sub(ff_sqr(z0), ff_slot(C + 3)), ff_mul(ff_r2(x, y), icp1));
     const ff disc = ff_sub(ff_sqr(b), ff_mul_f(ff_mul(a, c), 4.f));
-    if (disc.hi < 0.f) return false;
+    if (disc.hi < 0.f) return o;
     const ff s = ff_sqrt(disc);
     const ff mb = ff_neg(b);
     const ff r1 = (b.hi > 0.f) ? ff_div(ff_sub(mb, s), ff_mul_f(a, 2.f)) : ff_div(ff_mul_f(c, 2.f), ff_add(mb, s));
     const ff r2 = ff_div(c, ff_mul(a, r1));
     const ff z1 = ff_mad(vz, r1, z), z2 = ff_mad(vz, r2, z);
     *dt = ff_lt(ff_abs(z1), ff_abs(z2)) ? r1 : r2;
-    return true;
+    o.ok = true;
+    return o;
+}
+
+__device__ __forceinline__ bool ff_quadric_root(const double* C, ff x, ff y, ff z, ff vx, ff vy, ff vz, ff* dt) {
+    const RootF o = ff_quadric_root_o(C, x, y, z, vx, vy, vz);
+    *dt = o.dt;
+    return o.ok;
 }
 
 // Analytic time to intersect of PLANE / SPHERE / PARABOLOID / QUADRIC.
-__device__ __forceinline__ bool ff_analytic(const bt_surf& s, const double* pool, ff x, ff y, ff z, ff vx, ff vy,
-                                            ff vz, ff* dt) {
+__device__ __forceinline__ bool ff_analytic_in(const bt_surf& s, const double* pool, ff x, ff y, ff z, ff vx, ff vy,
+                                               ff vz, ff* dt) {
     const double* C = pool + s.ffc;
     switch (s.kind) {
     case BT_S_PLANE:
@@ -336,6 +371,21 @@ __device__ __forceinline__ bool ff_analytic(const bt_surf& s, const double* pool
     }
 }
 
+static __device__ __noinline__ RootF ff_analytic_o(const bt_surf& s, const double* pool, ff x, ff y, ff z, ff vx,
+                                                   ff vy, ff vz) {
+    RootF o;
+    o.ok = ff_analytic_in(s, pool, x, y, z, vx, vy, vz, &o.dt);
+    return o;
+}
+
+__device__ __forceinline__ bool ff_analytic(const bt_surf& s, const double* pool, ff x, ff y, ff z, ff vx, ff vy,
+                                            ff vz, ff* dt) {
+    const RootF o = ff_analytic_o(s, pool, x, y, z, vx, vy, vz);
+    *dt = o.dt;
+    return o.ok;
+}
+
+
 // Newton's tangent-plane iteration in float-float from dt, at most niter
 // corrections, stopping once a correction is below 1e-12 m.  Returns whether
 // it stopped that way; *zp and *inv_den hold the polynomial part of the sag
@@ -344,8 +394,8 @@ __device__ __forceinline__ bool ff_analytic(const bt_surf& s, const double* pool
 // measured at half the throughput: FP32 rounding of the cancelling terms of
 // the Cartesian Zernike arrays keeps the corrections above any useful
 // switch-over threshold, so the iterations run out.)
-__device__ __forceinline__ bool ff_newton_iter(const Prog& P, int si, ff x, ff y, ff z, ff vx, ff vy, ff vz, ff* dt,
-                                               int niter, ff* zp, float* inv_den) {
+__device__ __forceinline__ bool ff_newton_iter_in(const Prog& P, int si, ff x, ff y, ff z, ff vx, ff vy, ff vz,
+                                                  ff* dt, int niter, ff* zp, float* inv_den) {
     const float fvx = vx.hi, fvy = vy.hi, fvz = vz.hi;
     for (int it = 0; it < niter; it++) {
         const ff px = ff_mad(vx, *dt, x), py = ff_mad(vy, *dt, y), pz = ff_mad(vz, *dt, z);
@@ -360,6 +410,32 @@ __device__ __forceinline__ bool ff_newton_iter(const Prog& P, int si, ff x, ff y
     }
     return false;
 }
+
+struct NewtonF {
+    ff dt, zp;
+    float inv_den;
+    bool conv;
+};
+
+static __device__ __noinline__ NewtonF ff_newton_iter_o(const Prog& P, int si, ff x, ff y, ff z, ff vx, ff vy,
+                                                       ff vz, ff dt0, int niter) {
+    NewtonF o;
+    o.dt = dt0;
+    o.zp = ff{0.f, 0.f};
+    o.inv_den = 0.f;
+    o.conv = ff_newton_iter_in(P, si, x, y, z, vx, vy, vz, &o.dt, niter, &o.zp, &o.inv_den);
+    return o;
+}
+
+__device__ __forceinline__ bool ff_newton_iter(const Prog& P, int si, ff x, ff y, ff z, ff vx, ff vy, ff vz, ff* dt,
+                                               int niter, ff* zp, float* inv_den) {
+    const NewtonF o = ff_newton_iter_o(P, si, x, y, z, vx, vy, vz, *dt, niter);
+    *dt = o.dt;
+    *zp = o.zp;
+    *inv_den = o.inv_den;
+    return o.conv;
+}
+
 
 // Residual of surface si at dt in float-float (for a first child's success
 // test, as the reference's |sag - z| < 1e-12 at its final point).
@@ -486,7 +562,14 @@ __device__ __forceinline__ bool ffs_needs_refine(const bt_surf& s) {
 // ---------------------------------------------------------------------------
 
 // Slope (ux, uy) = (nx/nz, ny/nz) of a leaf at (x, y), float-float.
-__device__ __forceinline__ void ffs_leaf_slope(const bt_surf& s, const double* pool, ff x, ff y, ff* ux, ff* uy) {
+struct SlopeF {
+    ff ux, uy;
+};
+
+static __device__ __noinline__ SlopeF ffs_leaf_slope_o(const bt_surf& s, const double* pool, ff x, ff y) {
+    SlopeF o;
+    ff* ux = &o.ux;
+    ff* uy = &o.uy;
     const double* C = pool + s.ffc;
     switch (s.kind) {
     case BT_S_SPHERE: {
@@ -494,13 +577,13 @@ __device__ __forceinline__ void ffs_leaf_slope(const bt_surf& s, const double* p
         const ff k = ff_mul(ff_slot(C + 2), ff_rsqrt(w));
         *ux = ff_neg(ff_mul(x, k));
         *uy = ff_neg(ff_mul(y, k));
-        return;
+        return o;
     }
     case BT_S_PARABOLOID: {
         const ff k = ff_slot(C + 1);
         *ux = ff_neg(ff_mul(x, k));
         *uy = ff_neg(ff_mul(y, k));
-        return;
+        return o;
     }
     case BT_S_QUADRIC:
     case BT_S_ASPHERE: {
@@ -510,7 +593,7 @@ __device__ __forceinline__ void ffs_leaf_slope(const bt_surf& s, const double* p
         if (s.kind == BT_S_ASPHERE && s.n > 0) k = ff_add(k, ff_horner(r2, ff_ptr(pool, s.off + 3 * s.n), s.n));
         *ux = ff_neg(ff_mul(x, k));
         *uy = ff_neg(ff_mul(y, k));
-        return;
+        return o;
     }
     case BT_S_POLY: {
         const int nx = s.n, ny = s.m;
@@ -519,17 +602,42 @@ __device__ __forceinline__ void ffs_leaf_slope(const bt_surf& s, const double* p
         const ff xx = ff_sub(x, ff_slot(C + 0)), yy = ff_sub(y, ff_slot(C + 1));
         *ux = ff_neg(ff_horner2d(xx, yy, c + nx * ny, nx - 1, ny - 1));
         *uy = ff_neg(ff_horner2d(xx, yy, c + nx * ny + g, nx - 1, ny - 1));
-        return;
+        return o;
     }
     default:
         *ux = ff{0.f, 0.f};
         *uy = ff{0.f, 0.f};
-        return;
+        return o;
     }
 }
 
+__device__ __forceinline__ void ffs_leaf_slope(const bt_surf& s, const double* pool, ff x, ff y, ff* ux, ff* uy) {
+    const SlopeF o = ffs_leaf_slope_o(s, pool, x, y);
+    *ux = o.ux;
+    *uy = o.uy;
+}
+
 // Unit normal at (x, y) with the reference's conventions (bt_normal_precise).
+struct Vec3F {
+    ff x, y, z;
+};
+
+__device__ __forceinline__ void ffs_normal_in(const Prog& P, int si, ff x, ff y, ff* nx, ff* ny, ff* nz);
+
+static __device__ __noinline__ Vec3F ffs_normal_o(const Prog& P, int si, ff x, ff y) {
+    Vec3F o;
+    ffs_normal_in(P, si, x, y, &o.x, &o.y, &o.z);
+    return o;
+}
+
 __device__ __forceinline__ void ffs_normal(const Prog& P, int si, ff x, ff y, ff* nx, ff* ny, ff* nz) {
+    const Vec3F o = ffs_normal_o(P, si, x, y);
+    *nx = o.x;
+    *ny = o.y;
+    *nz = o.z;
+}
+
+__device__ __forceinline__ void ffs_normal_in(const Prog& P, int si, ff x, ff y, ff* nx, ff* ny, ff* nz) {
     const bt_surf& s = P.surfs[si];
     if (s.kind == BT_S_PLANE) {
         *nx = ff{0.f, 0.f}; *ny = ff{0.f, 0.f}; *nz = ff_one();
@@ -575,7 +683,7 @@ __device__ __forceinline__ ff ff_dot3(ff ax, ff ay, ff az, ff bx, ff by, ff bz) 
 }
 
 // Refractive index and its reciprocal in float-float (src/medium.cpp).
-__device__ __forceinline__ void ff_medium(const Prog& P, int mi, double w, ff* n, ff* inv_n) {
+static __device__ __noinline__ void ff_medium(const Prog& P, int mi, double w, ff* n, ff* inv_n) {
     const bt_medium& m = P.media[mi];
     if (m.kind == BT_M_CONST) {
         *n = ff_slot(&m.p[2]);
@@ -615,8 +723,8 @@ __device__ __forceinline__ bool ff_radius_less(ff dx, ff dy, ff rf, double r, bo
     return false;
 }
 
-__device__ __forceinline__ bool ff_obsc_run(const Prog& P, int begin, int end, ff x, ff y, double xd,
-                                            double yd) {
+static __device__ __noinline__ bool ff_obsc_run(const Prog& P, int begin, int end, ff x, ff y, double xd,
+                                                double yd) {
     uint32_t stack = 0;
     int sp = 0;
     for (int k = begin; k < end; k++) {
