@@ -38,7 +38,9 @@ enum bt_surf_kind {
 //              p9=1/R (0 if R == 0) p10=1 if the sag may use (1-q)*R/(conic+1)
 //              ASPHERE: n coefs at pool[off], n dz/dr coefs at pool[off+n],
 //              then both again as float-float pairs (one double slot each)
-//  POLY:       p0=xorigin p1=yorigin; n=xsize m=ysize;
+//  POLY:       p0=xorigin p1=yorigin p2=1 if triangular (square, coefficients
+//              with i + j >= size zero, also in the gradient arrays);
+//              n=xsize m=ysize;
 //              coefs pool[off .. off+n*m), gradx then grady ((n-1)*(m-1) each),
 //              then the three arrays again as float-float pairs
 //  BICUBIC:    p0=x0 p1=y0 p2=dx p3=dy p4=use_nan; n=nx m=ny; tab = 4 arrays

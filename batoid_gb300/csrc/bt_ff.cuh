@@ -67,6 +67,26 @@ __device__ __forceinline__ ff ff_horner2d(ff x, ff y, const ff* c, int nx, int n
     return r;
 }
 
+// The same over a triangular array (square, K = nx = ny, every coefficient
+// with i + j >= K zero, as the Cartesian form of a Zernike sum): row i is
+// evaluated over its K - i leading columns only.  The skipped terms are
+// exact zeros, so the value is the full Horner's.
+__device__ __forceinline__ ff ff_horner2d_tri(ff x, ff y, const ff* c, int K) {
+    ff r{0.f, 0.f};
+    for (int i = K - 1; i >= 0; i--) r = ff_fma(r, x, ff_horner(y, c + i * K, K - i));
+    return r;
+}
+
+__device__ __forceinline__ float f_horner2d_tri(float x, float y, const ff* c, int K) {
+    float r = 0.f;
+    for (int i = K - 1; i >= 0; i--) {
+        float row = 0.f;
+        for (int j = K - 1 - i; j >= 0; j--) row = fmaf(row, y, c[i * K + j].hi);
+        r = fmaf(r, x, row);
+    }
+    return r;
+}
+
 // Plain FP32 Horner on the high parts (for Newton derivatives).
 __device__ __forceinline__ float f_horner2d(float x, float y, const ff* c, int nx, int ny) {
     float r = 0.f;

@@ -208,9 +208,15 @@ static __device__ __noinline__ SagF ffs_leaf_eval_o(const bt_surf& s, const doub
         const int g = (nx - 1) * (ny - 1);
         const ff* c = ff_ptr(pool, s.off + nx * ny + 2 * g);
         *zc = ff{0.f, 0.f};
-        *zp = ff_horner2d(xx, yy, c, nx, ny);
-        *ux = -f_horner2d(xx.hi, yy.hi, c + nx * ny, nx - 1, ny - 1);
-        *uy = -f_horner2d(xx.hi, yy.hi, c + nx * ny + g, nx - 1, ny - 1);
+        if (d_nonzero(s.p[2])) {  // triangular arrays (Zernike sums)
+            *zp = ff_horner2d_tri(xx, yy, c, nx);
+            *ux = -f_horner2d_tri(xx.hi, yy.hi, c + nx * ny, nx - 1);
+            *uy = -f_horner2d_tri(xx.hi, yy.hi, c + nx * ny + g, nx - 1);
+        } else {
+            *zp = ff_horner2d(xx, yy, c, nx, ny);
+            *ux = -f_horner2d(xx.hi, yy.hi, c + nx * ny, nx - 1, ny - 1);
+            *uy = -f_horner2d(xx.hi, yy.hi, c + nx * ny + g, nx - 1, ny - 1);
+        }
         return o;
     }
     default:  // plane
@@ -600,8 +606,13 @@ static __device__ __noinline__ SlopeF ffs_leaf_slope_o(const bt_surf& s, const d
         const int g = (nx - 1) * (ny - 1);
         const ff* c = ff_ptr(pool, s.off + nx * ny + 2 * g);
         const ff xx = ff_sub(x, ff_slot(C + 0)), yy = ff_sub(y, ff_slot(C + 1));
-        *ux = ff_neg(ff_horner2d(xx, yy, c + nx * ny, nx - 1, ny - 1));
-        *uy = ff_neg(ff_horner2d(xx, yy, c + nx * ny + g, nx - 1, ny - 1));
+        if (d_nonzero(s.p[2])) {
+            *ux = ff_neg(ff_horner2d_tri(xx, yy, c + nx * ny, nx - 1));
+            *uy = ff_neg(ff_horner2d_tri(xx, yy, c + nx * ny + g, nx - 1));
+        } else {
+            *ux = ff_neg(ff_horner2d(xx, yy, c + nx * ny, nx - 1, ny - 1));
+            *uy = ff_neg(ff_horner2d(xx, yy, c + nx * ny + g, nx - 1, ny - 1));
+        }
         return o;
     }
     default:

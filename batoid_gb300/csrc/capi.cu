@@ -250,6 +250,17 @@ extern "C" int bt_polynomial_create(const double* coefs, const double* gradx, co
     }
     append_ff(s->pool, 0, xsize * ysize + 2 * gsz);
     push_ffc(s, r, {xorigin, yorigin});
+    // p2 = 1: square arrays whose coefficients with i + j >= K are zero (the
+    // Cartesian form of a Zernike sum); the trace then skips those terms
+    bool tri = xsize == ysize && xsize >= 2;
+    for (size_t i = 0; tri && i < ysize; i++)
+        for (size_t j = 0; j < xsize; j++) {
+            if (i + j >= xsize && coefs[i * xsize + j] != 0.0) tri = false;
+            if (i < ysize - 1 && j < xsize - 1 && i + j >= xsize - 1 &&
+                (gradx[i * (xsize - 1) + j] != 0.0 || grady[i * (xsize - 1) + j] != 0.0))
+                tri = false;
+        }
+    r.p[2] = tri ? 1.0 : 0.0;
     push_rec(s, r);
     return make_out(out, s);
 }
