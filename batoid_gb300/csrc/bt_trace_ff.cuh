@@ -154,7 +154,8 @@ __device__ __forceinline__ ff ffs_conic(const double* C, ff r2, ff* w_out) {
 // (-dz/dx, -dz/dy) for the Newton derivative.
 struct SagF {
     ff zc, zp;
-    float ux, uy;
+    float ux, uy;  // slope (-dz/dx, -dz/dy) of the whole sag, FP32
+    float px, py;  // the same for the polynomial part zp alone
 };
 
 static __device__ __noinline__ SagF ffs_leaf_eval_o(const bt_surf& s, const double* pool, ff x, ff y) {
@@ -165,6 +166,8 @@ static __device__ __noinline__ SagF ffs_leaf_eval_o(const bt_surf& s, const doub
     float* uy = &o.uy;
     const double* C = pool + s.ffc;
     *zp = ff{0.f, 0.f};
+    o.px = 0.f;
+    o.py = 0.f;
     switch (s.kind) {
     case BT_S_SPHERE: {
         // R (1 - q) = r^2 / (R (1 + q)), q = sqrt(1 - r^2/R^2), in the form
@@ -197,6 +200,8 @@ static __device__ __noinline__ SagF ffs_leaf_eval_o(const bt_surf& s, const doub
             float da = 0.f;
             for (int i = s.n - 1; i >= 0; i--) da = fmaf(da, r2.hi, dc[i].hi);
             kf += da;
+            o.px = -x.hi * da;
+            o.py = -y.hi * da;
         }
         *ux = -x.hi * kf;
         *uy = -y.hi * kf;
@@ -217,6 +222,8 @@ static __device__ __noinline__ SagF ffs_leaf_eval_o(const bt_surf& s, const doub
             *ux = -f_horner2d(xx.hi, yy.hi, c + nx * ny, nx - 1, ny - 1);
             *uy = -f_horner2d(xx.hi, yy.hi, c + nx * ny + g, nx - 1, ny - 1);
         }
+        o.px = *ux;
+        o.py = *uy;
         return o;
     }
     default:  // plane
@@ -230,37 +237,54 @@ static __device__ __noinline__ SagF ffs_leaf_eval_o(const bt_surf& s, const doub
 // Out of line (one copy of the code for every caller): the fully inlined
 // float-float form missed in the instruction cache on most issues.
 __device__ __forceinline__ void ffs_leaf_eval(const bt_surf& s, const double* pool, ff x, ff y, ff* zc, ff* zp,
-                                              float* ux, float* uy) {
+                                              float* ux, float* uy, float* px = nullptr, float* py = nullptr) {
     const SagF o = ffs_leaf_eval_o(s, pool, x, y);
     *zc = o.zc;
     *zp = o.zp;
     *ux = o.ux;
     *uy = o.uy;
+    if (px) {
+        *px = o.px;
+        *py = o.py;
+    }
 }
 
-__device__ __forceinline__ void ffs_eval(const Prog& P, int si, ff x, ff y, ff* zc, ff* zp, float* ux, float* uy) {
+// (px, py), when given: the FP32 slope of the polynomial part alone.
+__device__ __forceinline__ void ffs_eval(const Prog& P, int si, ff x, ff y, ff* zc, ff* zp, float* ux, float* uy,
+                                         float* px = nullptr, float* py = nullptr) {
     const bt_surf& s = P.surfs[si];
     if (s.kind != BT_S_SUM) {
-        ffs_leaf_eval(s, P.pool, x, y, zc, zp, ux, uy);
+        ffs_leaf_eval(s, P.pool, x, y, zc, zp, ux, uy, px, py);
         return;
     }
     ff c_acc{0.f, 0.f}, p_acc{0.f, 0.f};
-    float gx = 0.f, gy = 0.f;
+    float gx = 0.f, gy = 0.f, hx = 0.f, hy = 0.f;
     for (int c = 0; c < s.n; c++) {
         ff cz{0.f, 0.f}, pz;
-        float cx, cy;
+        float cx, cy, qx, qy;
         const bt_surf& cs = P.surfs[s.m + c];
-        if (cs.kind == BT_S_MODAL) ff_modal_eval(P, cs, x, y, &pz, &cx, &cy);
-        else ffs_leaf_eval(cs, P.pool, x, y, &cz, &pz, &cx, &cy);
+        if (cs.kind == BT_S_MODAL) {
+            ff_modal_eval(P, cs, x, y, &pz, &cx, &cy);
+            qx = cx;
+            qy = cy;
+        } else {
+            ffs_leaf_eval(cs, P.pool, x, y, &cz, &pz, &cx, &cy, &qx, &qy);
+        }
         c_acc = ff_add(c_acc, cz);
         p_acc = ff_add(p_acc, pz);
         gx += cx;
         gy += cy;
+        hx += qx;
+        hy += qy;
     }
     *zc = c_acc;
     *zp = p_acc;
     *ux = gx;
     *uy = gy;
+    if (px) {
+        *px = hx;
+        *py = hy;
+    }
 }
 
 // FP64 conic part of the sag (the reference's expressions, src/sphere.cpp,
@@ -393,9 +417,13 @@ __device__ __forceinline__ bool ff_analytic(const bt_surf& s, const double* pool
 
 
 // Newton's tangent-plane iteration in float-float from dt, at most niter
-// corrections, stopping once a correction is below 1e-12 m.  Returns whether
-// it stopped that way; *zp and *inv_den hold the polynomial part of the sag
-// and 1/F' at the last evaluation (the point before the last correction).
+// corrections, stopping once a correction is below 1e-7 m: with an FP32
+// derivative (relative error ~1e-7) the error left after that correction is
+// ~1e-14 m, and the FP64 step that follows (ff_newton_tti) finishes the
+// solve.  Returns whether it stopped that way; *zp is the polynomial part
+// of the sag carried to the corrected point (first order in the correction,
+// FP32 slope: the remainder is ~1e-17 m) and *inv_den 1/F' of the last
+// evaluation.
 // (Evaluating the polynomial terms in FP32 during the first iterations was
 // measured at half the throughput: FP32 rounding of the cancelling terms of
 // the Cartesian Zernike arrays keeps the corrections above any useful
@@ -406,13 +434,17 @@ __device__ __forceinline__ bool ff_newton_iter_in(const Prog& P, int si, ff x, f
     for (int it = 0; it < niter; it++) {
         const ff px = ff_mad(vx, *dt, x), py = ff_mad(vy, *dt, y), pz = ff_mad(vz, *dt, z);
         ff zc;
-        float ux, uy;
-        ffs_eval(P, si, px, py, &zc, zp, &ux, &uy);
+        float ux, uy, qx, qy;
+        ffs_eval(P, si, px, py, &zc, zp, &ux, &uy, &qx, &qy);
         const ff res = ff_sub(ff_add(zc, *zp), pz);
         *inv_den = 1.f / fmaf(ux, fvx, fmaf(uy, fvy, fvz));
         const ff ddt = ff_mul_f(res, *inv_den);
         *dt = ff_add(*dt, ddt);
-        if (fabsf(ddt.hi) < 1e-12f) return true;
+        if (fabsf(ddt.hi) < 1e-7f) {
+            // zp at the corrected point: dzp = -(qx vx + qy vy) ddt
+            *zp = ff_add_f(*zp, -fmaf(qx, fvx, qy * fvy) * ddt.hi);
+            return true;
+        }
     }
     return false;
 }
@@ -512,9 +544,7 @@ static __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const R
         float ux, uy;
         ffs_eval(P, si, ff_mad(vx, d, ax), ff_mad(vy, d, ay), &zc, &zp, &ux, &uy);
     }
-    // (after a converged iteration the polynomial part was evaluated before
-    // the last correction, < 1e-12 m earlier along the ray; its slope is
-    // small, so the difference is far below the FP64 conic part's rounding)
+    // (after a converged iteration zp was carried to this point)
     double res = ffs_conic64(P, si, px, py) + ff_to_d(zp) - pz;
     bool ok = d_abs_lt(res, 1e-12);
     // converged: the residual after this last correction is ~1e-7 of |res|;
@@ -725,6 +755,10 @@ static __device__ __noinline__ void ff_medium(const Prog& P, int mi, double w, f
 // hypot(dx, dy) < r decided from h^2 - r^2 in float-float unless within
 // 1e-13 relative of r^2; then *undecided.  rf: r as a float-float pair.
 __device__ __forceinline__ bool ff_radius_less(ff dx, ff dy, ff rf, double r, bool* undecided) {
+    // clear cases in FP32 first (h^2 and r^2 to ~3e-7 relative)
+    const float h2f = fmaf(dx.hi, dx.hi, dy.hi * dy.hi), r2f = rf.hi * rf.hi;
+    if (h2f < r2f * (1.f - 1e-5f)) return __double_as_longlong(r) > 0;
+    if (h2f > r2f * (1.f + 1e-5f)) return false;
     const ff r2 = ff_sqr(rf);
     const ff d = ff_sub(ff_r2(dx, dy), r2);
     const float thr = 1e-13f * r2.hi;

@@ -28,10 +28,10 @@ cudaError_t bt_read_trace_ff_device_status(int* status, cudaStream_t stream) {
 }
 
 // Stage-synchronous like k_trace: a barrier after every stage keeps one
-// stage's code live per block.  MINB: resident blocks per SM the register
-// budget is sized for (2: 128 registers, 16 warps per SM; 3: 80, 24 warps).
-template <int MINB>
-__global__ void __launch_bounds__(TRACE_FF_THREADS, MINB)
+// stage's code live per block.  Register budget for 2 resident blocks per
+// SM (128 registers, 16 warps per SM); 3 blocks (80 registers, 24 warps)
+// measured 18 % slower (spills).
+__global__ void __launch_bounds__(TRACE_FF_THREADS, TRACE_FF_MINB)
 k_trace_ff(const unsigned char* __restrict__ gblob, int blob_bytes, RV in, RV out,
            const __grid_constant__ SnapSet snaps, int nsnaps, int niter) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -77,17 +77,11 @@ cudaError_t bt_launch_trace_ff(const unsigned char* d_blob, int blob_bytes, cons
     if (in.n <= 0) return cudaSuccess;
     static SnapSet empty;
     const SnapSet& ss = snaps ? *snaps : empty;
-    static int minb = 0;
-    if (minb == 0) {
-        const char* env = getenv("BATOID_GB300_TRACE_FF_MINB");
-        minb = (env && atoi(env) == 3) ? 3 : TRACE_FF_MINB;
-    }
-    auto kern = (minb == 3) ? k_trace_ff<3> : k_trace_ff<TRACE_FF_MINB>;
     if (blob_bytes > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, blob_bytes);
+        cudaError_t e = cudaFuncSetAttribute(k_trace_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, blob_bytes);
         if (e != cudaSuccess) return e;
     }
-    const int grid = bt_grid_for(in.n, TRACE_FF_THREADS, minb);
-    kern<<<grid, TRACE_FF_THREADS, blob_bytes, stream>>>(d_blob, blob_bytes, in, out, ss, nsnaps, niter);
+    const int grid = bt_grid_for(in.n, TRACE_FF_THREADS, TRACE_FF_MINB);
+    k_trace_ff<<<grid, TRACE_FF_THREADS, blob_bytes, stream>>>(d_blob, blob_bytes, in, out, ss, nsnaps, niter);
     return cudaGetLastError();
 }
