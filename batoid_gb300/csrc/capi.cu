@@ -62,6 +62,10 @@ struct bt_table {
 // children follow it (root.m is the index of the first child, relative).
 // pool offsets are relative to `pool`.  tables[i] is the bicubic table of
 // recs[i] (nullptr otherwise); tables are shared, not owned.
+// Chunk buffers (and streams) of the host-buffer trace pipeline: copies in
+// of one chunk, the trace of another and copies out of a third overlap.
+#define BT_HOST_PIPE 3
+
 struct bt_surface {
     std::vector<bt_surf> recs;
     std::vector<double> pool;
@@ -1007,9 +1011,10 @@ struct bt_optic {
     // host pipeline scratch for bt_optic_trace_host
     std::mutex mu;
     size_t host_chunk = 0;
-    unsigned char* d_chunk[2] = {nullptr, nullptr};
-    cudaStream_t streams[2] = {nullptr, nullptr};
-    cudaEvent_t done[2] = {nullptr, nullptr};
+    // host-buffer pipeline: BT_HOST_PIPE chunk buffers, one stream each
+    unsigned char* d_chunk[BT_HOST_PIPE] = {nullptr, nullptr, nullptr};
+    cudaStream_t streams[BT_HOST_PIPE] = {nullptr, nullptr, nullptr};
+    cudaEvent_t done[BT_HOST_PIPE] = {nullptr, nullptr, nullptr};
 };
 
 extern "C" int bt_optic_create_ex(size_t nstages, const int* kinds, const bt_surface* const* surfaces,
@@ -1072,7 +1077,7 @@ extern "C" int bt_optic_create_ex(size_t nstages, const int* kinds, const bt_sur
 }
 
 static void release_host_pipeline(bt_optic* o) {
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < BT_HOST_PIPE; k++) {
         if (o->d_chunk[k]) cudaFree(o->d_chunk[k]);
         if (o->streams[k]) cudaStreamDestroy(o->streams[k]);
         if (o->done[k]) cudaEventDestroy(o->done[k]);
@@ -1168,7 +1173,7 @@ extern "C" int bt_optic_trace_host(const bt_optic* oc, const bt_rayvector* h, in
     const size_t bytes = chunk * (9 * sizeof(double) + 2);
     if (o->host_chunk != chunk) {
         release_host_pipeline(o);
-        for (int k = 0; k < 2; k++) {
+        for (int k = 0; k < BT_HOST_PIPE; k++) {
             cudaError_t e = cudaMalloc((void**)&o->d_chunk[k], bytes);
             if (e != cudaSuccess) { release_host_pipeline(o); return fail(BT_ERR_ALLOC, "traceHost: device scratch"); }
             CUDA_TRY(cudaStreamCreateWithFlags(&o->streams[k], cudaStreamNonBlocking), "traceHost streams");
@@ -1181,12 +1186,12 @@ extern "C" int bt_optic_trace_host(const bt_optic* oc, const bt_rayvector* h, in
     cudaEvent_t start;
     CUDA_TRY(cudaEventCreateWithFlags(&start, cudaEventDisableTiming), "traceHost");
     CUDA_TRY(cudaEventRecord(start, user), "traceHost");
-    for (int k = 0; k < 2; k++) CUDA_TRY(cudaStreamWaitEvent(o->streams[k], start, 0), "traceHost");
+    for (int k = 0; k < BT_HOST_PIPE; k++) CUDA_TRY(cudaStreamWaitEvent(o->streams[k], start, 0), "traceHost");
     cudaEventDestroy(start);
     const size_t n = h->size;
     size_t nchunks = (n + chunk - 1) / chunk;
     for (size_t c = 0; c < nchunks; c++) {
-        const int k = (int)(c & 1);
+        const int k = (int)(c % BT_HOST_PIPE);
         cudaStream_t s = o->streams[k];
         const size_t i0 = c * chunk;
         const size_t m = (n - i0) < chunk ? (n - i0) : chunk;
@@ -1206,7 +1211,7 @@ extern "C" int bt_optic_trace_host(const bt_optic* oc, const bt_rayvector* h, in
         CUDA_TRY(cudaMemcpyAsync(h->vignetted + i0, d.vig, m, cudaMemcpyDeviceToHost, s), "traceHost D2H");
         CUDA_TRY(cudaMemcpyAsync(h->failed + i0, d.fail, m, cudaMemcpyDeviceToHost, s), "traceHost D2H");
     }
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < BT_HOST_PIPE; k++) {
         CUDA_TRY(cudaEventRecord(o->done[k], o->streams[k]), "traceHost");
         CUDA_TRY(cudaStreamWaitEvent(user, o->done[k], 0), "traceHost");
     }

@@ -227,7 +227,7 @@ def measured_peaks():
         return {}
 
 
-def host_trace_e2e(L, _lib, prog, arrs, n, niter, steps, sp, chunk=1 << 21):
+def host_trace_e2e(L, _lib, prog, arrs, n, niter, steps, sp, chunk=1 << 20):
     """The trace through the C-ABI host-buffer entry point (bt_optic_trace_host):
     pinned host arrays in, results back in them; host clock around each call.
     Returns (ms per call, h2d bytes, d2h bytes)."""
@@ -283,7 +283,7 @@ def bench_paraboloid(bt, fp64_peak, n=1_000_000, reps=20, cpu=True):
     bpr = WC.READ_BYTES_PER_RAY + WC.WRITE_BYTES_PER_RAY
     gbs = bpr * n / (ms * 1e-3) / 1e9
     hbm_peak = measured_peaks().get("hbm_gbs", 6800.0)
-    c = load_counters("k_trace/paraboloid")
+    c = load_counters("k_trace_ff/paraboloid")
     out = {"workload": f"paraboloid: f/4 mirror (R 8 m, annulus 0.2-0.5 m) + flat detector, {n} rays, "
                        "field +-0.5 deg, 500 nm, vacuum",
            "value": n * nsurf / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "steps": reps,
@@ -291,6 +291,13 @@ def bench_paraboloid(bt, fp64_peak, n=1_000_000, reps=20, cpu=True):
            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
                         "bytes_per_ray": bpr, "peak_source": "MEASURED_PEAKS.json hbm_gbs",
                         "traffic": (c["dram_bytes_per_ray"] * n if c else None)}}
+    if c and "warp_inst_per_ray" in c:
+        sms = ctypes.c_int(0)
+        _lib.check(L.bt_device_sm_count(ctypes.byref(sms)))
+        peak = 4 * sms.value * 2.07
+        ach = c["warp_inst_per_ray"] * n / (ms * 1e-3) / 1e9
+        out["issue"] = {"achieved": ach, "peak": peak, "unit": "G warp-instructions/s", "frac": ach / peak,
+                        "peak_source": f"4 schedulers x {sms.value} SMs x 2.07 GHz"}
     fpr = executed_fp64_flops(c)
     if fpr and fp64_peak:
         ach = fpr * n / (ms * 1e-3) / 1e12
@@ -299,7 +306,7 @@ def bench_paraboloid(bt, fp64_peak, n=1_000_000, reps=20, cpu=True):
     e2e_ms, h2d, d2h = host_trace_e2e(L, _lib, prog, arrs, n, niter, 5, sp, chunk=1 << 19)
     out["e2e"] = {"value": n * nsurf / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                   "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
-                  "path": "bt_optic_trace_host, pinned host arrays, 2-stream chunks"}
+                  "path": "bt_optic_trace_host, pinned host arrays, 512k-ray chunks on 3 streams"}
     if cpu:
         ora, copt, make_rays, _ = cpu_workload("paraboloid")
         pristine = ora.Rays(*make_rays(n, seed=57721))
@@ -744,17 +751,27 @@ def run_gpu(args):
     # sanity: the benchmark traced real rays
     vig = float(rv_out.field("vignetted").float().mean().item())
 
-    # FP64 roofline of the fused trace kernel (one launch per step).  The
-    # numerator is the FP64 work the kernel executes (DADD + DMUL + 2 DFMA per
-    # ray, from the committed ncu census of the same kernel and workload);
-    # the reference-expression flop count is reported beside it.
+    # Roofline of the fused trace kernel (k_trace_ff, one launch per step).
+    # It is bound by instruction issue (float-float arithmetic on the FP32 and
+    # integer pipes; the FP64 pipe ~20 % busy): achieved = the warp
+    # instructions it executes per ray (committed ncu census of the same
+    # kernel and workload) x rays / step time, peak = 4 schedulers x SMs x
+    # the SM clock sampled during the timed region.  The FP64 view (executed
+    # DADD + DMUL + 2 DFMA vs the in-run DFMA probe) and the reference-flop
+    # count are reported beside it.
     fpeak = ctypes.c_double(0.0)
     _lib.check(L.bt_measure_fp64_peak(1 << 14, ctypes.byref(fpeak), sp))
     ref_flops_per_ray = WC.optic_flops_per_ray(opt, niter)
     ref_tflops = ref_flops_per_ray * n / (ms_per_step * 1e-3) / 1e12
-    counters = load_counters(f"k_trace/{args.workload}")
+    counters = load_counters(f"k_trace_ff/{args.workload}")
     exec_fpr = executed_fp64_flops(counters)
     exec_tflops = exec_fpr * n / (ms_per_step * 1e-3) / 1e12 if exec_fpr else None
+    sms = ctypes.c_int(0)
+    _lib.check(L.bt_device_sm_count(ctypes.byref(sms)))
+    sm_ghz = (clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0) / 1e3
+    issue_peak = 4 * sms.value * sm_ghz  # G warp instructions / s
+    issue_ach = (counters["warp_inst_per_ray"] * n / (ms_per_step * 1e-3) / 1e9
+                 if counters and "warp_inst_per_ray" in counters else None)
     bytes_per_ray = WC.READ_BYTES_PER_RAY + WC.WRITE_BYTES_PER_RAY
     hbm_gbs = bytes_per_ray * n / (ms_per_step * 1e-3) / 1e9
     hbm_peak = measured_peaks().get("hbm_gbs", 6800.0)
@@ -793,17 +810,18 @@ def run_gpu(args):
                        "rays_per_gpu": n, "surfaces": nsurf, "niter": niter,
                        "l2": "inputs larger than L2 (1.2 GB per step), no flush",
                        "vignetted_fraction": vig},
-            "roofline": {"bound": "fp64", "achieved": exec_tflops, "peak": fpeak.value, "unit": "TFLOP/s",
-                         "frac": exec_tflops / fpeak.value if (exec_tflops and fpeak.value) else None,
+            "roofline": {"bound": "issue", "achieved": issue_ach, "peak": issue_peak,
+                         "unit": "G warp-instructions/s",
+                         "frac": issue_ach / issue_peak if issue_ach else None,
                          "traffic": (counters["dram_bytes_per_ray"] * n if counters else None),
-                         "peak_source": "DFMA loop measured in this run (bt_measure_fp64_peak)",
-                         "executed_flops_per_ray": exec_fpr,
-                         "fp64_pipe": ({"slots_per_ray": counters["fp64_pipe_thread_inst_per_ray"],
-                                        "frac_of_dfma_loop": counters["fp64_pipe_thread_inst_per_ray"] * n
-                                        / (ms_per_step * 1e-3) / (fpeak.value * 1e12 / 2)}
-                                       if counters and fpeak.value else None),
+                         "peak_source": f"4 schedulers x {sms.value} SMs x {sm_ghz:.3f} GHz (clock sampled in "
+                                        "the timed region)",
+                         "kernel": "k_trace_ff",
                          "counters": counters,
-                         "fp64_pipe_busy": (counters or {}).get("fp64_pipe_busy_pct"),
+                         "fp64": {"achieved": exec_tflops, "peak": fpeak.value, "unit": "TFLOP/s",
+                                  "frac": exec_tflops / fpeak.value if (exec_tflops and fpeak.value) else None,
+                                  "executed_flops_per_ray": exec_fpr,
+                                  "peak_source": "DFMA loop measured in this run (bt_measure_fp64_peak)"},
                          "reference_flops": {"flops_per_ray": ref_flops_per_ray, "tflops": ref_tflops,
                                              "ratio_to_peak": ref_tflops / fpeak.value if fpeak.value else None,
                                              "convention": "FP64 operations of the reference's own expressions "
@@ -813,7 +831,7 @@ def run_gpu(args):
                                  "frac": hbm_gbs / hbm_peak, "bytes_per_ray": bytes_per_ray,
                                  "peak_source": "MEASURED_PEAKS.json hbm_gbs"}},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": e2e_ms, "path": "bt_optic_trace_host, pinned host arrays, 2-stream chunks"},
+                    "ms_per_step": e2e_ms, "path": "bt_optic_trace_host, pinned host arrays, 1M-ray chunks on 3 streams"},
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": args.steps,
