@@ -1189,12 +1189,38 @@ extern "C" int bt_optic_trace_host(const bt_optic* oc, const bt_rayvector* h, in
     for (int k = 0; k < BT_HOST_PIPE; k++) CUDA_TRY(cudaStreamWaitEvent(o->streams[k], start, 0), "traceHost");
     cudaEventDestroy(start);
     const size_t n = h->size;
-    size_t nchunks = (n + chunk - 1) / chunk;
+    // Chunk boundaries.  On long inputs the first and last chunk buffers
+    // are filled in steps of chunk/8, /8, /4, /2: the copy in before the
+    // first trace and the copy out after the last one are what the
+    // pipeline cannot overlap, so they are made small.
+    std::vector<size_t> cut{0};
+    {
+        auto push = [&](size_t m) { cut.push_back(cut.back() + m); };
+        const size_t e = chunk / 8;
+        if (e > 0 && n >= 4 * chunk) {
+            push(e);
+            push(e);
+            push(chunk / 4);
+            push(chunk / 2);
+            const size_t ramp = e + e + chunk / 4 + chunk / 2;  // the head's (and tail's) total
+            while (n - cut.back() >= ramp + chunk + chunk) push(chunk);
+            const size_t mid = n - cut.back() - ramp;  // in [chunk, 2 chunk)
+            push(mid / 2);
+            push(mid - mid / 2);
+            push(chunk / 2);
+            push(chunk / 4);
+            push(e);
+            push(n - cut.back());
+        } else {
+            while (cut.back() < n) push((n - cut.back()) < chunk ? (n - cut.back()) : chunk);
+        }
+    }
+    const size_t nchunks = cut.size() - 1;
     for (size_t c = 0; c < nchunks; c++) {
         const int k = (int)(c % BT_HOST_PIPE);
         cudaStream_t s = o->streams[k];
-        const size_t i0 = c * chunk;
-        const size_t m = (n - i0) < chunk ? (n - i0) : chunk;
+        const size_t i0 = cut[c];
+        const size_t m = cut[c + 1] - i0;
         RV d = chunk_rv(o->d_chunk[k], chunk, (long long)m);
         double* hd[9] = {h->x, h->y, h->z, h->vx, h->vy, h->vz, h->t, h->wavelength, h->flux};
         double* dd[9] = {d.x, d.y, d.z, d.vx, d.vy, d.vz, d.t, d.w, d.f};

@@ -256,12 +256,20 @@ class WavefrontSurrogate:
             if not np.any(sel):
                 continue
             A = np.concatenate([np.ones((sel.sum(), 1)), feat[sel, :nd].astype(np.float64)], axis=1)
-            self.theta[g] = np.linalg.lstsq(A, c[sel], rcond=None)[0]
+            # normal equations: the scaled features keep A^T A well
+            # conditioned (ones column and unit-range inputs)
+            try:
+                self.theta[g] = np.linalg.solve(A.T @ A, A.T @ c[sel])
+            except np.linalg.LinAlgError:
+                self.theta[g] = np.linalg.lstsq(A, c[sel], rcond=None)[0]
 
     def linear(self, feat, grp):
         nd = self.pt.ndof
-        th = self.theta[grp]
-        return th[:, 0, :] + np.einsum('nk,nkj->nj', feat[:, :nd].astype(np.float64), th[:, 1:, :])
+        out = np.empty((len(grp), self.J))
+        for g in np.unique(grp):
+            sel = grp == g
+            out[sel] = self.theta[g, 0, :] + feat[sel, :nd].astype(np.float64) @ self.theta[g, 1:, :]
+        return out
 
     def residual_targets(self, feat, grp, w, coefs):
         """Residual of the linear model in nm / scale."""
@@ -276,22 +284,43 @@ class WavefrontSurrogate:
         backward, Adam with the cosine learning-rate schedule and bias
         corrections computed on the device) is captured once in a CUDA
         graph and replayed; the step's ~30 launches then cost one graph
-        launch.  graph=False issues them one by one (same arithmetic)."""
+        launch.  graph=False issues them one by one (same arithmetic).
+
+        Minibatches are drawn from a device permutation per epoch (seeded
+        generator).  self.timing afterwards holds the wall time of the
+        linear fit (host) and of the network training (device steps)."""
+        import time
+        t0 = time.perf_counter()
         self.fit_linear(feat, grp, coefs)
         r = self.residual_targets(feat, grp, w, coefs)
         self.scale = float(np.sqrt(np.mean(r ** 2)))
         t_all = torch.from_numpy((r / self.scale).astype(np.float32)).to(D.device())
         x_all = torch.from_numpy(feat).to(D.device())
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
         n = len(feat)
         steps_per_epoch = n // batch
         total = epochs * steps_per_epoch
-        rng = np.random.default_rng(seed)
+        gen = torch.Generator(device=D.device())
+        gen.manual_seed(seed)
+
+        def perm_of_epoch():
+            return torch.randperm(n, generator=gen, device=D.device())[:steps_per_epoch * batch]
+
         if graph and steps_per_epoch > 0:
-            self._train_graph(x_all, t_all, epochs, steps_per_epoch, batch, lr, lr_min, err_weight, rng, log)
-            return
+            self._train_graph(x_all, t_all, epochs, steps_per_epoch, batch, lr, lr_min, err_weight, perm_of_epoch,
+                              log)
+        else:
+            self._train_eager(x_all, t_all, epochs, steps_per_epoch, batch, lr, lr_min, err_weight, perm_of_epoch,
+                              log)
+        self.timing = {"linear_fit_s": t1 - t0, "network_s": time.perf_counter() - t1,
+                       "steps": total, "samples": total * batch}
+
+    def _train_eager(self, x_all, t_all, epochs, steps_per_epoch, batch, lr, lr_min, err_weight, perm_of_epoch, log):
+        total = epochs * steps_per_epoch
         step = 0
         for ep in range(epochs):
-            perm = torch.from_numpy(rng.permutation(n)).to(D.device())
+            perm = perm_of_epoch()
             for k in range(steps_per_epoch):
                 idx = perm[k * batch:(k + 1) * batch]
                 x = x_all.index_select(0, idx)
@@ -307,7 +336,7 @@ class WavefrontSurrogate:
                 log(ep, float(bf["loss"][0].item()), float(bf["loss"][1].item()))
         torch.cuda.synchronize()
 
-    def _train_graph(self, x_all, t_all, epochs, steps_per_epoch, batch, lr, lr_min, err_weight, rng, log,
+    def _train_graph(self, x_all, t_all, epochs, steps_per_epoch, batch, lr, lr_min, err_weight, perm_of_epoch, log,
                      b1=0.9, b2=0.999):
         net, dev = self.net, D.device()
         n = x_all.shape[0]
@@ -343,8 +372,7 @@ class WavefrontSurrogate:
         with torch.cuda.stream(stream):
             done = 0
             for ep in range(epochs):
-                perm.copy_(torch.from_numpy(rng.permutation(n)[:steps_per_epoch * batch].reshape(steps_per_epoch,
-                                                                                                  batch)))
+                perm.copy_(perm_of_epoch().view(steps_per_epoch, batch))
                 k_in_epoch.zero_()
                 for k in range(steps_per_epoch):
                     if done == 0:

@@ -516,13 +516,35 @@ def bench_batched(bt, nstates=4096, reps=3, cpu=True, fp64_peak_tflops=None):
                 "d2h_bytes": int(coefs.numel() * 8 + status.numel() * 4),
                 "path": "PerturbedTelescope.zernike (host tables, copies, launch, copies back)"},
     }
+    # issue roofline of the batched kernel from its ncu census (warp
+    # instructions per pupil ray, fit included); executed FP64 flops and the
+    # reference-flop count beside it
+    c = load_counters("k_batch_zernike/tma_bending")
+    roof = {"bound": "issue", "achieved": None, "peak": None, "unit": "G warp-instructions/s", "frac": None,
+            "kernel": "k_batch_zernike"}
+    if c and "warp_inst_per_ray" in c:
+        from batoid_gb300 import _lib
+        sms = ctypes.c_int(0)
+        _lib.check(_lib.lib().bt_device_sm_count(ctypes.byref(sms)))
+        peak = 4 * sms.value * 2.07
+        ach = c["warp_inst_per_ray"] * rays / (ms * 1e-3) / 1e9
+        roof.update({"achieved": ach, "peak": peak, "frac": ach / peak, "warp_inst_per_ray": c["warp_inst_per_ray"],
+                     "peak_source": f"4 schedulers x {sms.value} SMs x 2.07 GHz",
+                     "traffic": c.get("dram_bytes_per_ray", 0.0) * rays})
     if fp64_peak_tflops:
         from batoid_gb300 import workcount as WC
         fpr = WC.wavefront_flops_per_ray(pt.perturbed(dofs[0]), J)
         ach = fpr * rays / (ms * 1e-3) / 1e12
-        out["roofline"] = {"bound": "fp64", "achieved": ach, "peak": fp64_peak_tflops, "unit": "TFLOP/s",
-                           "frac": ach / fp64_peak_tflops, "flops_per_ray": fpr,
-                           "peak_source": "DFMA loop measured in this run (bt_measure_fp64_peak)"}
+        efpr = executed_fp64_flops(c)
+        if efpr:
+            each = efpr * rays / (ms * 1e-3) / 1e12
+            roof["fp64"] = {"executed_flops_per_ray": efpr, "achieved": each, "peak": fp64_peak_tflops,
+                            "unit": "TFLOP/s", "frac": each / fp64_peak_tflops,
+                            "peak_source": "DFMA loop measured in this run (bt_measure_fp64_peak)"}
+        roof["reference_flops"] = {"flops_per_ray": fpr, "tflops": ach, "ratio_to_peak": ach / fp64_peak_tflops,
+                                   "convention": "FP64 operations of the reference's own expressions "
+                                                 "(workcount.wavefront_flops_per_ray); not executed as such"}
+    out["roofline"] = roof
     if cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import wavefront as owf
@@ -672,6 +694,8 @@ def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24,
     except (OSError, ValueError):
         pass
     bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    bf16_sus = peaks.get("bf16_tflops_sustained", 1700.0)
+    train_tflops = 3 * flops_fwd * sur.timing["samples"] / sur.timing["network_s"] / 1e12
     infer_tflops = flops_fwd * N / (infer_ms * 1e-3) / 1e12
     out_d = {
         "workload": f"MLP 33 -> 4x512 GELU -> 28 + error head, bf16/fp32-accumulate tcgen05 kernels; trained on "
@@ -687,7 +711,16 @@ def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24,
         "ms": {"inference": infer_ms, "fallback_trace": fb_ms, "batched_trace": trace_ms, "datagen_s": datagen_s,
                "train_s": train_s},
         "training": {"steps": steps, "batch": 8192, "epochs": epochs,
-                     "samples_per_s": steps * 8192 / train_s},
+                     "samples_per_s": sur.timing["samples"] / sur.timing["network_s"],
+                     "network_s": sur.timing["network_s"], "linear_fit_s": sur.timing["linear_fit_s"],
+                     "graph": True,
+                     "note": "samples_per_s: network training steps (CUDA-graph replay of gather, forward, loss, "
+                             "backward, Adam) over their synchronized wall time; the host least-squares fit of the "
+                             "linear model is linear_fit_s"},
+        "roofline_training": {"bound": "tensor", "achieved": train_tflops, "peak": bf16_sus, "unit": "TFLOP/s",
+                              "frac": train_tflops / bf16_sus, "flops_per_sample": 3 * flops_fwd,
+                              "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (seconds-long loop)",
+                              "note": "3 x forward flops per sample (forward, data gradient, weight gradient)"},
         "roofline_inference": {"bound": "tensor", "achieved": infer_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
                                "frac": infer_tflops / bf16_peak, "flops_per_sample": flops_fwd,
                                "note": "whole inference pipeline (pack, 5 GEMMs, combine) over its event time"},
