@@ -273,11 +273,18 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
     double* bv = reinterpret_cast<double*>(smem + L.bv);
     float* mcf = reinterpret_cast<float*>(smem + L.mcf);
     int* mcell = reinterpret_cast<int*>(smem + L.mcell);
-    Prog P = prog_from_blob(smem);
-    P.mc = mc + tid;
-    P.mcf = mcf + tid;
-    P.mcell = mcell + tid;
-    P.mstride = T;
+    // one copy of the program's pointers per block (the out-of-line
+    // helpers take it by reference: no per-thread stack copy)
+    __shared__ Prog sP;
+    if (tid == 0) {
+        sP = prog_from_blob(smem);
+        sP.mc = mc;
+        sP.mcf = mcf;
+        sP.mcell = mcell;
+        sP.mstride = T;
+    }
+    __syncthreads();
+    const Prog& P = sP;
     bt_stage& sph = stages[A.ntrace];
     const int modal_off = (A.modal_surf >= 0) ? P.surfs[A.modal_surf].off : 0;
     double* gw = gcorr + warp * NT;
@@ -320,8 +327,7 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
                 amp[m] = ff{h, __double2float_rn(a - (double)h)};
             }
         }
-        mcell[tid] = -1;
-        for (int e = lane; e < NT; e += 32) gw[e] = 0.0;
+        mcell[tid] = -1;  // the corner cache shares its space with the fit's gcorr
         __syncthreads();
 
         const double* F = A.field + (size_t)f * 18;
@@ -383,6 +389,7 @@ k_batch_zernike(const unsigned char* __restrict__ gblob, int blob_bytes, const _
             if (!s_last) continue;
             __threadfence();
         }
+        for (int e = lane; e < NT; e += 32) gw[e] = 0.0;
         // B^T v: warp w sums rows j = w, w + nwarps, ... of Z^T opd, every
         // lane over points i = lane, lane + 32, ... (independent accumulators)
         {

@@ -69,10 +69,14 @@ struct BatchSmem {
 __host__ __device__ inline BatchSmem bt_batch_smem_layout(int blob_bytes, int T, int J) {
     BatchSmem L;
     size_t off = ((size_t)blob_bytes + 127) & ~(size_t)127;
+    // the MODAL corner cache (ray phase) and the per-warp Gram corrections
+    // (fit phase) share one region
     L.mc = off;
-    off += (size_t)16 * T * sizeof(double);
     L.gcorr = off;
-    off += (size_t)(T / 32) * (J * (J + 1) / 2) * sizeof(double);
+    {
+        const size_t a = (size_t)16 * T * sizeof(double), b = (size_t)(T / 32) * (J * (J + 1) / 2) * sizeof(double);
+        off += a > b ? a : b;
+    }
     L.zv = off;
     off += (size_t)(T / 32) * 32 * sizeof(double);
     L.G = off;

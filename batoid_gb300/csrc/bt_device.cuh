@@ -26,8 +26,9 @@ struct Prog {
     int nstages;
     int nmedia;
     // Per-thread cache of the combined corner values of a MODAL surface
-    // (batched kernel only; null elsewhere).  Element k of the cache lives at
-    // mc[k * mstride] (interleaved across the block's threads).
+    // (batched kernel only; null elsewhere): the block's arrays, element k
+    // of thread t at mc[k * mstride + t] (interleaved across the threads),
+    // the cached cell of thread t at mcell[t].
     double* mc;
     float* mcf;
     int* mcell;
@@ -337,9 +338,10 @@ __device__ __forceinline__ bool bt_modal_locate(const Prog& P, const bt_surf& s,
     int ix, iy;
     if (!bt_modal_cell(s, x, y, &ix, &iy, xfrac, yfrac)) return false;
     const int cell = iy * s.n + ix;
-    if (*P.mcell == cell) return true;
-    bt_modal_fill(P.pool, &s, ix, iy, P.mc, P.mcf, P.mstride);
-    *P.mcell = cell;
+    int* cellp = P.mcell + threadIdx.x;
+    if (*cellp == cell) return true;
+    bt_modal_fill(P.pool, &s, ix, iy, P.mc + threadIdx.x, P.mcf + threadIdx.x, P.mstride);
+    *cellp = cell;
     return true;
 }
 
@@ -357,7 +359,7 @@ __device__ __forceinline__ void bt_modal_eval(const Prog& P, const bt_surf& s, d
     const int st = P.mstride;
     double v[16];
 #pragma unroll
-    for (int k = 0; k < 16; k++) v[k] = P.mc[k * st];
+    for (int k = 0; k < 16; k++) v[k] = P.mc[k * st + threadIdx.x];
     double val = 0.0, gx = 0.0, gy = 0.0;
     bt_hermite<double>(xf, yf, s.p[2], s.p[3], v, v + 4, v + 8, v + 12, &val, &gx, &gy, want_sag, want_slope);
     if (want_sag) *sag = val;
@@ -380,8 +382,8 @@ __device__ __forceinline__ void bt_modal_newton_eval(const Prog& P, const bt_sur
     float w[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) {
-        v[k] = P.mc[k * st];
-        w[k] = P.mcf[k * st];
+        v[k] = P.mc[k * st + threadIdx.x];
+        w[k] = P.mcf[k * st + threadIdx.x];
     }
     double val;
     bt_hermite<double>(xf, yf, s.p[2], s.p[3], v, v + 4, v + 8, v + 12, &val, nullptr, nullptr, true, false);

@@ -117,13 +117,14 @@ static __device__ __noinline__ void ff_modal_eval(const Prog& P, const bt_surf& 
     const int ix = (int)fu, iy = (int)fv;
     const float xf = (u.hi - fu) + u.lo, yf = (v.hi - fv) + v.lo;
     const int cell = iy * s.n + ix;
-    if (*P.mcell != cell) {
-        bt_modal_fill(P.pool, &s, ix, iy, P.mc, P.mcf, P.mstride);
-        *P.mcell = cell;
+    int* cellp = P.mcell + threadIdx.x;
+    if (*cellp != cell) {
+        bt_modal_fill(P.pool, &s, ix, iy, P.mc + threadIdx.x, P.mcf + threadIdx.x, P.mstride);
+        *cellp = cell;
     }
     float w[16];
 #pragma unroll
-    for (int k = 0; k < 16; k++) w[k] = P.mcf[k * P.mstride];
+    for (int k = 0; k < 16; k++) w[k] = P.mcf[k * P.mstride + threadIdx.x];
     float val, gx, gy;
     bt_hermite<float>(xf, yf, d_to_ff(s.p[2]).hi, d_to_ff(s.p[3]).hi, w, w + 4, w + 8, w + 12, &val, &gx, &gy, true,
                       true);
@@ -487,6 +488,8 @@ __device__ __forceinline__ bool ff_residual_ok(const Prog& P, int si, ff x, ff y
 }
 
 // FP64 state of a ray in a surface's frame, with its float-float copy.
+// Passed by value to the out-of-line helpers (in registers); by reference
+// it had to live on each thread's stack.
 struct RayLocal {
     double xd, yd, zd, vxd, vyd, vzd;
     ff x, y, z, vx, vy, vz;
@@ -502,7 +505,7 @@ struct RayLocal {
 // are then of the size of the sag, not of the distance the ray travelled
 // (15 m before the primary of a telescope), so their rounding (~1e-16 m)
 // stays far below the 1e-12 m convergence and success thresholds.
-static __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const RayLocal& L, int niter, double* dt_out) {
+static __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const RayLocal L, int niter, double* dt_out) {
     const bt_surf& s = P.surfs[si];
     const ff vx = L.vx, vy = L.vy, vz = L.vz;
     ff t0{0.f, 0.f};
@@ -576,7 +579,7 @@ static __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const R
 // surface's FP64 sag.  Success stays the analytic root's (a finite
 // discriminant), as in the reference; the step is applied only when the
 // residual is finite and below 1e-9 m.
-static __device__ __noinline__ double ff_refine64(const Prog& P, int si, const RayLocal& L, ff dt) {
+static __device__ __noinline__ double ff_refine64(const Prog& P, int si, const RayLocal L, ff dt) {
     double dtd = ff_to_d(dt);
     const double px = fma(L.vxd, dtd, L.xd), py = fma(L.vyd, dtd, L.yd), pz = fma(L.vzd, dtd, L.zd);
     ff zc, zp;

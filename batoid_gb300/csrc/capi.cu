@@ -1444,6 +1444,36 @@ extern "C" int bt_surrogate_combine(const float* feat, int nfeat, int nlin, cons
     return BT_OK;
 }
 
+extern "C" int bt_mlp_gather(const long long* perm, const long long* k_in_epoch, const float* x_all, int nxc,
+                             const float* t_all, int ntc, int batch, float* xb, float* tb, void* stream) {
+    if (batch < 0 || (batch > 0 && (!perm || !k_in_epoch || !x_all || !t_all || !xb || !tb)) || nxc < 1 || ntc < 1)
+        return fail(BT_ERR_ARG, "mlp gather: bad arguments");
+    CUDA_TRY(bt_launch_mlp_gather(perm, k_in_epoch, x_all, nxc, t_all, ntc, batch, xb, tb, (cudaStream_t)stream),
+             "mlp gather");
+    return BT_OK;
+}
+
+extern "C" int bt_mlp_schedule(long long* k_in_epoch, double* gstep, float* hyper, double lr, double lr_min,
+                               long long total, double b1, double b2, void* stream) {
+    if (!k_in_epoch || !gstep || !hyper || total < 1 || !(lr > 0.0) || !(b1 > 0.0 && b1 < 1.0) ||
+        !(b2 > 0.0 && b2 < 1.0))
+        return fail(BT_ERR_ARG, "mlp schedule: bad arguments");
+    CUDA_TRY(bt_launch_mlp_schedule(k_in_epoch, gstep, hyper, lr, lr_min, (double)total, b1, b2, (cudaStream_t)stream),
+             "mlp schedule");
+    return BT_OK;
+}
+
+extern "C" int bt_surrogate_guard(const float* feat, int nfeat, int ndof, const int* grp, const float* m0,
+                                  const float* jac, const float* reach, int K, double band_abs, double band_rel,
+                                  int* flag, int n, void* stream) {
+    if (n < 0 || (n > 0 && (!feat || !grp || !m0 || !jac || !flag)) || ndof < 0 || ndof > nfeat || K < 32 ||
+        (K % 32) != 0 || !(band_abs >= 0.0) || !(band_rel >= 0.0))
+        return fail(BT_ERR_ARG, "surrogate guard: bad arguments");
+    CUDA_TRY(bt_launch_surrogate_guard(feat, nfeat, ndof, grp, m0, jac, reach, K, (float)band_abs, (float)band_rel,
+                                       flag, n, (cudaStream_t)stream), "surrogate guard");
+    return BT_OK;
+}
+
 extern "C" int bt_mlp_adam(const float* partials, int nsplit, const float* grad, long long n, float* w, float* m,
                            float* v, float lr, float b1, float b2, float eps, float bc1, float bc2, int rows, int cols,
                            void* w16, void* w16t, void* stream) {

@@ -518,6 +518,33 @@ __global__ void k_mlp_pack(const float* __restrict__ x, int rows, int cols, int 
     }
 }
 
+// Both forms through a shared 32 x 32 tile (threads 32 columns x 8 rows):
+// rows of out and of out_t leave as 64-byte runs.
+__global__ void __launch_bounds__(256) k_mlp_pack_t(const float* __restrict__ x, int rows, int cols, int ld_out,
+                                                    int rows_out, __nv_bfloat16* __restrict__ out,
+                                                    __nv_bfloat16* __restrict__ out_t) {
+    __shared__ __nv_bfloat16 tile[32][34];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int tilesc = (ld_out + 31) / 32;
+    const int r0 = (blockIdx.x / tilesc) * 32, c0 = (blockIdx.x % tilesc) * 32;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int r = r0 + ty + 8 * k, c = c0 + tx;
+        if (r < rows_out && c < ld_out) {
+            const float v = (r < rows && c < cols) ? x[(size_t)r * cols + c] : 0.f;
+            const __nv_bfloat16 b = __float2bfloat16_rn(v);
+            out[(size_t)r * ld_out + c] = b;
+            tile[ty + 8 * k][tx] = b;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int c = c0 + ty + 8 * k, r = r0 + tx;
+        if (r < rows_out && c < ld_out) out_t[(size_t)c * rows_out + r] = tile[tx][ty + 8 * k];
+    }
+}
+
 // Row-major form only (no transposed copy), 8 columns per thread and one
 // 16-byte store; needs ld_out % 8 == 0, a 16-byte aligned `out` and
 // rows_out * ld_out / 8 < 2^31.
@@ -539,19 +566,28 @@ __global__ void k_mlp_pack8(const float* __restrict__ x, int rows, int cols, int
 
 // Gradient of the weighted mean-squared error of columns [0, ncols) and of
 // the error head (column err_col, which predicts the log of the row's
-// residual norm sqrt(sum_j r_j^2), a detached target).  One thread per row.
-__global__ void k_mlp_loss(const float* __restrict__ y, int ldy, const float* __restrict__ t,
-                           const float* __restrict__ wt, int rows, int rows_valid, int ncols, int err_col,
-                           float err_weight, int ld_out, __nv_bfloat16* __restrict__ dz,
-                           __nv_bfloat16* __restrict__ dzt, float* loss) {
-    __shared__ float s_main[256], s_err[256];
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+// residual norm sqrt(sum_j r_j^2), a detached target).  A block takes 32
+// rows: each warp 4 rows with lanes over the columns (coalesced dz rows),
+// the gradients staged in shared memory so that the transposed copy dzt
+// leaves as 64-byte runs of 32 consecutive rows.  Needs ld_out <= 128.
+#define MLP_LOSS_ROWS 32
+__global__ void __launch_bounds__(256) k_mlp_loss(const float* __restrict__ y, int ldy, const float* __restrict__ t,
+                                                  const float* __restrict__ wt, int rows, int rows_valid, int ncols,
+                                                  int err_col, float err_weight, int ld_out,
+                                                  __nv_bfloat16* __restrict__ dz, __nv_bfloat16* __restrict__ dzt,
+                                                  float* loss) {
+    __shared__ float g_s[MLP_LOSS_ROWS][129];
+    __shared__ float s_main[8], s_err[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int m0 = blockIdx.x * MLP_LOSS_ROWS;
+    const float scale = 2.0f / (float)rows_valid;
     float lm = 0.f, le = 0.f;
-    if (m < rows) {
+    for (int q = 0; q < MLP_LOSS_ROWS / 8; q++) {
+        const int rr = warp * (MLP_LOSS_ROWS / 8) + q, m = m0 + rr;
+        if (m >= rows) break;
         const bool valid = m < rows_valid;
-        const float scale = 2.0f / (float)rows_valid;
         float ss = 0.f;
-        for (int j = 0; j < ld_out; j++) {
+        for (int j = lane; j < ld_out; j += 32) {
             float g = 0.f;
             if (valid && j < ncols) {
                 const float r = y[(size_t)m * ldy + j] - t[(size_t)m * ncols + j];
@@ -560,52 +596,81 @@ __global__ void k_mlp_loss(const float* __restrict__ y, int ldy, const float* __
                 lm += w * r * r;
                 g = scale * w * r;
             }
-            if (j != err_col || !valid) {
-                dz[(size_t)m * ld_out + j] = __float2bfloat16_rn(g);
-                dzt[(size_t)j * rows + m] = __float2bfloat16_rn(g);
-            }
+            g_s[rr][j] = g;
         }
-        if (err_col >= 0) {
+        __syncwarp();
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        if (err_col >= 0 && lane == 0) {
             float g = 0.f;
             if (valid) {
                 const float target = 0.5f * __logf(ss + 1e-12f);
                 const float r = y[(size_t)m * ldy + err_col] - target;
-                le = r * r;
+                le += r * r;
                 g = scale * err_weight * r;
             }
-            dz[(size_t)m * ld_out + err_col] = __float2bfloat16_rn(g);
-            dzt[(size_t)err_col * rows + m] = __float2bfloat16_rn(g);
+            g_s[rr][err_col] = g;
         }
+        __syncwarp();
+        for (int j = lane; j < ld_out; j += 32) dz[(size_t)m * ld_out + j] = __float2bfloat16_rn(g_s[rr][j]);
     }
-    s_main[threadIdx.x] = lm;
-    s_err[threadIdx.x] = le;
     __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) {
-            s_main[threadIdx.x] += s_main[threadIdx.x + o];
-            s_err[threadIdx.x] += s_err[threadIdx.x + o];
-        }
-        __syncthreads();
+    // transposed copy: thread (j, r) with r fastest
+    for (int e = threadIdx.x; e < ld_out * MLP_LOSS_ROWS; e += blockDim.x) {
+        const int j = e / MLP_LOSS_ROWS, rr = e - j * MLP_LOSS_ROWS, m = m0 + rr;
+        if (m < rows) dzt[(size_t)j * rows + m] = __float2bfloat16_rn(g_s[rr][j]);
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lm += __shfl_xor_sync(0xffffffffu, lm, o);
+        le += __shfl_xor_sync(0xffffffffu, le, o);
+    }
+    if (lane == 0) {
+        s_main[warp] = lm;
+        s_err[warp] = le;
+    }
+    __syncthreads();
     if (threadIdx.x == 0 && loss) {
-        atomicAdd(loss, s_main[0] / (float)rows_valid);
-        atomicAdd(loss + 1, s_err[0] / (float)rows_valid);
+        float a = 0.f, b = 0.f;
+        for (int w = 0; w < 8; w++) {
+            a += s_main[w];
+            b += s_err[w];
+        }
+        atomicAdd(loss, a / (float)rows_valid);
+        atomicAdd(loss + 1, b / (float)rows_valid);
     }
 }
 
-// out[r] = sum_c xt[r][c]: one block per row.
-__global__ void k_mlp_colsum(const __nv_bfloat16* __restrict__ xt, int cols, float* __restrict__ out) {
-    __shared__ float s[256];
+// out[r] = sum_c xt[r][c]: one block per row; 16-byte loads (8 values)
+// when the row is 16-byte aligned and cols % 8 == 0, then warp shuffles.
+__global__ void __launch_bounds__(256) k_mlp_colsum(const __nv_bfloat16* __restrict__ xt, int cols,
+                                                    float* __restrict__ out) {
+    __shared__ float s[8];
     const __nv_bfloat16* row = xt + (size_t)blockIdx.x * cols;
     float acc = 0.f;
-    for (int c = threadIdx.x; c < cols; c += blockDim.x) acc += __bfloat162float(row[c]);
-    s[threadIdx.x] = acc;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
-        __syncthreads();
+    if ((cols & 7) == 0 && (((uintptr_t)row) & 15) == 0) {
+        const uint4* r4 = reinterpret_cast<const uint4*>(row);
+        for (int c = threadIdx.x; c < cols / 8; c += blockDim.x) {
+            const uint4 u = __ldg(r4 + c);
+            const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const float2 f = __bfloat1622float2(h[k]);
+                acc += f.x + f.y;
+            }
+        }
+    } else {
+        for (int c = threadIdx.x; c < cols; c += blockDim.x) acc += __bfloat162float(row[c]);
     }
-    if (threadIdx.x == 0) out[blockIdx.x] = s[0];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) a += s[w];
+        out[blockIdx.x] = a;
+    }
 }
 
 // Adam step on FP32 master weights from the sum of split-K partial gradients
@@ -644,6 +709,82 @@ __global__ void k_mlp_adam(const float* __restrict__ partials, int nsplit, const
     }
 }
 
+// The same update with the bf16 transposed copy written through a shared
+// tile: a block takes 32 x 32 weights (threads 32 columns x 8 rows, 4 rows
+// each), so both w16 rows and w16t rows leave as 64-byte runs.  Each
+// weight's arithmetic is the one of k_mlp_adam.
+__global__ void __launch_bounds__(256) k_mlp_adam_t(const float* __restrict__ partials, int nsplit,
+                                                    const float* __restrict__ gdir, float* __restrict__ w,
+                                                    float* __restrict__ m, float* __restrict__ v, float lr, float b1,
+                                                    float b2, float eps, float bc1, float bc2, int rows, int cols,
+                                                    __nv_bfloat16* __restrict__ w16, __nv_bfloat16* __restrict__ w16t,
+                                                    const float* __restrict__ hyper) {
+    __shared__ __nv_bfloat16 tile[32][34];
+    if (hyper) {
+        lr = hyper[0];
+        bc1 = hyper[1];
+        bc2 = hyper[2];
+    }
+    const long long n = (long long)rows * cols;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int tilesc = (cols + 31) / 32;
+    const int r0 = (blockIdx.x / tilesc) * 32, c0 = (blockIdx.x % tilesc) * 32;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int r = r0 + ty + 8 * k, c = c0 + tx;
+        if (r < rows && c < cols) {
+            const long long i = (long long)r * cols + c;
+            float g = gdir ? gdir[i] : 0.f;
+            for (int s = 0; s < nsplit; s++) g += partials[(size_t)s * n + i];
+            const float mi = b1 * m[i] + (1.f - b1) * g;
+            const float vi = b2 * v[i] + (1.f - b2) * g * g;
+            m[i] = mi;
+            v[i] = vi;
+            const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+            w[i] = wi;
+            const __nv_bfloat16 b = __float2bfloat16_rn(wi);
+            w16[i] = b;
+            tile[ty + 8 * k][tx] = b;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int c = c0 + ty + 8 * k, r = r0 + tx;
+        if (r < rows && c < cols) w16t[(size_t)c * rows + r] = tile[tx][ty + 8 * k];
+    }
+}
+
+// Start of a captured training step: rows perm[k * batch + b] of x_all and
+// t_all gathered into the step's minibatch (k = *k_in_epoch).
+__global__ void k_mlp_gather(const long long* __restrict__ perm, const long long* __restrict__ k_in_epoch,
+                             const float* __restrict__ x_all, int nxc, const float* __restrict__ t_all, int ntc,
+                             int batch, float* __restrict__ xb, float* __restrict__ tb) {
+    const long long k = *k_in_epoch;
+    const int w = nxc + ntc;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)batch * w;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int b = (int)(e / w), c = (int)(e - (long long)b * w);
+        const long long src = perm[k * batch + b];
+        if (c < nxc) xb[(size_t)b * nxc + c] = x_all[(size_t)src * nxc + c];
+        else tb[(size_t)b * ntc + (c - nxc)] = t_all[(size_t)src * ntc + (c - nxc)];
+    }
+}
+
+// Learning-rate schedule and Adam bias corrections of step g = *gstep
+// (from 0): hyper = {lr_min + (lr - lr_min) (1 + cos(pi g / total)) / 2,
+// 1 - b1^(g+1), 1 - b2^(g+1)}; then both step counters advance.  One thread.
+__global__ void k_mlp_schedule(long long* __restrict__ k_in_epoch, double* __restrict__ gstep,
+                               float* __restrict__ hyper, double lr, double lr_min, double total, double b1,
+                               double b2) {
+    const double g = *gstep;
+    hyper[0] = (float)(lr_min + 0.5 * (lr - lr_min) * (1.0 + cos(M_PI * g / total)));
+    hyper[1] = (float)(1.0 - pow(b1, g + 1.0));
+    hyper[2] = (float)(1.0 - pow(b2, g + 1.0));
+    *gstep = g + 1.0;
+    *k_in_epoch += 1;
+}
+
 static int mlp_grid(long long n) {
     long long b = (n + 255) / 256;
     long long cap = (long long)bt_sm_count() * 8;
@@ -657,6 +798,13 @@ cudaError_t bt_launch_mlp_pack(const float* x, int rows, int cols, int ld_out, i
         k_mlp_pack8<<<mlp_grid(nchunk), 256, 0, stream>>>(x, rows, cols, ld_out / 8, (int)nchunk, out);
         return cudaGetLastError();
     }
+    if (out_t) {
+        const long long tiles = (long long)((rows_out + 31) / 32) * ((ld_out + 31) / 32);
+        if (tiles < (1LL << 31)) {
+            k_mlp_pack_t<<<(unsigned)tiles, 256, 0, stream>>>(x, rows, cols, ld_out, rows_out, out, out_t);
+            return cudaGetLastError();
+        }
+    }
     k_mlp_pack<<<mlp_grid((long long)rows_out * ld_out), 256, 0, stream>>>(x, rows, cols, ld_out, rows_out, out, out_t);
     return cudaGetLastError();
 }
@@ -664,8 +812,24 @@ cudaError_t bt_launch_mlp_pack(const float* x, int rows, int cols, int ld_out, i
 cudaError_t bt_launch_mlp_loss(const float* y, int ldy, const float* t, const float* wt, int rows, int rows_valid,
                                int ncols, int err_col, float err_weight, int ld_out, __nv_bfloat16* dz,
                                __nv_bfloat16* dzt, float* loss, cudaStream_t stream) {
-    k_mlp_loss<<<(rows + 255) / 256, 256, 0, stream>>>(y, ldy, t, wt, rows, rows_valid, ncols, err_col, err_weight,
-                                                       ld_out, dz, dzt, loss);
+    if (ld_out > 128 || err_col >= ld_out) return cudaErrorInvalidValue;
+    k_mlp_loss<<<(rows + MLP_LOSS_ROWS - 1) / MLP_LOSS_ROWS, 256, 0, stream>>>(y, ldy, t, wt, rows, rows_valid, ncols,
+                                                                             err_col, err_weight, ld_out, dz, dzt,
+                                                                             loss);
+    return cudaGetLastError();
+}
+
+cudaError_t bt_launch_mlp_gather(const long long* perm, const long long* k_in_epoch, const float* x_all, int nxc,
+                                 const float* t_all, int ntc, int batch, float* xb, float* tb, cudaStream_t stream) {
+    if (batch <= 0) return cudaSuccess;
+    k_mlp_gather<<<mlp_grid((long long)batch * (nxc + ntc)), 256, 0, stream>>>(perm, k_in_epoch, x_all, nxc, t_all, ntc,
+                                                                              batch, xb, tb);
+    return cudaGetLastError();
+}
+
+cudaError_t bt_launch_mlp_schedule(long long* k_in_epoch, double* gstep, float* hyper, double lr, double lr_min,
+                                   double total, double b1, double b2, cudaStream_t stream) {
+    k_mlp_schedule<<<1, 1, 0, stream>>>(k_in_epoch, gstep, hyper, lr, lr_min, total, b1, b2);
     return cudaGetLastError();
 }
 
@@ -678,6 +842,12 @@ cudaError_t bt_launch_mlp_adam(const float* partials, int nsplit, const float* g
                                float* m, float* v, float lr, float b1, float b2, float eps, float bc1, float bc2,
                                int rows, int cols, __nv_bfloat16* w16, __nv_bfloat16* w16t, const float* hyper,
                                cudaStream_t stream) {
+    if (w16 && w16t && (long long)rows * cols == n) {
+        const long long tiles = (long long)((rows + 31) / 32) * ((cols + 31) / 32);
+        k_mlp_adam_t<<<(unsigned)tiles, 256, 0, stream>>>(partials, nsplit, grad_direct, w, m, v, lr, b1, b2, eps, bc1,
+                                                         bc2, rows, cols, w16, w16t, hyper);
+        return cudaGetLastError();
+    }
     k_mlp_adam<<<mlp_grid(n), 256, 0, stream>>>(partials, nsplit, grad_direct, n, w, m, v, lr, b1, b2, eps, bc1, bc2,
                                                 rows, cols, w16, w16t, hyper);
     return cudaGetLastError();
@@ -725,6 +895,50 @@ __global__ void k_surrogate_combine(const float* __restrict__ feat, int nfeat, i
             if (err_nm) err_nm[s] = scale * expf(y[(size_t)s * ldy + err_col]);
         }
     }
+}
+
+// Vignetting guard: one warp per sample, lanes over the group's kept
+// aperture margins k (K a multiple of 32, padding m0 = 3e38).  Predicted
+// margin m = m0[g][k] + sum_d jac[g][d][k] z[d] (z: the sample's normalised
+// dofs, the first ndof feature columns); the sample is flagged when any m
+// has the opposite sign of m0 or |m| < band_abs + band_rel |m - m0|, or
+// when some |z[d]| exceeds reach[d] (outside the box the margins were
+// chosen for).
+__global__ void k_surrogate_guard(const float* __restrict__ feat, int nfeat, int ndof, const int* __restrict__ grp,
+                                  const float* __restrict__ m0, const float* __restrict__ jac,
+                                  const float* __restrict__ reach, int K, float band_abs, float band_rel,
+                                  int* __restrict__ flag, int n) {
+    const int lane = threadIdx.x & 31;
+    const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long s = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); s < n; s += nw) {
+        const int g = grp[s];
+        const float* f = feat + (size_t)s * nfeat;
+        bool hit = false;
+        if (reach)
+            for (int d = lane; d < ndof; d += 32) hit |= !(fabsf(f[d]) <= reach[d]);
+        for (int k = lane; k < K; k += 32) {
+            const float a = m0[(size_t)g * K + k];
+            if (!(a < 1e38f)) continue;
+            float m = a;
+            const float* j = jac + (size_t)g * ndof * K + k;
+            for (int d = 0; d < ndof; d++) m = fmaf(j[(size_t)d * K], f[d], m);
+            const float side = (a >= 0.f) ? m : -m;
+            hit |= side < band_abs + band_rel * fabsf(m - a);
+        }
+        const unsigned any = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) flag[s] = any != 0u;
+    }
+}
+
+cudaError_t bt_launch_surrogate_guard(const float* feat, int nfeat, int ndof, const int* grp, const float* m0,
+                                      const float* jac, const float* reach, int K, float band_abs, float band_rel,
+                                      int* flag, int n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    const long long need = ((long long)n + 7) / 8;  // 8 warps (samples) per block
+    const int blocks = (int)(need < 152 * 16 ? need : 152 * 16);
+    k_surrogate_guard<<<blocks, 256, 0, stream>>>(feat, nfeat, ndof, grp, m0, jac, reach, K, band_abs, band_rel, flag,
+                                                  n);
+    return cudaGetLastError();
 }
 
 cudaError_t bt_launch_surrogate_combine(const float* feat, int nfeat, int nlin, const int* grp, const float* theta,

@@ -208,6 +208,7 @@ class WavefrontSurrogate:
         self.theta = None
         self.scale = 1.0
         self.kappa = 1.0
+        self.guard = None
 
     # -- data ----------------------------------------------------------------------
     def sample_states(self, nstates, seed, widen=1.0):
@@ -276,6 +277,47 @@ class WavefrontSurrogate:
         r = (coefs.reshape(-1, self.J + 1)[:, 1:] - self.linear(feat, grp)) * w[:, None] * 1e9
         return r
 
+    def _fit_linear_device(self, feat, grp, w, coefs):
+        """fit_linear and residual_targets with the sample-sized work on the
+        device (FP64): samples sorted by group, each group's normal equations
+        A^T A and A^T c by one matrix product, the (ndof+1)-sized systems
+        solved on the host.  Returns the residuals (nm) as a device tensor."""
+        dev = D.device()
+        nd = self.pt.ndof
+        G = self.F * len(self.wavelengths)
+        n = len(feat)
+        g = torch.from_numpy(np.ascontiguousarray(grp, dtype=np.int64)).to(dev)
+        order = torch.argsort(g, stable=True)
+        counts = torch.bincount(g, minlength=G).cpu().numpy()
+        A = torch.ones((n, nd + 1), dtype=torch.float64, device=dev)
+        A[:, 1:] = torch.from_numpy(np.ascontiguousarray(feat[:, :nd])).to(dev)[order].double()
+        C = torch.from_numpy(np.ascontiguousarray(coefs.reshape(-1, self.J + 1)[:, 1:])).to(dev)[order]
+        starts = np.concatenate([[0], np.cumsum(counts)])
+        ata = torch.zeros((G, nd + 1, nd + 1), dtype=torch.float64, device=dev)
+        atc = torch.zeros((G, nd + 1, self.J), dtype=torch.float64, device=dev)
+        for k in range(G):
+            if counts[k]:
+                a = A[starts[k]:starts[k + 1]]
+                ata[k] = a.T @ a
+                atc[k] = a.T @ C[starts[k]:starts[k + 1]]
+        ata, atc = ata.cpu().numpy(), atc.cpu().numpy()
+        self.theta = np.zeros((G, nd + 1, self.J))
+        self._theta_d = None
+        for k in range(G):
+            if counts[k]:
+                try:
+                    self.theta[k] = np.linalg.solve(ata[k], atc[k])
+                except np.linalg.LinAlgError:
+                    self.theta[k] = np.linalg.lstsq(ata[k], atc[k], rcond=None)[0]
+        th = torch.from_numpy(self.theta).to(dev)
+        for k in range(G):
+            if counts[k]:
+                sl = slice(starts[k], starts[k + 1])
+                C[sl] -= A[sl] @ th[k]
+        r = torch.empty_like(C)
+        r[order] = C * torch.from_numpy(np.ascontiguousarray(w, dtype=np.float64)).to(dev)[order, None] * 1e9
+        return r
+
     def train(self, feat, grp, w, coefs, epochs=30, batch=8192, lr=1e-3, lr_min=1e-5, err_weight=0.05, seed=0,
               log=None, graph=True):
         """Fits the linear model, then trains the MLP on its residuals.
@@ -288,13 +330,14 @@ class WavefrontSurrogate:
 
         Minibatches are drawn from a device permutation per epoch (seeded
         generator).  self.timing afterwards holds the wall time of the
-        linear fit (host) and of the network training (device steps)."""
+        linear fit (device products, host solves) and of the network
+        training (device steps)."""
         import time
         t0 = time.perf_counter()
-        self.fit_linear(feat, grp, coefs)
-        r = self.residual_targets(feat, grp, w, coefs)
-        self.scale = float(np.sqrt(np.mean(r ** 2)))
-        t_all = torch.from_numpy((r / self.scale).astype(np.float32)).to(D.device())
+        r = self._fit_linear_device(feat, grp, w, coefs)
+        self.scale = float(torch.sqrt(torch.mean(r * r)).item())
+        t_all = (r / self.scale).float().contiguous()
+        del r
         x_all = torch.from_numpy(feat).to(D.device())
         torch.cuda.synchronize()
         t1 = time.perf_counter()
@@ -339,7 +382,6 @@ class WavefrontSurrogate:
     def _train_graph(self, x_all, t_all, epochs, steps_per_epoch, batch, lr, lr_min, err_weight, perm_of_epoch, log,
                      b1=0.9, b2=0.999):
         net, dev = self.net, D.device()
-        n = x_all.shape[0]
         total = epochs * steps_per_epoch
         perm = torch.empty((steps_per_epoch, batch), dtype=torch.int64, device=dev)
         k_in_epoch = torch.zeros(1, dtype=torch.int64, device=dev)
@@ -347,23 +389,22 @@ class WavefrontSurrogate:
         hyper = torch.empty(3, dtype=torch.float32, device=dev)
         xb = torch.empty((batch, x_all.shape[1]), dtype=torch.float32, device=dev)
         tb = torch.empty((batch, t_all.shape[1]), dtype=torch.float32, device=dev)
-        b1t = torch.tensor(b1, dtype=torch.float64, device=dev)
-        b2t = torch.tensor(b2, dtype=torch.float64, device=dev)
+
+        L = _lib.lib()
+        nxc, ntc = x_all.shape[1], t_all.shape[1]
 
         def body():
-            idx = perm.index_select(0, k_in_epoch).view(-1)
-            torch.index_select(x_all, 0, idx, out=xb)
-            torch.index_select(t_all, 0, idx, out=tb)
+            # minibatch gather, network step, then the device schedule
+            # (learning rate and Adam bias corrections of this step; it
+            # advances both step counters) and Adam
+            _lib.check(L.bt_mlp_gather(perm.data_ptr(), k_in_epoch.data_ptr(), x_all.data_ptr(), nxc, t_all.data_ptr(),
+                                       ntc, batch, xb.data_ptr(), tb.data_ptr(), D.stream_ptr()))
             bf = net.pack(xb, batch, True)
             net.forward(bf, batch, True)
             net.backward(bf, batch, tb, batch, err_col=self.J, err_weight=err_weight)
-            # cosine schedule and Adam bias corrections of step g (from 0)
-            cur = lr_min + 0.5 * (lr - lr_min) * (1.0 + torch.cos(np.pi * gstep / max(total, 1)))
-            sched = torch.cat([cur, 1.0 - torch.pow(b1t, gstep + 1), 1.0 - torch.pow(b2t, gstep + 1)])
-            hyper.copy_(sched.to(torch.float32))
+            _lib.check(L.bt_mlp_schedule(k_in_epoch.data_ptr(), gstep.data_ptr(), hyper.data_ptr(), float(lr),
+                                         float(lr_min), max(total, 1), float(b1), float(b2), D.stream_ptr()))
             net.adam(bf, 0.0, b1=b1, b2=b2, hyper=hyper)
-            k_in_epoch.add_(1)
-            gstep.add_(1)
             return bf
 
         stream = torch.cuda.Stream()
@@ -419,22 +460,42 @@ class WavefrontSurrogate:
         out, err = self.predict_device(feat_d, grp_d, w_d)
         return D.to_host(out), D.to_host(err)
 
+    def build_guard(self, **kw):
+        """The vignetting guard of this surrogate's pupil grid, fields and
+        wavelengths (vignetting.VignettingGuard): samples whose dofs may
+        move a grid ray across an aperture edge fall back to the trace."""
+        from .vignetting import VignettingGuard
+        self.guard = VignettingGuard(self.pt, self.wavelengths, self.nx, self.dof_scale, **kw)
+        return self.guard
+
+    def guard_flags(self, feat, grp):
+        """Host bool flags of the vignetting guard (all False without one)."""
+        if self.guard is None:
+            return np.zeros(len(feat), dtype=bool)
+        f = self.guard.flags_device(torch.from_numpy(feat).to(D.device()), torch.from_numpy(grp).to(D.device()))
+        return D.to_host(f).astype(bool)
+
     def calibrate(self, feat, grp, w, coefs, quantile=0.99):
         """Safety factor on the predicted error: the given quantile of
-        actual / predicted over a validation set."""
+        actual / predicted over a validation set (the samples the vignetting
+        guard does not already send to the trace)."""
         pred, err = self.predict(feat, grp, w)
         actual = rms_nm(pred, coefs.reshape(-1, self.J + 1), w)
-        self.kappa = float(np.quantile(actual / np.maximum(err, 1e-6), quantile))
+        keep = ~self.guard_flags(feat, grp)
+        if not np.any(keep):
+            keep[:] = True
+        self.kappa = float(np.quantile(actual[keep] / np.maximum(err[keep], 1e-6), quantile))
         return self.kappa
 
     def with_fallback(self, dofs, widx, threshold_nm=2.0, threads=None, ctas_per_sm=None):
         """(coefs (S, F, J+1), traced mask (S, F)): surrogate where its
-        calibrated error estimate is within the threshold, batched trace
+        calibrated error estimate is within the threshold and the vignetting
+        guard (when built) sees no aperture crossing, batched trace
         elsewhere."""
         feat, grp, w = self.features(dofs, widx)
         pred, err = self.predict(feat, grp, w)
         S, F = len(dofs), self.F
-        fb = (self.kappa * err > threshold_nm).reshape(S, F)
+        fb = ((self.kappa * err > threshold_nm) | self.guard_flags(feat, grp)).reshape(S, F)
         out = pred.reshape(S, F, self.J + 1)
         if np.any(fb):
             traced = self.trace_jobs(dofs, widx, np.flatnonzero(fb.ravel()), threads, ctas_per_sm)

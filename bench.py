@@ -47,6 +47,7 @@ def parse():
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--batch-states", type=int, default=4096)
     p.add_argument("--no-surrogate", action="store_true")
+    p.add_argument("--no-guard", action="store_true", help="surrogate without the vignetting guard")
     p.add_argument("--surrogate-samples", type=int, default=2_000_000)
     p.add_argument("--surrogate-epochs", type=int, default=24)
     return p.parse_args()
@@ -569,7 +570,8 @@ def bench_batched(bt, nstates=4096, reps=3, cpu=True, fp64_peak_tflops=None):
     return out
 
 
-def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24, threshold_nm=2.0, cpu=True):
+def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24, threshold_nm=2.0, cpu=True,
+                    guard_on=True):
     """Learned surrogate: MLP 33 -> 4 x 512 GELU -> 28 (+ error head), BF16
     tensor-core kernels with FP32 accumulation, trained on batched-trace
     data (nx 32 pupil grids, 9 fields, 6 wavelengths); evaluated on held-out
@@ -596,6 +598,9 @@ def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24,
     sur.train(feat, grp, w, coefs, epochs=epochs, batch=8192, lr=1e-3)
     train_s = time.perf_counter() - t1
     steps = epochs * (len(feat) // 8192)
+    t1 = time.perf_counter()
+    guard = sur.build_guard() if guard_on else None
+    guard_s = time.perf_counter() - t1
     vd, vw = sur.sample_states(4096, seed=202)
     vc = sur.trace(vd, vw, threads=threads, ctas_per_sm=ctas)
     vf, vg, vwl = sur.features(vd, vw)
@@ -625,21 +630,29 @@ def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24,
     w_d = D.to_device(hwl)
     out = torch.empty((N, 29), dtype=torch.float64, device=D.device())
     err = torch.empty(N, dtype=torch.float32, device=D.device())
+    gflag = torch.zeros(N, dtype=torch.int32, device=D.device())
+
+    def infer():
+        sur.predict_device(feat_d, grp_d, w_d, out, err)
+        if guard is not None:
+            guard.flags_device(feat_d, grp_d, gflag)
+
     with torch.cuda.stream(stream):
         # untimed first pass, marked for profilers (ncu --nvtx-include "surrogate_inference/")
         torch.cuda.nvtx.range_push("surrogate_inference")
-        sur.predict_device(feat_d, grp_d, w_d, out, err)
+        infer()
         torch.cuda.nvtx.range_pop()
         stream.synchronize()
         e0.record(stream)
         for _ in range(10):
-            sur.predict_device(feat_d, grp_d, w_d, out, err)
+            infer()
         e1.record(stream)
         stream.synchronize()
     infer_ms = e0.elapsed_time(e1) / 10
     pred = D.to_host(out)
     perr = D.to_host(err) * kappa
-    fb = perr > threshold_nm
+    gfl = D.to_host(gflag).astype(bool)
+    fb = (perr > threshold_nm) | gfl
     jobs = np.flatnonzero(fb)
     fb_ms = 0.0
     if len(jobs):
@@ -724,7 +737,16 @@ def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24,
         "roofline_inference": {"bound": "tensor", "achieved": infer_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
                                "frac": infer_tflops / bf16_peak, "flops_per_sample": flops_fwd,
                                "note": "whole inference pipeline (pack, 5 GEMMs, combine) over its event time"},
-        "gpu_launches_per_inference": 7,
+        "gpu_launches_per_inference": 8 if guard is not None else 7,
+        "vignetting_guard": None if guard is None else {
+            "flagged_fraction": float(np.mean(gfl)), "fallback_by_error_head_only": float(np.mean(perr > threshold_nm)),
+            "kept_margins_per_group_max": int(guard.nkept.max()),
+            "kept_margins_per_group_mean": float(guard.nkept.mean()), "groups": int(guard.G), "build_s": guard_s,
+            "flagged_and_above_threshold_raw": int(np.sum(gfl & (e_raw > threshold_nm))),
+            "above_threshold_raw": int(np.sum(e_raw > threshold_nm)),
+            "note": "first-order model of the aperture margins of the nx 32 grid rays (central differences of "
+                    "traceFull on the nominal optic); a sample whose predicted margins may cross an aperture "
+                    "edge falls back to the batched trace"},
         "largest_errors": outliers,
         "above_threshold_profile": tail_profile,
     }
@@ -831,7 +853,8 @@ def run_gpu(args):
                                 fp64_peak_tflops=fpeak.value)
     surrogate = None
     if rank == 0 and not args.no_surrogate:
-        surrogate = bench_surrogate(bt, train_samples=args.surrogate_samples, epochs=args.surrogate_epochs)
+        surrogate = bench_surrogate(bt, train_samples=args.surrogate_samples, epochs=args.surrogate_epochs,
+                                    guard_on=not args.no_guard)
 
     if rank == 0:
         line = {

@@ -432,6 +432,29 @@ int bt_surrogate_combine(const float* feat, int nfeat, int nlin, const int* grp,
                          int ldy, const double* wl, double scale, int J, int err_col, double* out, float* err_nm,
                          int n, void* stream);
 
+/* Start of a training step captured in a CUDA graph (no reference
+ * counterpart): rows perm[k * batch + b] (k = *k_in_epoch, read on the
+ * device) of x_all [.][nxc] and t_all [.][ntc] into xb [batch][nxc] and
+ * tb [batch][ntc]. */
+int bt_mlp_gather(const long long* perm, const long long* k_in_epoch, const float* x_all, int nxc,
+                  const float* t_all, int ntc, int batch, float* xb, float* tb, void* stream);
+
+/* Writes hyper = {lr_min + (lr - lr_min) (1 + cos(pi g / total)) / 2,
+ * 1 - b1^(g+1), 1 - b2^(g+1)} for step g = *gstep (from 0), the array
+ * bt_mlp_adam_dev reads, then advances *gstep and *k_in_epoch by one. */
+int bt_mlp_schedule(long long* k_in_epoch, double* gstep, float* hyper, double lr, double lr_min, long long total,
+                    double b1, double b2, void* stream);
+
+/* Vignetting guard of the surrogate (no reference counterpart): for sample s
+ * in group grp[s], with z = feat[s][0..ndof) (normalised dofs), the kept
+ * aperture margins of its group m = m0[g][k] + sum_d jac[g][d][k] z[d]
+ * (m0: [groups][K], K a multiple of 32, entries >= 1e38 unused; jac:
+ * [groups][ndof][K]); flag[s] = 1 when any m has the opposite sign of m0[g][k]
+ * or |m| < band_abs + band_rel * |m - m0[g][k]|, or when reach (may be null;
+ * [ndof]) is given and some |z[d]| > reach[d]; else 0. */
+int bt_surrogate_guard(const float* feat, int nfeat, int ndof, const int* grp, const float* m0, const float* jac,
+                       const float* reach, int K, double band_abs, double band_rel, int* flag, int n, void* stream);
+
 /* Measures the device's FP64 FMA throughput (TFLOP/s, 2 flops per FMA)
  * with independent DFMA chains; `iters` FMAs per chain (e.g. 1 << 14).
  * The denominator of the tracer's FP64 roofline.  Synchronous. */

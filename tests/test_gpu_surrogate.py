@@ -118,3 +118,59 @@ def test_graph_captured_training_matches_launch_by_launch():
         runs.append([D.to_host(x) for x in sur.net.W])
     for a, b in zip(*runs):
         np.testing.assert_allclose(a, b, rtol=1e-4, atol=1e-6 * np.abs(b).max())
+
+
+def test_vignetting_guard_flags_every_aperture_crossing():
+    """The guard's first-order aperture margins (vignetting.py) predict the
+    traced margins of the kept (surface, ray) pairs within their band, and
+    every (state, field, wavelength) sample whose traced grid vignetting
+    differs from the nominal one is flagged: states at the corners of the
+    rigid-dof box (the largest beam shifts) and typical states; dofs outside
+    the box are flagged as such."""
+    modes = ModeSet(nmodes=8, n=128, seed=5)
+    optic = workloads.tma_optic(bt)
+    fields = np.deg2rad([[0.0, 0.0], [0.8, -0.5], [-1.0, 0.9]])
+    pt = PerturbedTelescope(optic, modes=modes, fields=fields)
+    sur = WavefrontSurrogate(pt, wavelengths=[500e-9, 800e-9], nx=24, hidden=256, layers=2, seed=1)
+    guard = sur.build_guard()
+    assert guard.nkept.max() > 0
+    rays = guard._grid_rays()
+    N = guard.nx ** 2
+    nominal = pt.perturbed(np.zeros(pt.ndof)).trace(rays.copy()).vignetted.reshape(guard.G, N)
+    nr = 5 * len(pt.rigid)
+    typical, widx_t = sur.sample_states(60, seed=7)
+    corner, widx_c = sur.sample_states(60, seed=8)
+    sign = np.where(np.random.default_rng(9).uniform(size=(60, nr)) < 0.5, -1.0, 1.0)
+    corner[:, :nr] = 0.999 * sign * sur.dof_scale[:nr]
+    nflips = 0
+    for dofs, widx, typ in ((typical, widx_t, True), (corner, widx_c, False)):
+        feat, grp, w = sur.features(dofs, widx)
+        flags = sur.guard_flags(feat, grp).reshape(len(dofs), len(fields))
+        flips = np.zeros_like(flags)
+        worst = 0.0
+        for s in range(len(dofs)):
+            opt = pt.perturbed(dofs[s])
+            vig = opt.trace(rays.copy()).vignetted.reshape(guard.G, N)
+            marg = guard._margins(opt, rays)
+            for f in range(len(fields)):
+                g = f * 2 + widx[s]
+                flips[s, f] = np.any(vig[g] != nominal[g])
+                k = guard.nkept[g]
+                if k == 0:
+                    continue
+                si, ri = guard.where[g]
+                z = dofs[s] / guard.dof_scale
+                pred = guard.m0[g, :k] + z @ guard.jac[g, :, :k]
+                actual = marg[si, g * N + ri]
+                band = guard.band_abs + guard.band_rel * np.abs(pred - guard.m0[g, :k])
+                worst = max(worst, float(np.max(np.abs(pred - actual) / band)))
+        assert worst < 0.5, worst
+        assert np.all(flags[flips])
+        nflips += int(flips.sum())
+        if typ:
+            assert flags.mean() < 0.2
+    assert nflips > 0
+    out = typical[:1].copy()
+    out[0, 0] = 1.5 * sur.dof_scale[0]
+    feat, grp, w = sur.features(out, widx_t[:1])
+    assert np.all(sur.guard_flags(feat, grp))

@@ -1,0 +1,67 @@
+"""Host logic of the surrogate's vignetting guard (batoid_gb300/vignetting.py):
+aperture margins against the oracle's obscuration test, and the choice of
+the margins to keep."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+
+
+def _obscurations():
+    import batoid_gb300 as bt
+    c = bt.ObscCircle(0.4, 0.05, -0.02)
+    a = bt.ObscAnnulus(0.2, 0.6, -0.03, 0.01)
+    return [c, a, bt.ObscNegation(c), bt.ObscNegation(a),
+            bt.ObscUnion(bt.ObscCircle(0.1), bt.ObscNegation(bt.ObscCircle(0.5))),
+            bt.ObscIntersection(bt.ObscNegation(bt.ObscCircle(0.1, 0.3, 0.0)), bt.ObscAnnulus(0.05, 0.7))]
+
+
+@pytest.mark.parametrize("k", range(6))
+def test_margin_sign_matches_oracle_obscuration(k):
+    """margin < 0 exactly where the oracle's restatement of the reference's
+    obscuration test (src/obscuration.cpp) obscures, away from the edge."""
+    import oracle as ora
+    from batoid_gb300.vignetting import obscuration_margin
+    ob = _obscurations()[k]
+    rng = np.random.default_rng(k)
+    x, y = rng.uniform(-0.8, 0.8, (2, 4000))
+    m = obscuration_margin(ob, x, y)
+    far = np.abs(m) > 1e-9
+    obscured = ora.contains(ob, x, y)
+    assert np.array_equal(obscured[far], (m < 0)[far])
+
+
+def test_margin_is_distance_to_edge():
+    import batoid_gb300 as bt
+    from batoid_gb300.vignetting import obscuration_margin
+    ob = bt.ObscNegation(bt.ObscAnnulus(1.0, 2.0))
+    m = obscuration_margin(ob, np.array([1.5, 1.1, 2.3, 0.0]), np.zeros(4))
+    np.testing.assert_allclose(m, [0.5, 0.1, -0.3, -1.0], atol=1e-15)
+    assert np.all(np.isinf(obscuration_margin(None, np.zeros(3), np.zeros(3))))
+    with pytest.raises(NotImplementedError):
+        obscuration_margin(bt.ObscRectangle(1.0, 1.0), np.zeros(2), np.zeros(2))
+
+
+def test_select_constraints():
+    """Kept: margins that can reach zero in the dof box; dropped: rays
+    vignetted for sure elsewhere, failed rays, far margins, no aperture."""
+    from batoid_gb300.vignetting import select_constraints
+    S, N, nd = 2, 5, 2
+    m0 = np.array([[1e-3, -2e-4, 5e-2, 1e-4, np.inf],
+                   [3e-2, 4e-2, -1e-1, np.nan, 2e-4]])
+    jac = np.zeros((S, N, nd))
+    jac[0, :, 0] = 1e-3      # reach 1e-3 m per unit of dof 0 at surface 0
+    jac[1, :, 1] = 1e-4
+    s, i = select_constraints(m0, jac, scale=np.array([1.0, 1.0]), widen=1.2, band_abs=0.0)
+    kept = set(zip(s.tolist(), i.tolist()))
+    # ray 0: surface 0 margin 1e-3 < 1.2e-3 -> kept; surface 1 far
+    # ray 1: surface 0 margin -2e-4 (near) -> kept
+    # ray 2: surface 1 margin -0.1 (sure vignetting) -> nothing kept
+    # ray 3: failed -> nothing kept
+    # ray 4: no aperture at surface 0; surface 1 margin 2e-4 > 1.2e-4 -> not kept
+    assert kept == {(0, 0), (0, 1)}
+    s, i = select_constraints(m0, jac, scale=np.array([1.0, 3.0]), widen=1.2, band_abs=0.0)
+    assert (1, 4) in set(zip(s.tolist(), i.tolist()))
