@@ -186,7 +186,7 @@ _SIGS = [
     ("bt_surrogate_combine", c_int, [_P, c_int, c_int, _P, _P, _P, c_int, _P, c_double, c_int, c_int, _P, _P, c_int,
                                      _P]),
     ("bt_mlp_gather", c_int, [_P, _P, _P, c_int, _P, c_int, c_int, _P, _P, _P]),
-    ("bt_mlp_schedule", c_int, [_P, _P, _P, c_double, c_double, ctypes.c_longlong, c_double, c_double, _P]),
+    ("bt_mlp_schedule", c_int, [_P, _P, _P, ctypes.c_longlong, _P, _P]),
     ("bt_surrogate_guard", c_int, [_P, c_int, c_int, _P, _P, _P, _P, c_int, c_double, c_double, _P, c_int, _P]),
     ("bt_measure_fp64_peak", c_int, [c_int, c_double_p, _P]),
     ("bt_measure_fp32_peak", c_int, [c_int, c_double_p, _P]),

@@ -43,8 +43,8 @@ cudaError_t bt_launch_surrogate_combine(const float* feat, int nfeat, int nlin, 
                                         double* out, float* err_nm, int n, cudaStream_t stream);
 cudaError_t bt_launch_mlp_gather(const long long* perm, const long long* k_in_epoch, const float* x_all, int nxc,
                                  const float* t_all, int ntc, int batch, float* xb, float* tb, cudaStream_t stream);
-cudaError_t bt_launch_mlp_schedule(long long* k_in_epoch, double* gstep, float* hyper, double lr, double lr_min,
-                                   double total, double b1, double b2, cudaStream_t stream);
+cudaError_t bt_launch_mlp_schedule(long long* k_in_epoch, long long* step, const float* table, long long total,
+                                   float* hyper, cudaStream_t stream);
 cudaError_t bt_launch_surrogate_guard(const float* feat, int nfeat, int ndof, const int* grp, const float* m0,
                                       const float* jac, const float* reach, int K, float band_abs, float band_rel,
                                       int* flag, int n, cudaStream_t stream);

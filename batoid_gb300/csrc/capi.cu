@@ -1453,13 +1453,10 @@ extern "C" int bt_mlp_gather(const long long* perm, const long long* k_in_epoch,
     return BT_OK;
 }
 
-extern "C" int bt_mlp_schedule(long long* k_in_epoch, double* gstep, float* hyper, double lr, double lr_min,
-                               long long total, double b1, double b2, void* stream) {
-    if (!k_in_epoch || !gstep || !hyper || total < 1 || !(lr > 0.0) || !(b1 > 0.0 && b1 < 1.0) ||
-        !(b2 > 0.0 && b2 < 1.0))
-        return fail(BT_ERR_ARG, "mlp schedule: bad arguments");
-    CUDA_TRY(bt_launch_mlp_schedule(k_in_epoch, gstep, hyper, lr, lr_min, (double)total, b1, b2, (cudaStream_t)stream),
-             "mlp schedule");
+extern "C" int bt_mlp_schedule(long long* k_in_epoch, long long* step, const float* table, long long total,
+                               float* hyper, void* stream) {
+    if (!k_in_epoch || !step || !table || !hyper || total < 1) return fail(BT_ERR_ARG, "mlp schedule: bad arguments");
+    CUDA_TRY(bt_launch_mlp_schedule(k_in_epoch, step, table, total, hyper, (cudaStream_t)stream), "mlp schedule");
     return BT_OK;
 }
 

@@ -709,49 +709,82 @@ __global__ void k_mlp_adam(const float* __restrict__ partials, int nsplit, const
     }
 }
 
-// The same update with the bf16 transposed copy written through a shared
-// tile: a block takes 32 x 32 weights (threads 32 columns x 8 rows, 4 rows
-// each), so both w16 rows and w16t rows leave as 64-byte runs.  Each
-// weight's arithmetic is the one of k_mlp_adam.
+// The same update for a weight matrix with both bf16 copies: a block takes
+// 8 rows x 128 columns, each thread 4 consecutive columns of a row with
+// 16-byte loads and stores (the split-K partials are the bulk of the
+// traffic); the transposed copy goes through a shared tile so that w16t
+// rows leave as 32-byte runs.  Needs cols % 4 == 0 and 16-byte aligned
+// arrays; each weight's arithmetic is the one of k_mlp_adam.
 __global__ void __launch_bounds__(256) k_mlp_adam_t(const float* __restrict__ partials, int nsplit,
                                                     const float* __restrict__ gdir, float* __restrict__ w,
                                                     float* __restrict__ m, float* __restrict__ v, float lr, float b1,
                                                     float b2, float eps, float bc1, float bc2, int rows, int cols,
                                                     __nv_bfloat16* __restrict__ w16, __nv_bfloat16* __restrict__ w16t,
                                                     const float* __restrict__ hyper) {
-    __shared__ __nv_bfloat16 tile[32][34];
+    __shared__ __nv_bfloat16 tile[8][130];
     if (hyper) {
         lr = hyper[0];
         bc1 = hyper[1];
         bc2 = hyper[2];
     }
     const long long n = (long long)rows * cols;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int tilesc = (cols + 31) / 32;
-    const int r0 = (blockIdx.x / tilesc) * 32, c0 = (blockIdx.x % tilesc) * 32;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const int r = r0 + ty + 8 * k, c = c0 + tx;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 4 columns, 8 rows
+    const int tilesc = (cols + 127) / 128;
+    const int r0 = (blockIdx.x / tilesc) * 8, c0 = (blockIdx.x % tilesc) * 128;
+    {
+        const int rr = ty, r = r0 + rr, c = c0 + 4 * tx;
         if (r < rows && c < cols) {
             const long long i = (long long)r * cols + c;
-            float g = gdir ? gdir[i] : 0.f;
-            for (int s = 0; s < nsplit; s++) g += partials[(size_t)s * n + i];
-            const float mi = b1 * m[i] + (1.f - b1) * g;
-            const float vi = b2 * v[i] + (1.f - b2) * g * g;
-            m[i] = mi;
-            v[i] = vi;
-            const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
-            w[i] = wi;
-            const __nv_bfloat16 b = __float2bfloat16_rn(wi);
-            w16[i] = b;
-            tile[ty + 8 * k][tx] = b;
+            float4 g = gdir ? *reinterpret_cast<const float4*>(gdir + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 4
+            for (int s = 0; s < nsplit; s++) {
+                const float4 p = __ldcs(reinterpret_cast<const float4*>(partials + (size_t)s * n + i));
+                g.x += p.x;
+                g.y += p.y;
+                g.z += p.z;
+                g.w += p.w;
+            }
+            float4 mv = *reinterpret_cast<float4*>(m + i), vv = *reinterpret_cast<float4*>(v + i),
+                   wv = *reinterpret_cast<float4*>(w + i);
+            float* gp = &g.x;
+            float* mp = &mv.x;
+            float* vp = &vv.x;
+            float* wp = &wv.x;
+            __align__(8) __nv_bfloat16 b[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float mi = b1 * mp[q] + (1.f - b1) * gp[q];
+                const float vi = b2 * vp[q] + (1.f - b2) * gp[q] * gp[q];
+                mp[q] = mi;
+                vp[q] = vi;
+                wp[q] = wp[q] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+                b[q] = __float2bfloat16_rn(wp[q]);
+                tile[rr][4 * tx + q] = b[q];
+            }
+            *reinterpret_cast<float4*>(m + i) = mv;
+            *reinterpret_cast<float4*>(v + i) = vv;
+            *reinterpret_cast<float4*>(w + i) = wv;
+            *reinterpret_cast<uint2*>(w16 + i) = *reinterpret_cast<const uint2*>(b);
         }
     }
     __syncthreads();
+    // transposed copy: 128 columns x 8 rows, thread c < 128 writes column c's
+    // 8 rows, one 16-byte store when they are whole and aligned
+    const bool vec = (rows % 8 == 0) && ((((uintptr_t)w16t) & 15) == 0);
+    for (int cc = threadIdx.x; cc < 128; cc += blockDim.x) {
+        const int c = c0 + cc;
+        if (c >= cols) continue;
+        if (vec && r0 + 8 <= rows) {
+            __align__(16) __nv_bfloat16 b[8];
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const int c = c0 + ty + 8 * k, r = r0 + tx;
-        if (r < rows && c < cols) w16t[(size_t)c * rows + r] = tile[tx][ty + 8 * k];
+            for (int q = 0; q < 8; q++) b[q] = tile[q][cc];
+            *reinterpret_cast<uint4*>(w16t + (size_t)c * rows + r0) = *reinterpret_cast<const uint4*>(b);
+        } else {
+            for (int q = 0; q < 8; q++) {
+                const int r = r0 + q;
+                if (r < rows) w16t[(size_t)c * rows + r] = tile[q][cc];
+            }
+        }
     }
 }
 
@@ -771,17 +804,16 @@ __global__ void k_mlp_gather(const long long* __restrict__ perm, const long long
     }
 }
 
-// Learning-rate schedule and Adam bias corrections of step g = *gstep
-// (from 0): hyper = {lr_min + (lr - lr_min) (1 + cos(pi g / total)) / 2,
-// 1 - b1^(g+1), 1 - b2^(g+1)}; then both step counters advance.  One thread.
-__global__ void k_mlp_schedule(long long* __restrict__ k_in_epoch, double* __restrict__ gstep,
-                               float* __restrict__ hyper, double lr, double lr_min, double total, double b1,
-                               double b2) {
-    const double g = *gstep;
-    hyper[0] = (float)(lr_min + 0.5 * (lr - lr_min) * (1.0 + cos(M_PI * g / total)));
-    hyper[1] = (float)(1.0 - pow(b1, g + 1.0));
-    hyper[2] = (float)(1.0 - pow(b2, g + 1.0));
-    *gstep = g + 1.0;
+// hyper = table[step] ({lr, bc1, bc2} of the step, computed on the host),
+// then both step counters advance.  One thread.
+__global__ void k_mlp_schedule(long long* __restrict__ k_in_epoch, long long* __restrict__ step,
+                               const float* __restrict__ table, long long total, float* __restrict__ hyper) {
+    long long g = *step;
+    if (g >= total) g = total - 1;
+    hyper[0] = table[3 * g];
+    hyper[1] = table[3 * g + 1];
+    hyper[2] = table[3 * g + 2];
+    *step += 1;
     *k_in_epoch += 1;
 }
 
@@ -827,9 +859,9 @@ cudaError_t bt_launch_mlp_gather(const long long* perm, const long long* k_in_ep
     return cudaGetLastError();
 }
 
-cudaError_t bt_launch_mlp_schedule(long long* k_in_epoch, double* gstep, float* hyper, double lr, double lr_min,
-                                   double total, double b1, double b2, cudaStream_t stream) {
-    k_mlp_schedule<<<1, 1, 0, stream>>>(k_in_epoch, gstep, hyper, lr, lr_min, total, b1, b2);
+cudaError_t bt_launch_mlp_schedule(long long* k_in_epoch, long long* step, const float* table, long long total,
+                                   float* hyper, cudaStream_t stream) {
+    k_mlp_schedule<<<1, 1, 0, stream>>>(k_in_epoch, step, table, total, hyper);
     return cudaGetLastError();
 }
 
@@ -842,8 +874,10 @@ cudaError_t bt_launch_mlp_adam(const float* partials, int nsplit, const float* g
                                float* m, float* v, float lr, float b1, float b2, float eps, float bc1, float bc2,
                                int rows, int cols, __nv_bfloat16* w16, __nv_bfloat16* w16t, const float* hyper,
                                cudaStream_t stream) {
-    if (w16 && w16t && (long long)rows * cols == n) {
-        const long long tiles = (long long)((rows + 31) / 32) * ((cols + 31) / 32);
+    const bool aligned = ((((uintptr_t)partials | (uintptr_t)grad_direct | (uintptr_t)w | (uintptr_t)m |
+                            (uintptr_t)v) & 15) == 0) && ((((uintptr_t)w16) & 7) == 0);
+    if (w16 && w16t && (long long)rows * cols == n && cols % 4 == 0 && aligned) {
+        const long long tiles = (long long)((rows + 7) / 8) * ((cols + 127) / 128);
         k_mlp_adam_t<<<(unsigned)tiles, 256, 0, stream>>>(partials, nsplit, grad_direct, w, m, v, lr, b1, b2, eps, bc1,
                                                          bc2, rows, cols, w16, w16t, hyper);
         return cudaGetLastError();

@@ -385,7 +385,12 @@ class WavefrontSurrogate:
         total = epochs * steps_per_epoch
         perm = torch.empty((steps_per_epoch, batch), dtype=torch.int64, device=dev)
         k_in_epoch = torch.zeros(1, dtype=torch.int64, device=dev)
-        gstep = torch.zeros(1, dtype=torch.float64, device=dev)
+        step = torch.zeros(1, dtype=torch.int64, device=dev)
+        # {lr, bc1, bc2} of every step, as the launch-by-launch path computes them
+        g = np.arange(max(total, 1), dtype=np.float64)
+        table = np.stack([lr_min + 0.5 * (lr - lr_min) * (1.0 + np.cos(np.pi * g / max(total, 1))),
+                          1.0 - b1 ** (g + 1), 1.0 - b2 ** (g + 1)], axis=1).astype(np.float32)
+        table_d = torch.from_numpy(table.ravel()).to(dev)
         hyper = torch.empty(3, dtype=torch.float32, device=dev)
         xb = torch.empty((batch, x_all.shape[1]), dtype=torch.float32, device=dev)
         tb = torch.empty((batch, t_all.shape[1]), dtype=torch.float32, device=dev)
@@ -394,16 +399,16 @@ class WavefrontSurrogate:
         nxc, ntc = x_all.shape[1], t_all.shape[1]
 
         def body():
-            # minibatch gather, network step, then the device schedule
-            # (learning rate and Adam bias corrections of this step; it
-            # advances both step counters) and Adam
+            # minibatch gather, network step, then this step's learning rate
+            # and Adam bias corrections from the table (advancing both step
+            # counters) and Adam
             _lib.check(L.bt_mlp_gather(perm.data_ptr(), k_in_epoch.data_ptr(), x_all.data_ptr(), nxc, t_all.data_ptr(),
                                        ntc, batch, xb.data_ptr(), tb.data_ptr(), D.stream_ptr()))
             bf = net.pack(xb, batch, True)
             net.forward(bf, batch, True)
             net.backward(bf, batch, tb, batch, err_col=self.J, err_weight=err_weight)
-            _lib.check(L.bt_mlp_schedule(k_in_epoch.data_ptr(), gstep.data_ptr(), hyper.data_ptr(), float(lr),
-                                         float(lr_min), max(total, 1), float(b1), float(b2), D.stream_ptr()))
+            _lib.check(L.bt_mlp_schedule(k_in_epoch.data_ptr(), step.data_ptr(), table_d.data_ptr(), max(total, 1),
+                                         hyper.data_ptr(), D.stream_ptr()))
             net.adam(bf, 0.0, b1=b1, b2=b2, hyper=hyper)
             return bf
 
@@ -475,12 +480,17 @@ class WavefrontSurrogate:
         f = self.guard.flags_device(torch.from_numpy(feat).to(D.device()), torch.from_numpy(grp).to(D.device()))
         return D.to_host(f).astype(bool)
 
-    def calibrate(self, feat, grp, w, coefs, quantile=0.99):
+    def calibrate(self, feat, grp, w, coefs, quantile=0.99, threshold_nm=2.0):
         """Safety factor on the predicted error: the given quantile of
         actual / predicted over a validation set (the samples the vignetting
-        guard does not already send to the trace)."""
+        guard does not already send to the trace).  With a guard, its
+        margins whose crossings do not coincide with errors above
+        threshold_nm on this set are pruned first (VignettingGuard.prune)."""
         pred, err = self.predict(feat, grp, w)
         actual = rms_nm(pred, coefs.reshape(-1, self.J + 1), w)
+        if self.guard is not None:
+            dofs = feat[:, :self.pt.ndof].astype(np.float64) * self.dof_scale
+            self.guard.prune(dofs, grp, actual > threshold_nm)
         keep = ~self.guard_flags(feat, grp)
         if not np.any(keep):
             keep[:] = True

@@ -12,10 +12,18 @@ of every (field, wavelength) group once and with each dof stepped both ways
 (central differences), and keeps, per group, the (surface, ray) margins
 that could cross zero inside the dof ranges: m(d) = m0 + J d.  A sample is
 flagged when any of its group's kept margins, predicted at its dofs, has
-changed sign or lies within a band of zero (band_abs plus band_rel of the
-predicted change, covering the model's second-order error), or when a dof
+changed sign or lies within a band of zero (band_abs, 1 nm, plus band_rel
+of the predicted change: the model's second-order error scales with the
+change), or when a dof
 lies outside the ranges the margins were chosen for
 (``bt_surrogate_guard``, one warp per sample on the device).
+
+Not every crossing matters: a grid ray that sits on an aperture edge in the
+nominal state (a grid point at the pupil's rim) flips with nanometre
+motions in almost every state, and the training data already sample both
+of its states.  ``prune`` drops the margins whose crossings, over a
+validation set, almost never coincide with a surrogate error above the
+threshold, as the error head's safety factor is calibrated on the same set.
 
 Margins follow the obscuration tree: a circle obscures its inside (margin
 r - R), an annulus obscures inner <= r < outer (margin max(inner - r,
@@ -81,7 +89,7 @@ class VignettingGuard:
     selection (defaults: 1 for rigid dofs, uniform on [-1, 1]; 5 for
     bending amplitudes, Gaussian with unit sigma)."""
 
-    def __init__(self, pt, wavelengths, nx, dof_scale, reach=None, band_abs=5e-6, band_rel=0.05, widen=1.2):
+    def __init__(self, pt, wavelengths, nx, dof_scale, reach=None, band_abs=1e-9, band_rel=0.05, widen=1.2):
         self.pt = pt
         self.wavelengths = np.asarray(wavelengths, dtype=float)
         self.nx = int(nx)
@@ -164,11 +172,51 @@ class VignettingGuard:
         return self.m0[group] + np.einsum('sd,sdk->sk', z, self.jac[group])
 
     # -- device side ----------------------------------------------------------------------
+    def hits(self, dofs, group):
+        """(S, K) bool: which kept margins of each sample's group trigger the
+        rule (sign change or within the band of the edge)."""
+        m = self.predict(dofs, group)
+        m0 = self.m0[group]
+        used = np.isfinite(m0)
+        side = np.where(m0 >= 0, m, -m)
+        with np.errstate(invalid="ignore"):
+            return used & (side < self.band_abs + self.band_rel * np.abs(np.where(used, m - m0, 0.0)))
+
+    def flags_host(self, dofs, group):
+        """The device rule evaluated on the host in FP64 (for checks)."""
+        z = np.asarray(dofs, dtype=float) / self.dof_scale
+        out_box = np.any(np.abs(z) > self.reach, axis=1)
+        return np.any(self.hits(dofs, group), axis=1) | out_box
+
+    def prune(self, dofs, group, bad, min_bad_frac=0.1, min_hits=8):
+        """Drops the kept margins whose triggers, over validation samples
+        (dofs (S, ndof), group (S,), bad (S,) bool: surrogate error above
+        the threshold), coincide with an error in fewer than min_bad_frac of
+        at least min_hits samples.  Returns the number dropped."""
+        h = self.hits(dofs, group)
+        bad = np.asarray(bad, dtype=bool)
+        dropped = 0
+        for g in range(self.G):
+            sel = group == g
+            if not np.any(sel):
+                continue
+            hg, bg = h[sel], bad[sel]
+            for k in range(int(self.nkept[g])):
+                n = int(hg[:, k].sum())
+                if n >= min_hits and np.mean(bg[hg[:, k]]) < min_bad_frac and np.isfinite(self.m0[g, k]):
+                    self.m0[g, k] = np.inf
+                    self.jac[g, :, k] = 0.0
+                    dropped += 1
+        self.dropped = getattr(self, "dropped", 0) + dropped
+        self._dev = None
+        return dropped
+
     def _device(self):
+        import torch
         if self._dev is None:
             m0 = np.where(np.isfinite(self.m0), self.m0, np.float32(3e38)).astype(np.float32)
-            self._dev = (D.to_device(m0.ravel()), D.to_device(self.jac.astype(np.float32).ravel()),
-                         D.to_device(self.reach.astype(np.float32)))
+            f32 = (lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32).ravel()).to(D.device()))
+            self._dev = (f32(m0), f32(self.jac), f32(self.reach))
         return self._dev
 
     def flags_device(self, feat_d, grp_d, out=None):

@@ -741,6 +741,7 @@ def bench_surrogate(bt, train_samples=2_000_000, heldout_states=7282, epochs=24,
         "vignetting_guard": None if guard is None else {
             "flagged_fraction": float(np.mean(gfl)), "fallback_by_error_head_only": float(np.mean(perr > threshold_nm)),
             "kept_margins_per_group_max": int(guard.nkept.max()),
+            "pruned_margins": int(getattr(guard, "dropped", 0)),
             "kept_margins_per_group_mean": float(guard.nkept.mean()), "groups": int(guard.G), "build_s": guard_s,
             "flagged_and_above_threshold_raw": int(np.sum(gfl & (e_raw > threshold_nm))),
             "above_threshold_raw": int(np.sum(e_raw > threshold_nm)),

@@ -439,11 +439,12 @@ int bt_surrogate_combine(const float* feat, int nfeat, int nlin, const int* grp,
 int bt_mlp_gather(const long long* perm, const long long* k_in_epoch, const float* x_all, int nxc,
                   const float* t_all, int ntc, int batch, float* xb, float* tb, void* stream);
 
-/* Writes hyper = {lr_min + (lr - lr_min) (1 + cos(pi g / total)) / 2,
- * 1 - b1^(g+1), 1 - b2^(g+1)} for step g = *gstep (from 0), the array
- * bt_mlp_adam_dev reads, then advances *gstep and *k_in_epoch by one. */
-int bt_mlp_schedule(long long* k_in_epoch, double* gstep, float* hyper, double lr, double lr_min, long long total,
-                    double b1, double b2, void* stream);
+/* Copies hyper[0..3) = table[3 g .. 3 g + 3) for step g = *step (clamped
+ * to total - 1): the {learning rate, Adam bias corrections} of each step,
+ * tabulated on the host, into the array bt_mlp_adam_dev reads; then
+ * advances *step and *k_in_epoch by one. */
+int bt_mlp_schedule(long long* k_in_epoch, long long* step, const float* table, long long total, float* hyper,
+                    void* stream);
 
 /* Vignetting guard of the surrogate (no reference counterpart): for sample s
  * in group grp[s], with z = feat[s][0..ndof) (normalised dofs), the kept

@@ -65,3 +65,27 @@ def test_select_constraints():
     assert kept == {(0, 0), (0, 1)}
     s, i = select_constraints(m0, jac, scale=np.array([1.0, 3.0]), widen=1.2, band_abs=0.0)
     assert (1, 4) in set(zip(s.tolist(), i.tolist()))
+
+
+def test_guard_prune_drops_margins_without_errors():
+    """prune keeps a margin whose triggers coincide with errors and drops one
+    that triggers on every sample without them (a ray on an aperture edge)."""
+    from batoid_gb300.vignetting import VignettingGuard
+    g = VignettingGuard.__new__(VignettingGuard)
+    g.G, g.K = 1, 32
+    g.dof_scale = np.ones(2)
+    g.band_abs, g.band_rel = 1e-6, 0.05
+    g.m0 = np.full((1, 32), np.inf)
+    g.jac = np.zeros((1, 2, 32))
+    g.m0[0, 0], g.jac[0, 0, 0] = 1e-3, -1e-3     # crosses when z0 > 1
+    g.m0[0, 1], g.jac[0, 1, 1] = 1e-9, 1e-9      # on the edge: triggers always
+    g.nkept = np.array([2])
+    g._dev = None
+    rng = np.random.default_rng(0)
+    dofs = rng.uniform(-1.5, 1.5, (400, 2))
+    group = np.zeros(400, dtype=int)
+    h = g.hits(dofs, group)
+    assert h[:, 1].mean() > 0.3 and 0 < h[:, 0].mean() < 0.5
+    bad = dofs[:, 0] > 1.35  # 5 % of the samples, all past the crossing of margin 0
+    assert g.prune(dofs, group, bad) == 1
+    assert np.isfinite(g.m0[0, 0]) and np.isinf(g.m0[0, 1])
