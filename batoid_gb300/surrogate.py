@@ -58,13 +58,16 @@ class MLP:
                 w *= 0.1
                 w[n_out:, :] = 0.0
             self.W.append(torch.from_numpy(w).to(D.device()))
-            self.b.append(_f32(o, zero=True))
             self.W16.append(self.W[-1].to(torch.bfloat16).contiguous())
             self.W16t.append(self.W[-1].t().contiguous().to(torch.bfloat16))
             self.mW.append(_f32((o, i), zero=True))
             self.vW.append(_f32((o, i), zero=True))
-            self.mb.append(_f32(o, zero=True))
-            self.vb.append(_f32(o, zero=True))
+        # biases, their moments (and, per buffer set, their gradients) are
+        # views of one flat array each: one Adam launch updates all biases
+        self._boff = [0] + [int(x) for x in np.cumsum([o for o, _ in self.shapes])]
+        self.b_flat, self.mb_flat, self.vb_flat = (_f32(self._boff[-1], zero=True) for _ in range(3))
+        self.b, self.mb, self.vb = ([f[self._boff[l]:self._boff[l + 1]] for l in range(len(self.shapes))]
+                                    for f in (self.b_flat, self.mb_flat, self.vb_flat))
         self.step_count = 0
         self._bufs = {}
 
@@ -81,7 +84,8 @@ class MLP:
                 bf["h16t"] = [_bf16((H, B)) for _ in range(self.layers)]
                 bf["dz"] = [_bf16((B, H)) for _ in range(self.layers)] + [_bf16((B, PAD))]
                 bf["dzt"] = [_bf16((H, B)) for _ in range(self.layers)] + [_bf16((PAD, B))]
-                bf["db"] = [_f32(o) for o, _ in self.shapes]
+                bf["db_flat"] = _f32(self._boff[-1])
+                bf["db"] = [bf["db_flat"][self._boff[l]:self._boff[l + 1]] for l in range(len(self.shapes))]
                 bf["loss"] = _f32(2, zero=True)
                 splits = [self._splitk(o, i, B) for o, i in self.shapes]
                 bf["splits"] = splits
@@ -154,8 +158,9 @@ class MLP:
                 _lib.check(L.bt_mlp_adam_dev(_p(bf["ws"][l]), bf["splits"][l], None, o * i, _p(self.W[l]),
                                              _p(self.mW[l]), _p(self.vW[l]), _p(hyper), b1, b2, eps, o, i,
                                              _p(self.W16[l]), _p(self.W16t[l]), s))
-                _lib.check(L.bt_mlp_adam_dev(None, 0, _p(bf["db"][l]), o, _p(self.b[l]), _p(self.mb[l]),
-                                             _p(self.vb[l]), _p(hyper), b1, b2, eps, 1, o, None, None, s))
+            nb = self._boff[-1]
+            _lib.check(L.bt_mlp_adam_dev(None, 0, _p(bf["db_flat"]), nb, _p(self.b_flat), _p(self.mb_flat),
+                                         _p(self.vb_flat), _p(hyper), b1, b2, eps, 1, nb, None, None, s))
             return
         self.step_count += 1
         bc1 = 1.0 - b1 ** self.step_count
@@ -164,8 +169,9 @@ class MLP:
             _lib.check(L.bt_mlp_adam(_p(bf["ws"][l]), bf["splits"][l], None, o * i, _p(self.W[l]), _p(self.mW[l]),
                                      _p(self.vW[l]), lr, b1, b2, eps, bc1, bc2, o, i, _p(self.W16[l]),
                                      _p(self.W16t[l]), s))
-            _lib.check(L.bt_mlp_adam(None, 0, _p(bf["db"][l]), o, _p(self.b[l]), _p(self.mb[l]), _p(self.vb[l]), lr,
-                                     b1, b2, eps, bc1, bc2, 1, o, None, None, s))
+        nb = self._boff[-1]
+        _lib.check(L.bt_mlp_adam(None, 0, _p(bf["db_flat"]), nb, _p(self.b_flat), _p(self.mb_flat), _p(self.vb_flat),
+                                 lr, b1, b2, eps, bc1, bc2, 1, nb, None, None, s))
 
     def gradients(self, bf):
         """(dW, db) lists as host arrays (split-K partials summed)."""
