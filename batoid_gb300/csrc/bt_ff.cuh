@@ -54,16 +54,34 @@ __device__ __forceinline__ const ff* ff_ptr(const double* pool, int off) {
 }
 
 // Horner in one variable: sum_{i<n} c[i] x^i.
-__device__ __forceinline__ ff ff_horner(ff x, const ff* c, int n) {
+__device__ __forceinline__ ff ff_horner_serial(ff x, const ff* c, int n) {
     ff r{0.f, 0.f};
     for (int i = n - 1; i >= 0; i--) r = ff_fma(r, x, c[i]);
     return r;
 }
 
+// The same as E(x^2) + x O(x^2) (even and odd coefficients): two
+// independent Horner chains in x^2, half the dependent steps of one chain.
+// The float-float chains are latency-bound, so the second chain is nearly
+// free.  Rounding differs from the single chain at the ~1e-14 relative
+// level of float-float arithmetic.
+__device__ __forceinline__ ff ff_horner(ff x, const ff* c, int n) {
+    if (n < 4) return ff_horner_serial(x, c, n);
+    const ff x2 = ff_mul(x, x);
+    ff e{0.f, 0.f}, o{0.f, 0.f};
+    int i = n - 1;
+    if ((i & 1) == 0) e = c[i--];
+    for (; i >= 1; i -= 2) {
+        o = ff_fma(o, x2, c[i]);
+        e = ff_fma(e, x2, c[i - 1]);
+    }
+    return ff_fma(o, x, e);
+}
+
 // 2-D Horner with the reference's layout (row i: polynomial in y for x^i).
 __device__ __forceinline__ ff ff_horner2d(ff x, ff y, const ff* c, int nx, int ny) {
     ff r{0.f, 0.f};
-    for (int i = ny - 1; i >= 0; i--) r = ff_fma(r, x, ff_horner(y, c + i * nx, nx));
+    for (int i = ny - 1; i >= 0; i--) r = ff_fma(r, x, ff_horner_serial(y, c + i * nx, nx));
     return r;
 }
 
@@ -71,17 +89,45 @@ __device__ __forceinline__ ff ff_horner2d(ff x, ff y, const ff* c, int nx, int n
 // with i + j >= K zero, as the Cartesian form of a Zernike sum): row i is
 // evaluated over its K - i leading columns only.  The skipped terms are
 // exact zeros, so the value is the full Horner's.
+// Rows are taken in pairs (i, i - 1) whose Horner chains run interleaved in
+// one loop (two independent dependency chains); every row and the outer
+// recurrence are evaluated exactly as one row at a time would, so the value
+// is unchanged.
 __device__ __forceinline__ ff ff_horner2d_tri(ff x, ff y, const ff* c, int K) {
     ff r{0.f, 0.f};
-    for (int i = K - 1; i >= 0; i--) r = ff_fma(r, x, ff_horner(y, c + i * K, K - i));
+    int i = K - 1;
+    for (; i >= 1; i -= 2) {
+        const int L = K - i;  // row i has L columns, row i - 1 has L + 1
+        const ff* ca = c + i * K;
+        const ff* cb = c + (i - 1) * K;
+        ff a{0.f, 0.f}, b = cb[L];
+        for (int j = L - 1; j >= 0; j--) {
+            a = ff_fma(a, y, ca[j]);
+            b = ff_fma(b, y, cb[j]);
+        }
+        r = ff_fma(ff_fma(r, x, a), x, b);
+    }
+    if (i == 0) r = ff_fma(r, x, ff_horner_serial(y, c, K));
     return r;
 }
 
 __device__ __forceinline__ float f_horner2d_tri(float x, float y, const ff* c, int K) {
     float r = 0.f;
-    for (int i = K - 1; i >= 0; i--) {
+    int i = K - 1;
+    for (; i >= 1; i -= 2) {
+        const int L = K - i;
+        const ff* ca = c + i * K;
+        const ff* cb = c + (i - 1) * K;
+        float a = 0.f, b = cb[L].hi;
+        for (int j = L - 1; j >= 0; j--) {
+            a = fmaf(a, y, ca[j].hi);
+            b = fmaf(b, y, cb[j].hi);
+        }
+        r = fmaf(fmaf(r, x, a), x, b);
+    }
+    if (i == 0) {
         float row = 0.f;
-        for (int j = K - 1 - i; j >= 0; j--) row = fmaf(row, y, c[i * K + j].hi);
+        for (int j = K - 1; j >= 0; j--) row = fmaf(row, y, c[j].hi);
         r = fmaf(r, x, row);
     }
     return r;
