@@ -191,10 +191,25 @@ __device__ __forceinline__ ff ff_sqr(ff a) {
 // a * b + c.
 __device__ __forceinline__ ff ff_mad(ff a, ff b, ff c) { return ff_add(ff_mul(a, b), c); }
 
+// Hardware approximations (PTX rcp.approx / sqrt.approx, relative error of
+// a few 2^-23): starting points of the float-float corrections below, whose
+// result error is then of the order of the square of the starting error.
+__device__ __forceinline__ float f_rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ float f_sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // a / b: a quotient estimate from the high parts, one correction from the
 // float-float remainder a - q b.
 __device__ __forceinline__ ff ff_div(ff a, ff b) {
-    const float r = __frcp_rn(b.hi);
+    const float r = f_rcp_approx(b.hi);
     const float q1 = a.hi * r;
     // a - q1 * b, with the product q1 * b.hi exact
     const float p = q1 * b.hi;
@@ -207,10 +222,10 @@ __device__ __forceinline__ ff ff_div(ff a, ff b) {
 
 // sqrt(a) (NaN for a < 0, 0 for 0): the FP32 root and one correction.
 __device__ __forceinline__ ff ff_sqrt(ff a) {
-    const float s = sqrtf(a.hi);
+    const float s = f_sqrt_approx(a.hi);
     if (!(a.hi > 0.f)) return ff{s, 0.f};
     const float e = fmaf(-s, s, a.hi) + a.lo;
-    const float c = e * (0.5f / s);
+    const float c = e * (0.5f * f_rcp_approx(s));
     const float h = s + c;
     return ff{h, c - (h - s)};
 }

@@ -438,7 +438,7 @@ __device__ __forceinline__ bool ff_newton_iter_in(const Prog& P, int si, ff x, f
         float ux, uy, qx, qy;
         ffs_eval(P, si, px, py, &zc, zp, &ux, &uy, &qx, &qy);
         const ff res = ff_sub(ff_add(zc, *zp), pz);
-        *inv_den = 1.f / fmaf(ux, fvx, fmaf(uy, fvy, fvz));
+        *inv_den = f_rcp_approx(fmaf(ux, fvx, fmaf(uy, fvy, fvz)));
         const ff ddt = ff_mul_f(res, *inv_den);
         *dt = ff_add(*dt, ddt);
         if (fabsf(ddt.hi) < 1e-7f) {
@@ -586,7 +586,7 @@ static __device__ __noinline__ double ff_refine64(const Prog& P, int si, const R
     float ux, uy;
     ffs_eval(P, si, ff_mad(L.vx, dt, L.x), ff_mad(L.vy, dt, L.y), &zc, &zp, &ux, &uy);
     const double res = ffs_conic64(P, si, px, py) - pz;
-    if (d_abs_lt(res, 1e-9)) dtd += res * f2d_bits(1.f / fmaf(ux, L.vx.hi, fmaf(uy, L.vy.hi, L.vz.hi)));
+    if (d_abs_lt(res, 1e-9)) dtd += res * f2d_bits(f_rcp_approx(fmaf(ux, L.vx.hi, fmaf(uy, L.vy.hi, L.vz.hi))));
     return dtd;
 }
 
