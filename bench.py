@@ -157,9 +157,13 @@ def cpu_baseline(workload, target_s=12.0):
         r, d, _ = time_cpu(workload, n, threads)
         rates.append(r)
         spent += d
+    # one thread, on a sample of about 2 s
+    n1 = max(1 << 12, int(n * 2.0 / (dt * threads)))
+    r1, d1, _ = time_cpu(workload, n1, 1)
     return {"value": statistics.median(rates), "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{workload}: {n} rays x {len(rates)} repeats ({spent:.1f} s of CPU trace), "
-                      f"oracle C restatement of the reference trace, OpenMP {threads} threads"}
+                      f"oracle C restatement of the reference trace, OpenMP {threads} threads",
+            "one_thread": {"value": r1, "unit": UNIT, "cores": 1, "sample": f"{n1} rays, {d1:.1f} s"}}
 
 
 def run_reference(args):
