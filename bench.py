@@ -232,7 +232,7 @@ def measured_peaks():
         return {}
 
 
-def host_trace_e2e(L, _lib, prog, arrs, n, niter, steps, sp, chunk=1 << 20):
+def host_trace_e2e(L, _lib, prog, arrs, n, niter, steps, sp, chunk=1 << 19):
     """The trace through the C-ABI host-buffer entry point (bt_optic_trace_host):
     pinned host arrays in, results back in them; host clock around each call.
     Returns (ms per call, h2d bytes, d2h bytes)."""
@@ -308,10 +308,10 @@ def bench_paraboloid(bt, fp64_peak, n=1_000_000, reps=20, cpu=True):
         ach = fpr * n / (ms * 1e-3) / 1e12
         out["fp64"] = {"executed_flops_per_ray": fpr, "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
                        "frac": ach / fp64_peak}
-    e2e_ms, h2d, d2h = host_trace_e2e(L, _lib, prog, arrs, n, niter, 5, sp, chunk=1 << 19)
+    e2e_ms, h2d, d2h = host_trace_e2e(L, _lib, prog, arrs, n, niter, 5, sp, chunk=1 << 18)
     out["e2e"] = {"value": n * nsurf / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                   "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
-                  "path": "bt_optic_trace_host, pinned host arrays, 512k-ray chunks on 3 streams"}
+                  "path": "bt_optic_trace_host, pinned host arrays, 256k-ray chunks on 3 streams"}
     if cpu:
         ora, copt, make_rays, _ = cpu_workload("paraboloid")
         pristine = ora.Rays(*make_rays(n, seed=57721))
@@ -892,7 +892,7 @@ def run_gpu(args):
                                  "frac": hbm_gbs / hbm_peak, "bytes_per_ray": bytes_per_ray,
                                  "peak_source": "MEASURED_PEAKS.json hbm_gbs"}},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": e2e_ms, "path": "bt_optic_trace_host, pinned host arrays, 1M-ray chunks on 3 streams"},
+                    "ms_per_step": e2e_ms, "path": "bt_optic_trace_host, pinned host arrays, 512k-ray chunks on 3 streams"},
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": args.steps,
