@@ -60,3 +60,26 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--gpus", "2"])
     bench.run_reference(bench.parse())   # returns before any CPU work
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_loads_no_product_library():
+    """The reference arm (the oracle's restatement of the reference trace on
+    the host cores) imports nothing of the product package and maps none of
+    its libraries; its line is the contract's, with impl "reference"."""
+    import json
+    import subprocess
+    code = ("import sys, json, io, contextlib; sys.argv = ['bench.py', '--impl', 'reference', '--nrays', '4096', "
+            "'--steps', '1', '--warmup', '1']; import bench; buf = io.StringIO()\n"
+            "with contextlib.redirect_stdout(buf): bench.main()\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print(json.dumps({'line': buf.getvalue().strip().splitlines()[-1], "
+            "'imported': [m for m in sys.modules if m.startswith('batoid_gb300')], "
+            "'mapped': 'libbatoid_gb300' in maps}))")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    rep = json.loads(out.stdout.strip().splitlines()[-1])
+    assert rep["imported"] == [] and not rep["mapped"]
+    line = json.loads(rep["line"])
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port"
+    assert line["e2e"]["h2d_bytes_per_step"] == 0
