@@ -50,6 +50,10 @@ def parse():
     p.add_argument("--no-guard", action="store_true", help="surrogate without the vignetting guard")
     p.add_argument("--surrogate-samples", type=int, default=2_000_000)
     p.add_argument("--surrogate-epochs", type=int, default=24)
+    p.add_argument("--per-stage", type=int, default=None, metavar="REPS",
+                   help="instead of the bench line: the workload's optic truncated after each interface, one "
+                        "untimed launch each, then REPS timed ones (0: the single launch only, for an ncu census "
+                        "of one launch per truncation); prints one JSON line of per-interface times")
     return p.parse_args()
 
 
@@ -906,10 +910,59 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_per_stage(args):
+    """Cost of each interface of the workload's optic: the optic truncated
+    after interface k (k = 1..N), traced out of place on the workload's
+    rays; the difference of consecutive truncations is interface k's time
+    (the first also carries the kernel's ray loads and stores)."""
+    import torch
+    import batoid_gb300 as bt
+    from batoid_gb300 import _lib, workloads as W
+    build_optic, make_rays, _ = W.WORKLOADS[args.workload]
+    opt = build_optic(bt)
+
+    def leaves(o):
+        return [x for it in o.items for x in leaves(it)] if hasattr(o, "items") else [o]
+
+    ifs = leaves(opt)
+    n = args.nrays
+    rv_in = bt.RayVector(*make_rays(n, seed=4242))
+    rv_out = bt.RayVector._empty(n)
+    L = _lib.lib()
+    stream = torch.cuda.current_stream()
+    niter = bt.global_vars._batoid_niter
+    rows, prev = [], 0.0
+    for k in range(1, len(ifs) + 1):
+        sub = bt.CompoundOptic(ifs[:k], name=f"first_{k}", inMedium=opt.inMedium, outMedium=opt.outMedium)
+        prog = sub._program(rv_in.coordSys)
+
+        def step():
+            _lib.check(L.bt_optic_trace_into(prog._optic.ptr, rv_in._rv, rv_out._rv, niter, stream.cuda_stream))
+
+        step()
+        torch.cuda.synchronize()
+        ms = None
+        if args.per_stage > 0:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.per_stage):
+                step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.per_stage
+        rows.append({"interface": ifs[k - 1].name, "surface": type(ifs[k - 1].surface).__name__,
+                     "ms_through": ms, "ms_interface": None if ms is None else ms - prev})
+        prev = ms or 0.0
+    print(json.dumps({"per_stage": rows, "workload": args.workload, "rays": n, "reps": args.per_stage}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.per_stage is not None:
+        run_per_stage(args)
     else:
         run_gpu(args)
 
