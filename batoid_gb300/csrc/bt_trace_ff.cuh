@@ -409,8 +409,14 @@ static __device__ __noinline__ RootF ff_analytic_o(const bt_surf& s, const doubl
     return o;
 }
 
+// (A plane's root inline: the call would cost more than the root.)
 __device__ __forceinline__ bool ff_analytic(const bt_surf& s, const double* pool, ff x, ff y, ff z, ff vx, ff vy,
                                             ff vz, ff* dt) {
+    if (s.kind == BT_S_PLANE) {
+        if (vz.hi == 0.f) return false;
+        *dt = ff_div(ff_neg(z), vz);
+        return true;
+    }
     const RootF o = ff_analytic_o(s, pool, x, y, z, vx, vy, vz);
     *dt = o.dt;
     return o.ok;
@@ -674,7 +680,14 @@ static __device__ __noinline__ Vec3F ffs_normal_o(const Prog& P, int si, ff x, f
     return o;
 }
 
+// (Plane and sphere normals inline: a few float-float operations, cheaper
+// than the call.)
 __device__ __forceinline__ void ffs_normal(const Prog& P, int si, ff x, ff y, ff* nx, ff* ny, ff* nz) {
+    const bt_surf& s = P.surfs[si];
+    if (s.kind == BT_S_PLANE || s.kind == BT_S_SPHERE) {
+        ffs_normal_in(P, si, x, y, nx, ny, nz);
+        return;
+    }
     const Vec3F o = ffs_normal_o(P, si, x, y);
     *nx = o.x;
     *ny = o.y;
