@@ -965,6 +965,28 @@ __device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, 
             fx = fc.ok ? fc.x : d_to_ff(r.x);
             fy = fc.ok ? fc.y : d_to_ff(r.y);
         }
-        if (ff_obsc_run(P, st.obsc_begin, st.obsc_end, fx, fy, r.x, r.y)) r.vig = true;
+        // the common clear aperture, NOT(circle or annulus about the axis),
+        // decided inline when the FP32 test is clear (ff_radius_less's first
+        // step); everything else by the out-of-line postfix program
+        int fast = -1;  // -1: not decided here; 0 / 1: obscured or not
+        if (st.obsc_end - st.obsc_begin == 2) {
+            const bt_obsc& o = P.obsc[st.obsc_begin];
+            if (P.obsc[st.obsc_begin + 1].op == BT_O_NEGATION) {
+                const float h2f = fmaf(fx.hi, fx.hi, fy.hi * fy.hi);
+                if (o.op == BT_O_CIRCLE && !d_nonzero(o.p[1]) && !d_nonzero(o.p[2]) && o.p[0] > 0.0) {
+                    const float rf = ff_slot(&o.p[3]).hi, r2f = rf * rf;
+                    if (h2f < r2f * (1.f - 1e-5f)) fast = 0;          // inside the circle: clear
+                    else if (h2f > r2f * (1.f + 1e-5f)) fast = 1;     // outside: obscured
+                } else if (o.op == BT_O_ANNULUS && !d_nonzero(o.p[2]) && !d_nonzero(o.p[3]) && o.p[0] > 0.0 &&
+                           o.p[1] > 0.0) {
+                    const float ri = ff_slot(&o.p[4]).hi, ro = ff_slot(&o.p[5]).hi;
+                    const float ri2 = ri * ri, ro2 = ro * ro;
+                    if (h2f > ri2 * (1.f + 1e-5f) && h2f < ro2 * (1.f - 1e-5f)) fast = 0;  // in the annulus
+                    else if (h2f < ri2 * (1.f - 1e-5f) || h2f > ro2 * (1.f + 1e-5f)) fast = 1;
+                }
+            }
+        }
+        if (fast < 0) fast = ff_obsc_run(P, st.obsc_begin, st.obsc_end, fx, fy, r.x, r.y) ? 1 : 0;
+        if (fast) r.vig = true;
     }
 }
