@@ -923,12 +923,22 @@ __device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, 
                         nx_ = ff_neg(nx_); ny_ = ff_neg(ny_); nz_ = ff_neg(nz_);
                         alpha = ff_neg(alpha);
                     }
+                    // 1/n2: a constant medium's from its record; others
+                    // cached per ray (a lens's glass between its faces'
+                    // vacuum gaps is evaluated once)
                     const int mi = st.medium;
-                    if (mi != mc.idx) {
-                        ff_medium(P, mi, r.w, &mc.n, &mc.inv_n);
-                        mc.idx = mi;
+                    const bt_medium& md = P.media[mi];
+                    ff inv_n2;
+                    if (md.kind == BT_M_CONST) {
+                        inv_n2 = ff_slot(&md.p[3]);
+                    } else {
+                        if (mi != mc.idx) {
+                            ff_medium(P, mi, r.w, &mc.n, &mc.inv_n);
+                            mc.idx = mi;
+                        }
+                        inv_n2 = mc.inv_n;
                     }
-                    const ff eta = ff_mul(n1, mc.inv_n);
+                    const ff eta = ff_mul(n1, inv_n2);
                     const ff sinsqr = ff_mul(ff_sqr(eta), ff_sub(ff_one(), ff_sqr(alpha)));
                     if (sinsqr.hi > 1.f || (sinsqr.hi == 1.f && sinsqr.lo > 0.f)) {
                         vx = NAN; vy = NAN; vz = NAN;
@@ -937,8 +947,8 @@ __device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, 
                     } else {
                         // (eta v^ - (eta alpha + cos) n) / n2
                         const ff cosr = ff_sqrt(ff_sub(ff_one(), sinsqr));
-                        const ff a = ff_mul(eta, mc.inv_n);
-                        const ff b = ff_mul(ff_add(ff_mul(eta, alpha), cosr), mc.inv_n);
+                        const ff a = ff_mul(eta, inv_n2);
+                        const ff b = ff_mul(ff_add(ff_mul(eta, alpha), cosr), inv_n2);
                         fc.vx = ff_sub(ff_mul(a, nvx), ff_mul(b, nx_));
                         fc.vy = ff_sub(ff_mul(a, nvy), ff_mul(b, ny_));
                         fc.vz = ff_sub(ff_mul(a, nvz), ff_mul(b, nz_));
