@@ -983,12 +983,14 @@ __device__ __forceinline__ void run_stage_ff(const Prog& P, const bt_stage& st, 
             const bt_obsc& o = P.obsc[st.obsc_begin];
             if (P.obsc[st.obsc_begin + 1].op == BT_O_NEGATION) {
                 const float h2f = fmaf(fx.hi, fx.hi, fy.hi * fy.hi);
-                if (o.op == BT_O_CIRCLE && !d_nonzero(o.p[1]) && !d_nonzero(o.p[2]) && o.p[0] > 0.0) {
+                // (positive radii tested on the integer pipe, as ff_radius_less)
+                if (o.op == BT_O_CIRCLE && !d_nonzero(o.p[1]) && !d_nonzero(o.p[2]) &&
+                    __double_as_longlong(o.p[0]) > 0) {
                     const float rf = ff_slot(&o.p[3]).hi, r2f = rf * rf;
                     if (h2f < r2f * (1.f - 1e-5f)) fast = 0;          // inside the circle: clear
                     else if (h2f > r2f * (1.f + 1e-5f)) fast = 1;     // outside: obscured
-                } else if (o.op == BT_O_ANNULUS && !d_nonzero(o.p[2]) && !d_nonzero(o.p[3]) && o.p[0] > 0.0 &&
-                           o.p[1] > 0.0) {
+                } else if (o.op == BT_O_ANNULUS && !d_nonzero(o.p[2]) && !d_nonzero(o.p[3]) &&
+                           __double_as_longlong(o.p[0]) > 0 && __double_as_longlong(o.p[1]) > 0) {
                     const float ri = ff_slot(&o.p[4]).hi, ro = ff_slot(&o.p[5]).hi;
                     const float ri2 = ri * ri, ro2 = ro * ro;
                     if (h2f > ri2 * (1.f + 1e-5f) && h2f < ro2 * (1.f - 1e-5f)) fast = 0;  // in the annulus
