@@ -33,6 +33,7 @@ struct SnapSet {
 cudaError_t bt_read_device_status(int* status, cudaStream_t stream);
 cudaError_t bt_read_split_device_status(int* status, cudaStream_t stream);
 cudaError_t bt_read_trace_ff_device_status(int* status, cudaStream_t stream);
+long long bt_trace_ff_round_rays();
 
 // trace_ff.cu: the float-float form of the fused trace
 cudaError_t bt_launch_trace_ff(const unsigned char* d_blob, int blob_bytes, const RV& in, const RV& out,

@@ -1168,6 +1168,12 @@ extern "C" int bt_optic_trace_host(const bt_optic* oc, const bt_rayvector* h, in
     int rc = check_rv(h);
     if (rc != BT_OK || h->size == 0) return rc;
     if (chunk == 0) chunk = (size_t)1 << 22;
+    {
+        // whole rounds of the persistent grid per chunk (and per eighth of
+        // one, the pieces the first and last buffers are filled in)
+        const size_t round8 = (size_t)bt_trace_ff_round_rays() * 8;
+        if (round8 > 0 && chunk >= round8) chunk = (chunk + round8 / 2) / round8 * round8;
+    }
     if (chunk > h->size) chunk = h->size;
     std::lock_guard<std::mutex> lock(o->mu);
     const size_t bytes = chunk * (9 * sizeof(double) + 2);

@@ -74,6 +74,9 @@ k_trace_ff(const unsigned char* __restrict__ gblob, int blob_bytes, RV in, RV ou
     }
 }
 
+// Rays one launch of the persistent grid takes per round.
+long long bt_trace_ff_round_rays() { return (long long)bt_sm_count() * TRACE_FF_MINB * TRACE_FF_THREADS; }
+
 cudaError_t bt_launch_trace_ff(const unsigned char* d_blob, int blob_bytes, const RV& in, const RV& out,
                                const SnapSet* snaps, int nsnaps, int niter, cudaStream_t stream) {
     if (in.n <= 0) return cudaSuccess;

@@ -239,8 +239,10 @@ int bt_optic_trace_into(const bt_optic* o, const bt_rayvector* in, const bt_rayv
 int bt_optic_trace_full(const bt_optic* o, const bt_rayvector* rv, const bt_rayvector* snaps,
                         int niter, void* stream);
 /* End-to-end trace of HOST arrays (pinned for overlap): copies in, traces
- * and copies out, pipelined in chunks of `chunk` rays over device scratch
- * buffers that the library allocates.  Synchronous. */
+ * and copies out, pipelined in chunks of about `chunk` rays (0: 4M) over
+ * device scratch buffers that the library allocates; a chunk of at least
+ * 8 rounds of the trace kernel's persistent grid is rounded to a whole
+ * number of 8 rounds.  Synchronous. */
 int bt_optic_trace_host(const bt_optic* o, const bt_rayvector* host_rv, int niter, size_t chunk,
                         void* stream);
 
