@@ -337,6 +337,29 @@ struct RootF {
     bool ok;
 };
 
+__device__ __forceinline__ RootF ff_quadric_root_inl(const double* C, ff x, ff y, ff z, ff vx, ff vy, ff vz) {
+    RootF o;
+    o.ok = false;
+    ff* dt = &o.dt;
+    const ff icp1 = ff_slot(C + 1);
+    const ff z0 = ff_sub(z, ff_slot(C + 2));
+    const ff vrr0 = ff_add(ff_mul(vx, x), ff_mul(vy, y));
+    const ff a = ff_add(ff_sqr(vz), ff_mul(ff_r2(vx, vy), icp1));
+    const ff b = ff_mul_f(ff_add(ff_mul(vz, z0), ff_mul(vrr0, icp1)), 2.f);
+    const ff c = ff_add(ff_sub(ff_sqr(z0), ff_slot(C + 3)), ff_mul(ff_r2(x, y), icp1));
+    const ff disc = ff_sub(ff_sqr(b), ff_mul_f(ff_mul(a, c), 4.f));
+    if (disc.hi < 0.f) return o;
+    const ff s = ff_sqrt(disc);
+    const ff mb = ff_neg(b);
+    const ff r1 = (b.hi > 0.f) ? ff_div(ff_sub(mb, s), ff_mul_f(a, 2.f)) : ff_div(ff_mul_f(c, 2.f), ff_add(mb, s));
+    const ff r2 = ff_div(c, ff_mul(a, r1));
+    const ff z1 = ff_mad(vz, r1, z), z2 = ff_mad(vz, r2, z);
+    *dt = ff_lt(ff_abs(z1), ff_abs(z2)) ? r1 : r2;
+    o.ok = true;
+    return o;
+}
+
+
 static __device__ __noinline__ RootF ff_quadric_root_o(const double* C, ff x, ff y, ff z, ff vx, ff vy, ff vz) {
     RootF o;
     o.ok = false;
@@ -521,13 +544,21 @@ static __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const R
         c0 = s.m;
         const bt_surf& first = P.surfs[c0];
         if (first.kind == BT_S_ASPHERE) {
-            if (!ff_quadric_root(P.pool + first.ffc, L.x, L.y, L.z, vx, vy, vz, &t0)) return false;
+            {
+                const RootF q = ff_quadric_root_inl(P.pool + first.ffc, L.x, L.y, L.z, vx, vy, vz);
+                if (!q.ok) return false;
+                t0 = q.dt;
+            }
         } else if (first.kind != BT_S_POLY) {
             if (!ff_analytic(first, P.pool, L.x, L.y, L.z, vx, vy, vz, &t0)) return false;
             child_done = true;
         }
     } else if (s.kind == BT_S_ASPHERE) {
-        if (!ff_quadric_root(P.pool + s.ffc, L.x, L.y, L.z, vx, vy, vz, &t0)) return false;
+        {
+            const RootF q = ff_quadric_root_inl(P.pool + s.ffc, L.x, L.y, L.z, vx, vy, vz);
+            if (!q.ok) return false;
+            t0 = q.dt;
+        }
     }
     // anchor
     const double t0d = ff_to_d(t0);
