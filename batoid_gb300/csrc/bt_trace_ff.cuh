@@ -569,11 +569,11 @@ static __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const R
     float inv_den = 0.f;
     if (c0 >= 0 && !child_done) {
         // the first child's own Newton; it must succeed (src/sum.cpp:47-56)
-        if (!ff_newton_iter(P, c0, ax, ay, az, vx, vy, vz, &d, niter, &zp, &inv_den) &&
+        if (!ff_newton_iter_in(P, c0, ax, ay, az, vx, vy, vz, &d, niter, &zp, &inv_den) &&
             !ff_residual_ok(P, c0, ax, ay, az, vx, vy, vz, d))
             return false;
     }
-    const bool conv = ff_newton_iter(P, si, ax, ay, az, vx, vy, vz, &d, niter, &zp, &inv_den);
+    const bool conv = ff_newton_iter_in(P, si, ax, ay, az, vx, vy, vz, &d, niter, &zp, &inv_den);
     // FP64 residual at the FP64 point x + v dt
     double dtd = t0d + ff_to_d(d);
     const double px = fma(L.vxd, dtd, L.xd), py = fma(L.vyd, dtd, L.yd), pz = fma(L.vzd, dtd, L.zd);
