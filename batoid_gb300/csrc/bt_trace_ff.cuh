@@ -533,6 +533,21 @@ struct RayLocal {
 // p0 = x + v t0 (FP64 FMAs), in the offset d = dt - t0: the residual's terms
 // are then of the size of the sag, not of the distance the ray travelled
 // (15 m before the primary of a telescope), so their rounding (~1e-16 m)
+// Inside the out-of-line Newton solve, the starting quadric root and the
+// Newton loop are inline where BT_FF_INLINE_NEWTON is 1 (the plain trace:
+// measured 4 % faster) and calls elsewhere (the batched kernel, whose
+// Sums with a bending-mode child measured 15 % slower inline).
+#ifndef BT_FF_INLINE_NEWTON
+#define BT_FF_INLINE_NEWTON 0
+#endif
+#if BT_FF_INLINE_NEWTON
+#define BT_FF_QROOT ff_quadric_root_inl
+#define BT_FF_NEWTON ff_newton_iter_in
+#else
+#define BT_FF_QROOT ff_quadric_root_o
+#define BT_FF_NEWTON ff_newton_iter
+#endif
+
 // stays far below the 1e-12 m convergence and success thresholds.
 static __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const RayLocal L, int niter, double* dt_out) {
     const bt_surf& s = P.surfs[si];
@@ -545,7 +560,7 @@ static __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const R
         const bt_surf& first = P.surfs[c0];
         if (first.kind == BT_S_ASPHERE) {
             {
-                const RootF q = ff_quadric_root_inl(P.pool + first.ffc, L.x, L.y, L.z, vx, vy, vz);
+                const RootF q = BT_FF_QROOT(P.pool + first.ffc, L.x, L.y, L.z, vx, vy, vz);
                 if (!q.ok) return false;
                 t0 = q.dt;
             }
@@ -555,7 +570,7 @@ static __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const R
         }
     } else if (s.kind == BT_S_ASPHERE) {
         {
-            const RootF q = ff_quadric_root_inl(P.pool + s.ffc, L.x, L.y, L.z, vx, vy, vz);
+            const RootF q = BT_FF_QROOT(P.pool + s.ffc, L.x, L.y, L.z, vx, vy, vz);
             if (!q.ok) return false;
             t0 = q.dt;
         }
@@ -569,11 +584,11 @@ static __device__ __noinline__ bool ff_newton_tti(const Prog& P, int si, const R
     float inv_den = 0.f;
     if (c0 >= 0 && !child_done) {
         // the first child's own Newton; it must succeed (src/sum.cpp:47-56)
-        if (!ff_newton_iter_in(P, c0, ax, ay, az, vx, vy, vz, &d, niter, &zp, &inv_den) &&
+        if (!BT_FF_NEWTON(P, c0, ax, ay, az, vx, vy, vz, &d, niter, &zp, &inv_den) &&
             !ff_residual_ok(P, c0, ax, ay, az, vx, vy, vz, d))
             return false;
     }
-    const bool conv = ff_newton_iter_in(P, si, ax, ay, az, vx, vy, vz, &d, niter, &zp, &inv_den);
+    const bool conv = BT_FF_NEWTON(P, si, ax, ay, az, vx, vy, vz, &d, niter, &zp, &inv_den);
     // FP64 residual at the FP64 point x + v dt
     double dtd = t0d + ff_to_d(d);
     const double px = fma(L.vxd, dtd, L.xd), py = fma(L.vyd, dtd, L.yd), pz = fma(L.vzd, dtd, L.zd);

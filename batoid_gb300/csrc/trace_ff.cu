@@ -6,6 +6,7 @@
 #include "bt_device.cuh"
 #include "bt_stage_smem.cuh"
 #include "bt_trace_core.cuh"
+#define BT_FF_INLINE_NEWTON 1
 #include "bt_trace_ff.cuh"
 
 #define TRACE_FF_THREADS 256
