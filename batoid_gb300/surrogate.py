@@ -283,46 +283,37 @@ class WavefrontSurrogate:
         r = (coefs.reshape(-1, self.J + 1)[:, 1:] - self.linear(feat, grp)) * w[:, None] * 1e9
         return r
 
-    def _fit_linear_device(self, feat, grp, w, coefs):
-        """fit_linear and residual_targets with the sample-sized work on the
-        device (FP64): samples sorted by group, each group's normal equations
-        A^T A and A^T c by one matrix product, the (ndof+1)-sized systems
-        solved on the host.  Returns the residuals (nm) as a device tensor."""
-        dev = D.device()
+    def _fit_linear_sorted(self, feat, grp, w, coefs):
+        """fit_linear and residual_targets in one pass over the samples
+        sorted by group (contiguous slices instead of a mask per group):
+        each group's normal equations by one FP64 product, the
+        (ndof+1)-sized systems solved directly.  Returns the residuals (nm)
+        as a device tensor."""
         nd = self.pt.ndof
         G = self.F * len(self.wavelengths)
-        n = len(feat)
-        g = torch.from_numpy(np.ascontiguousarray(grp, dtype=np.int64)).to(dev)
-        order = torch.argsort(g, stable=True)
-        counts = torch.bincount(g, minlength=G).cpu().numpy()
-        A = torch.ones((n, nd + 1), dtype=torch.float64, device=dev)
-        A[:, 1:] = torch.from_numpy(np.ascontiguousarray(feat[:, :nd])).to(dev)[order].double()
-        C = torch.from_numpy(np.ascontiguousarray(coefs.reshape(-1, self.J + 1)[:, 1:])).to(dev)[order]
+        order = np.argsort(grp, kind="stable")
+        counts = np.bincount(grp, minlength=G)
         starts = np.concatenate([[0], np.cumsum(counts)])
-        ata = torch.zeros((G, nd + 1, nd + 1), dtype=torch.float64, device=dev)
-        atc = torch.zeros((G, nd + 1, self.J), dtype=torch.float64, device=dev)
-        for k in range(G):
-            if counts[k]:
-                a = A[starts[k]:starts[k + 1]]
-                ata[k] = a.T @ a
-                atc[k] = a.T @ C[starts[k]:starts[k + 1]]
-        ata, atc = ata.cpu().numpy(), atc.cpu().numpy()
+        A = np.empty((len(feat), nd + 1))
+        A[:, 0] = 1.0
+        A[:, 1:] = feat[order, :nd]
+        C = coefs.reshape(-1, self.J + 1)[order, 1:]
         self.theta = np.zeros((G, nd + 1, self.J))
         self._theta_d = None
+        R = np.empty_like(C)
         for k in range(G):
-            if counts[k]:
-                try:
-                    self.theta[k] = np.linalg.solve(ata[k], atc[k])
-                except np.linalg.LinAlgError:
-                    self.theta[k] = np.linalg.lstsq(ata[k], atc[k], rcond=None)[0]
-        th = torch.from_numpy(self.theta).to(dev)
-        for k in range(G):
-            if counts[k]:
-                sl = slice(starts[k], starts[k + 1])
-                C[sl] -= A[sl] @ th[k]
-        r = torch.empty_like(C)
-        r[order] = C * torch.from_numpy(np.ascontiguousarray(w, dtype=np.float64)).to(dev)[order, None] * 1e9
-        return r
+            if not counts[k]:
+                continue
+            sl = slice(starts[k], starts[k + 1])
+            a, c = A[sl], C[sl]
+            try:
+                self.theta[k] = np.linalg.solve(a.T @ a, a.T @ c)
+            except np.linalg.LinAlgError:
+                self.theta[k] = np.linalg.lstsq(a, c, rcond=None)[0]
+            R[sl] = (c - a @ self.theta[k]) * w[order[sl], None] * 1e9
+        r = np.empty_like(R)
+        r[order] = R
+        return torch.from_numpy(r).to(D.device())
 
     def train(self, feat, grp, w, coefs, epochs=30, batch=8192, lr=1e-3, lr_min=1e-5, err_weight=0.05, seed=0,
               log=None, graph=True):
@@ -336,11 +327,11 @@ class WavefrontSurrogate:
 
         Minibatches are drawn from a device permutation per epoch (seeded
         generator).  self.timing afterwards holds the wall time of the
-        linear fit (device products, host solves) and of the network
+        linear fit (host, samples sorted by group) and of the network
         training (device steps)."""
         import time
         t0 = time.perf_counter()
-        r = self._fit_linear_device(feat, grp, w, coefs)
+        r = self._fit_linear_sorted(feat, grp, w, coefs)
         self.scale = float(torch.sqrt(torch.mean(r * r)).item())
         t_all = (r / self.scale).float().contiguous()
         del r
