@@ -540,11 +540,17 @@ struct RayLocal {
 #ifndef BT_FF_INLINE_NEWTON
 #define BT_FF_INLINE_NEWTON 0
 #endif
-#if BT_FF_INLINE_NEWTON
+#ifndef BT_FF_INLINE_QROOT
+#define BT_FF_INLINE_QROOT BT_FF_INLINE_NEWTON
+#endif
+#if BT_FF_INLINE_QROOT
 #define BT_FF_QROOT ff_quadric_root_inl
-#define BT_FF_NEWTON ff_newton_iter_in
 #else
 #define BT_FF_QROOT ff_quadric_root_o
+#endif
+#if BT_FF_INLINE_NEWTON
+#define BT_FF_NEWTON ff_newton_iter_in
+#else
 #define BT_FF_NEWTON ff_newton_iter
 #endif
 
