@@ -735,6 +735,10 @@ static __device__ __noinline__ Vec3F ffs_normal_o(const Prog& P, int si, ff x, f
 // (Plane and sphere normals inline: a few float-float operations, cheaper
 // than the call.)
 __device__ __forceinline__ void ffs_normal(const Prog& P, int si, ff x, ff y, ff* nx, ff* ny, ff* nz) {
+#if BT_FF_INLINE_NEWTON
+    ffs_normal_in(P, si, x, y, nx, ny, nz);
+    return;
+#endif
     const bt_surf& s = P.surfs[si];
     if (s.kind == BT_S_PLANE || s.kind == BT_S_SPHERE) {
         ffs_normal_in(P, si, x, y, nx, ny, nz);
