@@ -1,6 +1,6 @@
-"""Host logic of the surrogate's vignetting guard (batoid_gb300/vignetting.py):
-aperture margins against the oracle's obscuration test, and the choice of
-the margins to keep."""
+"""Host logic of the surrogate: the vignetting guard (batoid_gb300/vignetting.py:
+aperture margins against the oracle's obscuration test, the choice and the
+pruning of the margins to keep) and the linear model's fit."""
 import os
 import sys
 
@@ -89,3 +89,30 @@ def test_guard_prune_drops_margins_without_errors():
     bad = dofs[:, 0] > 1.35  # 5 % of the samples, all past the crossing of margin 0
     assert g.prune(dofs, group, bad) == 1
     assert np.isfinite(g.m0[0, 0]) and np.isinf(g.m0[0, 1])
+
+
+def test_sorted_linear_fit_equals_per_group_fit(monkeypatch):
+    """The surrogate's linear model fitted over samples sorted by group
+    (WavefrontSurrogate._fit_linear_sorted) equals the per-group fit and its
+    residuals (fit_linear, residual_targets) to rounding."""
+    from batoid_gb300 import _device
+    from batoid_gb300.surrogate import WavefrontSurrogate
+    monkeypatch.setattr(_device, "device", lambda: "cpu")
+    rng = np.random.default_rng(3)
+    n, nd, J, G = 4000, 6, 5, 6
+    feat = rng.uniform(-1, 1, (n, nd + 3)).astype(np.float32)
+    grp = rng.integers(0, G, n).astype(np.int32)
+    coefs = np.concatenate([np.zeros((n, 1)), rng.normal(size=(n, J))], axis=1)
+    w = np.full(n, 6e-7)
+
+    class _PT:
+        ndof = nd
+
+    sur = WavefrontSurrogate.__new__(WavefrontSurrogate)
+    sur.pt, sur.F, sur.wavelengths, sur.J = _PT(), G, np.ones(1), J
+    r = sur._fit_linear_sorted(feat, grp, w, coefs).numpy()
+    theta = sur.theta.copy()
+    sur.fit_linear(feat, grp, coefs)
+    r_ref = sur.residual_targets(feat, grp, w, coefs)
+    np.testing.assert_allclose(theta, sur.theta, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(r, r_ref, rtol=0, atol=1e-9 * np.abs(r_ref).max())
