@@ -543,6 +543,9 @@ struct RayLocal {
 #ifndef BT_FF_INLINE_QROOT
 #define BT_FF_INLINE_QROOT BT_FF_INLINE_NEWTON
 #endif
+#ifndef BT_FF_INLINE_NORMAL
+#define BT_FF_INLINE_NORMAL BT_FF_INLINE_NEWTON
+#endif
 #if BT_FF_INLINE_QROOT
 #define BT_FF_QROOT ff_quadric_root_inl
 #else
@@ -735,7 +738,7 @@ static __device__ __noinline__ Vec3F ffs_normal_o(const Prog& P, int si, ff x, f
 // (Plane and sphere normals inline: a few float-float operations, cheaper
 // than the call.)
 __device__ __forceinline__ void ffs_normal(const Prog& P, int si, ff x, ff y, ff* nx, ff* ny, ff* nz) {
-#if BT_FF_INLINE_NEWTON
+#if BT_FF_INLINE_NORMAL
     ffs_normal_in(P, si, x, y, nx, ny, nz);
     return;
 #endif
