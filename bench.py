@@ -40,7 +40,7 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="tma_corrector")
     p.add_argument("--nrays", type=int, default=16 * 1024 * 1024)
-    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-huygens", action="store_true")
     p.add_argument("--no-paraboloid", action="store_true")
@@ -238,14 +238,15 @@ def measured_peaks():
 
 def host_trace_e2e(L, _lib, prog, arrs, n, niter, steps, sp, chunk=1 << 19):
     """The trace through the C-ABI host-buffer entry point (bt_optic_trace_host):
-    pinned host arrays in, results back in them; host clock around each call.
-    Returns (ms per call, h2d bytes, d2h bytes)."""
+    pinned host arrays in, results back in them; host clock around each call
+    (inputs restored between calls, outside the clock).  Returns (median ms
+    per call, h2d bytes, d2h bytes)."""
     import torch
     host = [torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).pin_memory() for x in arrs[:9]]
     hflags = [torch.from_numpy(np.ascontiguousarray(x, dtype=np.uint8)).pin_memory() for x in arrs[9:]]
     pristine = [h.clone() for h in host] + [f.clone() for f in hflags]
     hrv = _lib.BtRayVector(*[h.data_ptr() for h in host], *[f.data_ptr() for f in hflags], n)
-    total = 0.0
+    times = []
     for it in range(1 + steps):
         for dst, src in zip(host + hflags, pristine):
             dst.copy_(src)
@@ -254,8 +255,8 @@ def host_trace_e2e(L, _lib, prog, arrs, n, niter, steps, sp, chunk=1 << 19):
         _lib.check(L.bt_optic_trace_host(prog._optic.ptr, ctypes.byref(hrv), niter, chunk, sp))
         dt = (time.perf_counter() - t1) * 1e3
         if it > 0:
-            total += dt
-    return total / max(steps, 1), n * (9 * 8 + 2), n * (8 * 8 + 2)
+            times.append(dt)
+    return (statistics.median(times) if times else 0.0), n * (9 * 8 + 2), n * (8 * 8 + 2)
 
 
 def bench_paraboloid(bt, fp64_peak, n=1_000_000, reps=20, cpu=True):
